@@ -1,0 +1,342 @@
+"""Benchmark of the closest-point query path on one or more GB300s.
+
+Workload (the 1M-triangle configuration): a seeded torus (R = 1, r = 0.3,
+1024 x 512 quads -> 1,048,576 triangles, 2 % radial noise) and 4,194,304 query
+points uniform in [-2, 2]^3 with squared max radius = FLT_MAX, binary SAH BVH
+built on the host. A step is one closest-point pass over all queries of the
+rank, inputs resident on the device; L2 is flushed (a 256 MiB device write)
+before every timed step, outside the timed events.
+
+Prints one JSON line (rank 0). ``--impl reference`` instead times the reference
+CPU algorithm (the C restatement in oracle/, all host threads) on bounded
+samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "closest-pt queries/s @1M tris (plain vs batched+quantised, 1 GB300); fwd+bwd ms"
+UNIT = "queries/s"
+N_QUERIES = 4_194_304
+TORUS = (1024, 512)
+FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--variant", default="auto")
+    ap.add_argument("--queries", type=int, default=N_QUERIES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# --------------------------------------------------------------- workload
+def make_workload(rank: int, n_queries: int):
+    from fcpw_gb300 import workloads as W
+    v, f = W.torus(*TORUS, seed=W.SEED_BASE + 2)
+    pts = W.uniform_points(n_queries, 3, -2.0, 2.0, W.SEED_BASE + 2 + 1000 * (rank + 1))
+    return v, f, pts
+
+
+def build_scene(v, f):
+    import fcpw_gb300 as F
+    s = F.Scene3D()
+    s.set_object_count(1)
+    s.set_object_vertices(v, 0)
+    s.set_object_triangles(f, 0)
+    t = time.perf_counter()
+    s.build(F.AggregateType.Bvh_SurfaceArea, False)
+    return s, time.perf_counter() - t
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (200 ms period)."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_baseline(scene, pts, budget_s: float = 12.0, max_queries: int = N_QUERIES):
+    """The reference CPU closest-point traversal (oracle port), all host threads,
+    on a bounded prefix of the query set sized to about budget_s seconds."""
+    from fcpw_gb300 import records as R
+    from oracle import oracle as O
+    nodes, prims, _ = scene.cpu_bvh.export()
+    threads = os.cpu_count() or 1
+    n0 = min(len(pts), 20000)
+    t = time.perf_counter()
+    O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts[:n0], R.FLT_MAX), nthreads=threads)
+    rate = n0 / max(time.perf_counter() - t, 1e-9)
+    n = int(min(max_queries, len(pts), max(n0, rate * budget_s)))
+    sph = R.make_spheres(pts[:n], R.FLT_MAX)
+    t = time.perf_counter()
+    O.closest_points_bvh(3, nodes, prims, sph, nthreads=threads)
+    dt = time.perf_counter() - t
+    return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {n} of the {len(pts)} queries, oracle/fcpw_oracle.c closest_point_bvh "
+                      f"(reference bvh.inl:1291-1418 restated), {threads} threads, {dt:.2f} s"}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(variant: str):
+    """DRAM bytes per launch from the committed ncu summary of this kernel, if any."""
+    p = ROOT / "profiles" / "closest_point_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return d.get(variant)
+
+
+# ------------------------------------------------------------------ main
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import fcpw_gb300 as F
+    from fcpw_gb300 import records as R
+    from fcpw_gb300._lib import check, lib
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    v, f, pts = make_workload(rank, args.queries)
+    scene, build_s = build_scene(v, f)
+    gpu = F.GPUScene3D("", False, device=local)
+    t = time.perf_counter()
+    gpu.transfer_to_gpu(scene)
+    transfer_s = time.perf_counter() - t
+    n = len(pts)
+
+    spheres = torch.empty((n, 4), dtype=torch.float32, device=dev)
+    spheres[:, :3] = torch.from_numpy(pts).to(dev)
+    spheres[:, 3] = float(R.FLT_MAX)
+    out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = C.c_void_p(stream.cuda_stream)
+    L = lib()
+
+    def step():
+        check(L.fcpwgb_find_closest_points_device(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, 0, sptr))
+
+    # traversal statistics -> algorithmic bytes of one launch (untimed)
+    stats = (C.c_uint64 * 4)()
+    check(L.fcpwgb_closest_points_traversal_stats(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, stats))
+    n_q, n_pop, n_inner, n_prim = [int(x) for x in stats]
+    s_node, s_prim, s_in, s_out, w = 32, 40, 16, 40, 2
+    alg_bytes = n_q * (s_in + s_out) + s_node * (n_q + w * n_inner) + s_prim * n_prim
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record(stream)
+        step()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    value = world * n / (ms_max / 1e3)
+
+    # end to end through the host-array C ABI call (pinned host buffers, copies inside)
+    h_sph = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
+    h_sph.copy_(spheres.cpu())
+    h_out = torch.empty((n, 10), dtype=torch.float32, pin_memory=True)
+    for _ in range(2):
+        check(L.fcpwgb_find_closest_points(gpu.handle, h_sph.data_ptr(), h_out.data_ptr(), n, 0))
+    e2e_t = []
+    for _ in range(max(3, args.steps // 2)):
+        t = time.perf_counter()
+        check(L.fcpwgb_find_closest_points(gpu.handle, h_sph.data_ptr(), h_out.data_ptr(), n, 0))
+        e2e_t.append(time.perf_counter() - t)
+    clocks = sampler.stop()
+    e2e_s = statistics.median(e2e_t)
+    e2e_t_t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(e2e_t_t, op=dist.ReduceOp.MAX)
+    e2e_value = world * n / float(e2e_t_t.item())
+
+    # accuracy against the FP64 brute force on a sample (rank 0)
+    accuracy = None
+    result = None
+    if rank == 0:
+        from oracle import oracle as O
+        res = out.cpu().numpy().view(R.INTERACTION).reshape(-1)
+        _, prims, _ = scene.cpu_bvh.export()
+        k = 256
+        d64, _ = O.closest_points_brute_f64(3, prims, R.make_spheres(pts[:k], R.FLT_MAX))
+        rel = np.abs(res["d"][:k].astype(np.float64) - d64) / d64
+        accuracy = {"samples": k, "max_rel_err_vs_fp64": float(rel.max()), "mean_rel_err_vs_fp64": float(rel.mean())}
+
+        peak, peak_kind = peaks()
+        achieved = alg_bytes / (ms / 1e3) / 1e9
+        traffic = profiled_traffic("binary")
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded torus + uniform queries)",
+            "config": {"workload": "closest point, seeded torus 1,048,576 triangles, 4,194,304 queries "
+                                   "uniform in [-2,2]^3 per GPU, r2 = FLT_MAX, binary SAH BVH",
+                       "variant": "binary (reference traversal order)", "queries_per_gpu": n,
+                       "triangles": int(len(f)), "l2": "flushed (256 MiB write) before every timed step",
+                       "bvh_build_s": round(build_s, 3), "transfer_s": round(transfer_s, 3)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 40},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": f"hbm_gbs ({peak_kind})",
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "per_query": {"nodes_popped": n_pop / n_q, "inner_expanded": n_inner / n_q,
+                                       "prim_tests": n_prim / n_q}},
+            "clocks": clocks, "accuracy": accuracy,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            result["cpu_baseline"] = cpu_baseline(scene, pts)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def run_reference(args):
+    """The reference CPU implementation of the path (its C restatement, all host threads)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from fcpw_gb300 import records as R
+    from oracle import oracle as O
+    v, f, pts = make_workload(0, args.queries)
+    scene, _ = build_scene(v, f)
+    nodes, prims, _ = scene.cpu_bvh.export()
+    threads = os.cpu_count() or 1
+    sample = min(len(pts), 262_144)
+    sph = R.make_spheres(pts[:sample], R.FLT_MAX)
+    for _ in range(args.warmup):
+        O.closest_points_bvh(3, nodes, prims, sph[: sample // 8], nthreads=threads)
+    times = []
+    for i in range(args.steps):
+        t = time.perf_counter()
+        O.closest_points_bvh(3, nodes, prims, sph, nthreads=threads)
+        times.append(time.perf_counter() - t)
+    ms = 1e3 * sum(times) / len(times)
+    value = sample / (ms / 1e3)
+    desc = (f"{sample} of the {len(pts)} queries per step, oracle/fcpw_oracle.c closest_point_bvh "
+            f"(reference bvh.inl:1291-1418 restated), {threads} threads")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded torus + uniform queries)",
+        "config": {"workload": "closest point, seeded torus 1,048,576 triangles, 4,194,304 queries "
+                               "uniform in [-2,2]^3 per GPU, r2 = FLT_MAX, binary SAH BVH",
+                   "sample_queries_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

@@ -1,0 +1,94 @@
+"""ctypes binding of the C ABI declared in include/fcpw_gb300.h.
+
+The library is loaded from ``fcpw_gb300/lib/libfcpw_gb300.so`` (built in-tree by
+``fcpw_gb300.build.build()``). There is no fallback: when the library is missing
+every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "lib" / "libfcpw_gb300.so"
+_lib = None
+
+c_void_p, c_int, c_uint32, c_float = C.c_void_p, C.c_int, C.c_uint32, C.c_float
+P = C.c_void_p
+
+# name -> (restype, argtypes); mirrors include/fcpw_gb300.h
+SIGNATURES = {
+    "fcpwgb_last_error": (C.c_char_p, []),
+    "fcpwgb_version": (C.c_char_p, []),
+    "fcpwgb_device_count": (c_int, []),
+    "fcpwgb_cpu_bvh_build": (c_int, [c_int, P, c_uint32, P, c_uint32, c_int, c_int, C.POINTER(c_void_p)]),
+    "fcpwgb_cpu_bvh_destroy": (None, [P]),
+    "fcpwgb_cpu_bvh_info": (c_int, [P, P]),
+    "fcpwgb_cpu_bvh_export": (c_int, [P, P, P, P]),
+    "fcpwgb_cpu_bvh_export_topology": (c_int, [P, P, P, P, P]),
+    "fcpwgb_cpu_bvh_update_positions": (c_int, [P, P]),
+    "fcpwgb_gpu_scene_create": (c_int, [c_int, c_int, C.POINTER(c_void_p)]),
+    "fcpwgb_gpu_scene_destroy": (None, [P]),
+    "fcpwgb_gpu_scene_transfer": (c_int, [P, c_int, P, c_uint32, P, c_uint32, P, c_uint32, P, c_uint32]),
+    "fcpwgb_gpu_scene_transfer_cpu_bvh": (c_int, [P, P]),
+    "fcpwgb_gpu_scene_refit": (c_int, [P, P, P]),
+    "fcpwgb_gpu_scene_update_vertices_device": (c_int, [P, P, c_uint32, P]),
+    "fcpwgb_find_closest_points": (c_int, [P, P, P, c_uint32, c_int]),
+    "fcpwgb_intersect_rays": (c_int, [P, P, P, c_uint32, c_int]),
+    "fcpwgb_intersect_spheres": (c_int, [P, P, P, P, c_uint32]),
+    "fcpwgb_find_closest_silhouette_points": (c_int, [P, P, P, P, c_uint32, c_float, c_float]),
+    "fcpwgb_find_closest_points_device": (c_int, [P, P, P, c_uint32, c_int, P]),
+    "fcpwgb_intersect_rays_device": (c_int, [P, P, P, c_uint32, c_int, P]),
+    "fcpwgb_intersect_spheres_device": (c_int, [P, P, P, P, c_uint32, P]),
+    "fcpwgb_find_closest_silhouette_points_device": (c_int, [P, P, P, P, c_uint32, c_float, c_float, P]),
+    "fcpwgb_closest_points_traversal_stats": (c_int, [P, P, P, c_uint32, P]),
+    "fcpwgb_gpu_scene_check_errors": (c_int, [P, C.POINTER(c_uint32)]),
+}
+
+
+class BvhInfo(C.Structure):
+    _fields_ = [("dim", c_int), ("bvh_type", c_int), ("n_nodes", c_uint32), ("n_leaves", c_uint32),
+                ("max_depth", c_uint32), ("n_primitives", c_uint32), ("n_silhouettes", c_uint32),
+                ("n_vertices", c_uint32)]
+
+
+class FcpwError(RuntimeError):
+    """A non-zero status returned by the native library."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"fcpw_gb300 error {code}: {message}")
+        self.code = code
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def lib():
+    """Loads the native library (once) and declares every entry point."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise RuntimeError(f"fcpw_gb300 native library not built: {_LIB_PATH} is missing "
+                               "(run `python -c 'import fcpw_gb300.build as b; b.build()'`)")
+        handle = C.CDLL(str(_LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = lib().fcpwgb_last_error()
+        raise FcpwError(rc, msg.decode() if msg else "")
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (None for None)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data

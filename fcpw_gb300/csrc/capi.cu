@@ -1,0 +1,617 @@
+// C ABI of the GB300 query path (include/fcpw_gb300.h).
+//
+// A fcpwgb_gpu_scene holds one transferred tree in device memory, one CUDA
+// stream, the refit schedule and reusable staging buffers for the host-array
+// entry points. Every tree handed in is validated on the host (offsets in
+// range, a proper binary tree in pre-order, depth within the 64-entry
+// traversal stack) before anything is uploaded, so device traversals never
+// index outside their arrays.
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "fcpw_gb300.h"
+#include "host_bvh.h"
+#include "kernels.h"
+#include "scene.h"
+
+using namespace fcpwgb;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_lastError;
+
+namespace fcpwgb {
+int setError(int code, const std::string &msg) {
+    g_lastError = msg;
+    return code;
+}
+int cudaFail(cudaError_t e, const char *where) {
+    return setError(e == cudaErrorMemoryAllocation ? FCPWGB_ERR_OUT_OF_MEMORY : FCPWGB_ERR_CUDA,
+                    std::string(where) + ": " + cudaGetErrorString(e));
+}
+}  // namespace fcpwgb
+
+#define FCPWGB_CUDA(call)                                    \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cudaFail(e_, #call);   \
+    } while (0)
+
+extern "C" const char *fcpwgb_last_error(void) { return g_lastError.c_str(); }
+extern "C" const char *fcpwgb_version(void) { return "fcpw_gb300 0.1 (sm_103a)"; }
+extern "C" int fcpwgb_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+// ----------------------------------------------------------- CPU producer
+struct fcpwgb_cpu_bvh {
+    std::unique_ptr<HostBvh> bvh;
+};
+
+extern "C" int fcpwgb_cpu_bvh_build(int dim, const float *positions, uint32_t n_vertices, const int32_t *indices,
+                                    uint32_t n_primitives, int aggregate_type, int with_silhouettes,
+                                    fcpwgb_cpu_bvh **out) {
+    if (!out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    Heuristic h;
+    switch (aggregate_type) {
+        case FCPWGB_AGGREGATE_BVH_LONGEST_AXIS: h = Heuristic::LongestAxisCenter; break;
+        case FCPWGB_AGGREGATE_BVH_OVERLAP_SURFACE: h = Heuristic::OverlapSurfaceArea; break;
+        case FCPWGB_AGGREGATE_BVH_SURFACE_AREA: h = Heuristic::SurfaceArea; break;
+        case FCPWGB_AGGREGATE_BVH_OVERLAP_VOLUME: h = Heuristic::OverlapVolume; break;
+        case FCPWGB_AGGREGATE_BVH_VOLUME: h = Heuristic::Volume; break;
+        default:
+            return setError(FCPWGB_ERR_UNSUPPORTED,
+                            "the GPU path needs a BVH aggregate (Bvh_*); Baseline is not supported");
+    }
+    try {
+        auto *b = new fcpwgb_cpu_bvh;
+        b->bvh.reset(new HostBvh(dim, positions, n_vertices, indices, n_primitives, h, with_silhouettes != 0));
+        *out = b;
+    } catch (const std::bad_alloc &) {
+        return setError(FCPWGB_ERR_OUT_OF_MEMORY, "host allocation failed while building the BVH");
+    } catch (const std::exception &e) {
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, e.what());
+    }
+    return FCPWGB_OK;
+}
+
+extern "C" void fcpwgb_cpu_bvh_destroy(fcpwgb_cpu_bvh *bvh) { delete bvh; }
+
+extern "C" int fcpwgb_cpu_bvh_info(const fcpwgb_cpu_bvh *b, fcpwgb_bvh_info *info) {
+    if (!b || !info) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    info->dim = b->bvh->dim();
+    info->bvh_type = b->bvh->bvhType();
+    info->n_nodes = b->bvh->nNodes();
+    info->n_leaves = b->bvh->nLeaves();
+    info->max_depth = b->bvh->maxDepth();
+    info->n_primitives = b->bvh->nPrimitives();
+    info->n_silhouettes = b->bvh->nSilhouetteRefs();
+    info->n_vertices = b->bvh->nVertices();
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_cpu_bvh_export(const fcpwgb_cpu_bvh *b, void *nodes, void *primitives, void *silhouettes) {
+    if (!b) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL bvh");
+    if (nodes) b->bvh->exportNodes(nodes);
+    if (primitives) b->bvh->exportPrimitives(primitives);
+    if (silhouettes) b->bvh->exportSilhouettes(silhouettes);
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_cpu_bvh_export_topology(const fcpwgb_cpu_bvh *b, int32_t *index_map, int32_t *prim_vertices,
+                                              uint32_t *prim_index, int32_t *sil_vertices) {
+    if (!b) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL bvh");
+    b->bvh->exportTopology(index_map, prim_vertices, prim_index, sil_vertices);
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_cpu_bvh_update_positions(fcpwgb_cpu_bvh *b, const float *positions) {
+    if (!b || !positions) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    b->bvh->updatePositions(positions);
+    return FCPWGB_OK;
+}
+
+// ------------------------------------------------------------- GPU scene
+namespace fcpwgb {
+
+int GpuScene::activate() const {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cudaFail(e, "cudaSetDevice");
+    return FCPWGB_OK;
+}
+
+SceneView GpuScene::view() const {
+    SceneView v;
+    v.dim = dim;
+    v.snch = snch;
+    v.nodes = (const unsigned char *)nodes.ptr;
+    v.prims = (const unsigned char *)prims.ptr;
+    v.sils = (const unsigned char *)sils.ptr;
+    v.nNodes = nNodes;
+    v.nPrims = nPrims;
+    v.nSils = nSils;
+    v.maxDepth = maxDepth;
+    v.errorWord = (uint32_t *)errorWord.ptr;
+    return v;
+}
+
+cudaStream_t GpuScene::pick(void *s) const { return s ? (cudaStream_t)s : stream; }
+
+}  // namespace fcpwgb
+
+static size_t primBytes(int dim) { return dim == 3 ? sizeof(DevTriangle) : sizeof(DevSegment2); }
+static size_t silBytes(int dim) { return dim == 3 ? sizeof(DevEdge) : sizeof(DevVertex2); }
+
+extern "C" int fcpwgb_gpu_scene_create(int dim, int device, fcpwgb_gpu_scene **out) {
+    if (!out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    if (dim != 2 && dim != 3) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "dim must be 2 or 3");
+    int count = fcpwgb_device_count();
+    if (count == 0) return setError(FCPWGB_ERR_CUDA, "no CUDA device is visible");
+    if (device < 0 || device >= count) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "device index out of range");
+    std::unique_ptr<fcpwgb_gpu_scene> s(new fcpwgb_gpu_scene);
+    s->dim = dim;
+    s->device = device;
+    FCPWGB_CUDA(cudaSetDevice(device));
+    FCPWGB_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    int rc = s->errorWord.ensure(sizeof(uint32_t) * 4);
+    if (rc) return rc;
+    FCPWGB_CUDA(cudaMemsetAsync(s->errorWord.ptr, 0, sizeof(uint32_t) * 4, s->stream));
+    FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+    *out = s.release();
+    return FCPWGB_OK;
+}
+
+extern "C" void fcpwgb_gpu_scene_destroy(fcpwgb_gpu_scene *s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) {
+        cudaStreamSynchronize(s->stream);
+        cudaStreamDestroy(s->stream);
+    }
+    delete s;
+}
+
+// Validates a pre-order binary tree; fills parents, leaves and the max depth.
+static int validateTree(const std::vector<uint32_t> &nPrims, const std::vector<uint32_t> &offsets,
+                        uint32_t nPrimitives, std::vector<int32_t> &parents, std::vector<uint32_t> &leaves,
+                        uint32_t &maxDepth) {
+    uint32_t n = (uint32_t)nPrims.size();
+    parents.assign(n, -2);
+    leaves.clear();
+    maxDepth = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> stack;  // (node, depth)
+    stack.push_back({0u, 0u});
+    parents[0] = -1;
+    uint32_t visited = 0;
+    uint64_t primsCovered = 0;
+    while (!stack.empty()) {
+        auto [i, depth] = stack.back();
+        stack.pop_back();
+        visited++;
+        if (depth > 62) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "tree deeper than 62 levels");
+        maxDepth = depth > maxDepth ? depth : maxDepth;
+        if (nPrims[i] > 0) {
+            if ((uint64_t)offsets[i] + nPrims[i] > nPrimitives)
+                return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf primitive range out of bounds");
+            primsCovered += nPrims[i];
+            leaves.push_back(i);
+        } else {
+            uint64_t l = (uint64_t)i + 1, r = (uint64_t)i + offsets[i];
+            if (offsets[i] < 2 || r >= n || l >= n)
+                return setError(FCPWGB_ERR_INVALID_ARGUMENT, "inner node child offset out of range");
+            if (parents[l] != -2 || parents[r] != -2)
+                return setError(FCPWGB_ERR_INVALID_ARGUMENT, "node referenced by two parents");
+            parents[l] = (int32_t)i;
+            parents[r] = (int32_t)i;
+            stack.push_back({(uint32_t)r, depth + 1});
+            stack.push_back({(uint32_t)l, depth + 1});
+        }
+    }
+    if (visited != n) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "unreachable nodes in the tree");
+    (void)primsCovered;
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *s, int bvh_type, const void *nodes, uint32_t n_nodes,
+                                         const void *primitives, uint32_t n_primitives, const void *silhouettes,
+                                         uint32_t n_silhouettes, const int32_t *prim_vertices,
+                                         uint32_t n_vertices) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    int rc = s->activate();
+    if (rc) return rc;
+    bool is2d = bvh_type == FCPWGB_LINE_SEGMENT_BVH || bvh_type == FCPWGB_LINE_SEGMENT_SNCH;
+    bool is3d = bvh_type == FCPWGB_TRIANGLE_BVH || bvh_type == FCPWGB_TRIANGLE_SNCH;
+    if (!is2d && !is3d) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "unknown bvh_type");
+    if ((is2d && s->dim != 2) || (is3d && s->dim != 3))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "bvh_type does not match the scene dimension");
+    bool snch = bvh_type == FCPWGB_LINE_SEGMENT_SNCH || bvh_type == FCPWGB_TRIANGLE_SNCH;
+    if (!nodes || n_nodes == 0 || !primitives || n_primitives == 0)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "a non-empty tree and primitive array are required");
+    if (snch && n_silhouettes > 0 && !silhouettes)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "silhouettes missing");
+
+    // gather node topology and check it
+    std::vector<uint32_t> nP(n_nodes), off(n_nodes);
+    std::vector<uint32_t> nS, sOff;
+    if (snch) { nS.resize(n_nodes); sOff.resize(n_nodes); }
+    for (uint32_t i = 0; i < n_nodes; i++) {
+        if (snch) {
+            const fcpwgb_snch_node &nd = ((const fcpwgb_snch_node *)nodes)[i];
+            nP[i] = nd.nPrimitives; off[i] = nd.offset; nS[i] = nd.nSilhouettes; sOff[i] = nd.silhouetteOffset;
+            if ((uint64_t)nd.silhouetteOffset + nd.nSilhouettes > n_silhouettes)
+                return setError(FCPWGB_ERR_INVALID_ARGUMENT, "silhouette range out of bounds");
+        } else {
+            const fcpwgb_bvh_node &nd = ((const fcpwgb_bvh_node *)nodes)[i];
+            nP[i] = nd.nPrimitives; off[i] = nd.offset;
+        }
+    }
+    std::vector<int32_t> parents;
+    std::vector<uint32_t> leaves;
+    uint32_t maxDepth = 0;
+    rc = validateTree(nP, off, n_primitives, parents, leaves, maxDepth);
+    if (rc) return rc;
+    if (prim_vertices) {
+        for (uint64_t k = 0; k < (uint64_t)n_primitives * s->dim; k++)
+            if (prim_vertices[k] < 0 || (uint32_t)prim_vertices[k] >= n_vertices)
+                return setError(FCPWGB_ERR_INVALID_ARGUMENT, "prim_vertices index out of range");
+    }
+
+    // device layouts
+    std::vector<unsigned char> hNodes((size_t)n_nodes * (snch ? 64 : 32), 0);
+    for (uint32_t i = 0; i < n_nodes; i++) {
+        unsigned char *d = hNodes.data() + (size_t)i * (snch ? 64 : 32);
+        if (snch) {
+            const fcpwgb_snch_node &nd = ((const fcpwgb_snch_node *)nodes)[i];
+            std::memcpy(d, &nd.box, 24);
+            std::memcpy(d + 24, &nd.nPrimitives, 4);
+            std::memcpy(d + 28, &nd.offset, 4);
+            std::memcpy(d + 32, &nd.cone, 20);
+            std::memcpy(d + 52, &nd.nSilhouettes, 4);
+            std::memcpy(d + 56, &nd.silhouetteOffset, 4);
+        } else {
+            std::memcpy(d, (const unsigned char *)nodes + (size_t)i * 32, 32);
+        }
+    }
+    std::vector<unsigned char> hPrims((size_t)n_primitives * primBytes(s->dim), 0);
+    if (s->dim == 3) {
+        std::memcpy(hPrims.data(), primitives, hPrims.size());
+    } else {
+        for (uint32_t k = 0; k < n_primitives; k++) {
+            const fcpwgb_line_segment &sg = ((const fcpwgb_line_segment *)primitives)[k];
+            DevSegment2 d;
+            d.pa = make_float2(sg.pa.x, sg.pa.y);
+            d.pb = make_float2(sg.pb.x, sg.pb.y);
+            d.index = sg.index;
+            d.pad = 0;
+            std::memcpy(hPrims.data() + (size_t)k * sizeof(DevSegment2), &d, sizeof(d));
+        }
+    }
+    std::vector<unsigned char> hSils;
+    if (snch && n_silhouettes > 0) {
+        hSils.resize((size_t)n_silhouettes * silBytes(s->dim));
+        if (s->dim == 3) {
+            std::memcpy(hSils.data(), silhouettes, hSils.size());
+        } else {
+            for (uint32_t k = 0; k < n_silhouettes; k++) {
+                const fcpwgb_vertex &v = ((const fcpwgb_vertex *)silhouettes)[k];
+                DevVertex2 d;
+                d.p = make_float2(v.p.x, v.p.y);
+                d.n0 = make_float2(v.n0.x, v.n0.y);
+                d.n1 = make_float2(v.n1.x, v.n1.y);
+                d.index = v.index;
+                d.hasOneAdjacentFace = v.hasOneAdjacentFace;
+                std::memcpy(hSils.data() + (size_t)k * sizeof(DevVertex2), &d, sizeof(d));
+            }
+        }
+    }
+
+    // upload
+    s->resetTree();
+    if ((rc = s->nodes.upload(hNodes.data(), hNodes.size(), s->stream))) return rc;
+    if ((rc = s->prims.upload(hPrims.data(), hPrims.size(), s->stream))) return rc;
+    if (!hSils.empty() && (rc = s->sils.upload(hSils.data(), hSils.size(), s->stream))) return rc;
+    if ((rc = s->parents.upload(parents.data(), parents.size() * sizeof(int32_t), s->stream))) return rc;
+    if ((rc = s->leaves.upload(leaves.data(), leaves.size() * sizeof(uint32_t), s->stream))) return rc;
+    if ((rc = s->counters.ensure((size_t)n_nodes * sizeof(uint32_t)))) return rc;
+    if (prim_vertices) {
+        if ((rc = s->primVerts.upload(prim_vertices, (size_t)n_primitives * s->dim * sizeof(int32_t), s->stream)))
+            return rc;
+        s->nVertices = n_vertices;
+    }
+    FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+
+    s->bvhType = bvh_type;
+    s->snch = snch;
+    s->nNodes = n_nodes;
+    s->nPrims = n_primitives;
+    s->nSils = snch ? n_silhouettes : 0;
+    s->nLeaves = (uint32_t)leaves.size();
+    s->maxDepth = maxDepth;
+    s->transferred = true;
+    s->treeVersion++;
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_transfer_cpu_bvh(fcpwgb_gpu_scene *s, const fcpwgb_cpu_bvh *b) {
+    if (!s || !b) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    const HostBvh &h = *b->bvh;
+    bool snch = h.hasSilhouettes();
+    std::vector<unsigned char> nodes((size_t)h.nNodes() * (snch ? sizeof(fcpwgb_snch_node) : sizeof(fcpwgb_bvh_node)));
+    std::vector<unsigned char> prims((size_t)h.nPrimitives() * (h.dim() == 3 ? sizeof(fcpwgb_triangle) : sizeof(fcpwgb_line_segment)));
+    std::vector<unsigned char> sils((size_t)h.nSilhouetteRefs() * (h.dim() == 3 ? sizeof(fcpwgb_edge) : sizeof(fcpwgb_vertex)));
+    std::vector<int32_t> primVerts((size_t)h.nPrimitives() * h.dim());
+    std::vector<int32_t> silVerts((size_t)h.nSilhouetteRefs() * (h.dim() + 1));
+    h.exportNodes(nodes.data());
+    h.exportPrimitives(prims.data());
+    if (snch) h.exportSilhouettes(sils.data());
+    h.exportTopology(nullptr, primVerts.data(), nullptr, snch ? silVerts.data() : nullptr);
+    int rc = fcpwgb_gpu_scene_transfer(s, h.bvhType(), nodes.data(), h.nNodes(), prims.data(), h.nPrimitives(),
+                                       sils.empty() ? nullptr : sils.data(), h.nSilhouetteRefs(), primVerts.data(),
+                                       h.nVertices());
+    if (rc) return rc;
+    if (snch && !silVerts.empty()) {
+        if ((rc = s->silVerts.upload(silVerts.data(), silVerts.size() * sizeof(int32_t), s->stream))) return rc;
+        FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    return FCPWGB_OK;
+}
+
+static int requireTree(fcpwgb_gpu_scene *s) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    if (!s->transferred) return setError(FCPWGB_ERR_NOT_TRANSFERRED, "transferToGPU has not been called");
+    return s->activate();
+}
+
+namespace fcpwgb {
+int runRefit(fcpwgb_gpu_scene *s, cudaStream_t st) {
+    FCPWGB_CUDA(cudaMemsetAsync(s->counters.ptr, 0, (size_t)s->nNodes * sizeof(uint32_t), st));
+    RefitView v;
+    v.dim = s->dim;
+    v.snch = s->snch;
+    v.nodes = (unsigned char *)s->nodes.ptr;
+    v.prims = (const unsigned char *)s->prims.ptr;
+    v.sils = (const unsigned char *)s->sils.ptr;
+    v.parents = (const int32_t *)s->parents.ptr;
+    v.leaves = (const uint32_t *)s->leaves.ptr;
+    v.nLeaves = s->nLeaves;
+    v.nNodes = s->nNodes;
+    v.counters = (uint32_t *)s->counters.ptr;
+    FCPWGB_CUDA(launchRefit(v, st));
+    return s->afterRefit(st);
+}
+}  // namespace fcpwgb
+
+extern "C" int fcpwgb_gpu_scene_refit(fcpwgb_gpu_scene *s, const void *primitives, const void *silhouettes) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (primitives) {
+        if (s->dim == 3) {
+            if ((rc = s->prims.upload(primitives, (size_t)s->nPrims * sizeof(DevTriangle), s->stream))) return rc;
+        } else {
+            std::vector<DevSegment2> tmp(s->nPrims);
+            for (uint32_t k = 0; k < s->nPrims; k++) {
+                const fcpwgb_line_segment &sg = ((const fcpwgb_line_segment *)primitives)[k];
+                tmp[k].pa = make_float2(sg.pa.x, sg.pa.y);
+                tmp[k].pb = make_float2(sg.pb.x, sg.pb.y);
+                tmp[k].index = sg.index;
+                tmp[k].pad = 0;
+            }
+            if ((rc = s->prims.upload(tmp.data(), tmp.size() * sizeof(DevSegment2), s->stream))) return rc;
+            FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+        }
+    }
+    if (silhouettes && s->snch && s->nSils > 0) {
+        if (s->dim == 3) {
+            if ((rc = s->sils.upload(silhouettes, (size_t)s->nSils * sizeof(DevEdge), s->stream))) return rc;
+        } else {
+            std::vector<DevVertex2> tmp(s->nSils);
+            for (uint32_t k = 0; k < s->nSils; k++) {
+                const fcpwgb_vertex &v = ((const fcpwgb_vertex *)silhouettes)[k];
+                tmp[k].p = make_float2(v.p.x, v.p.y);
+                tmp[k].n0 = make_float2(v.n0.x, v.n0.y);
+                tmp[k].n1 = make_float2(v.n1.x, v.n1.y);
+                tmp[k].index = v.index;
+                tmp[k].hasOneAdjacentFace = v.hasOneAdjacentFace;
+            }
+            if ((rc = s->sils.upload(tmp.data(), tmp.size() * sizeof(DevVertex2), s->stream))) return rc;
+            FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+        }
+    }
+    if ((rc = runRefit(s, s->stream))) return rc;
+    FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *s, const float *positions,
+                                                       uint32_t n_vertices, void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (!s->primVerts.ptr)
+        return setError(FCPWGB_ERR_UNSUPPORTED, "the tree was transferred without prim_vertices");
+    if (!positions || n_vertices != s->nVertices)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "positions must hold the transferred vertex count");
+    cudaStream_t st = s->pick(stream);
+    FCPWGB_CUDA(launchGatherPrimitives(s->dim, positions, (const int32_t *)s->primVerts.ptr, s->nPrims,
+                                       (unsigned char *)s->prims.ptr, st));
+    if (s->snch && s->nSils > 0 && s->silVerts.ptr)
+        FCPWGB_CUDA(launchGatherSilhouettes(s->dim, positions, (const int32_t *)s->silVerts.ptr, s->nSils,
+                                            (unsigned char *)s->sils.ptr, st));
+    return runRefit(s, st);
+}
+
+// ------------------------------------------------------------------ queries
+// device-array entry points
+extern "C" int fcpwgb_find_closest_points_device(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                 fcpwgb_interaction *out, uint32_t n, int record_normals,
+                                                 void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return s->closestPoints((const DevSphere *)spheres, (DevInteraction *)out, n, record_normals, s->pick(stream));
+}
+
+extern "C" int fcpwgb_intersect_rays_device(fcpwgb_gpu_scene *s, const fcpwgb_ray *rays, fcpwgb_interaction *out,
+                                            uint32_t n, int occl, void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > 0 && (!rays || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return s->rays((const DevRay *)rays, (DevInteraction *)out, n, occl, s->pick(stream));
+}
+
+extern "C" int fcpwgb_intersect_spheres_device(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                               const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out, uint32_t n,
+                                               void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > 0 && (!spheres || !rand_nums || !out))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    FCPWGB_CUDA(launchSphereSampleBinary(s->view(), (const DevSphere *)spheres, (const float3 *)rand_nums,
+                                         (DevInteraction *)out, n, s->pick(stream)));
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
+                                                            const fcpwgb_bounding_sphere *spheres,
+                                                            const uint32_t *flip, fcpwgb_interaction *out,
+                                                            uint32_t n, float sq_min_r, float precision,
+                                                            void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > 0 && (!spheres || !flip || !out))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    cudaStream_t st = s->pick(stream);
+    if (!s->snch || s->nSils == 0) {
+        // no silhouette data: the reference kernel leaves every result at its default
+        FCPWGB_CUDA(launchFillDefault((DevInteraction *)out, n, st));
+        return FCPWGB_OK;
+    }
+    FCPWGB_CUDA(launchSilhouetteBinary(s->view(), (const DevSphere *)spheres, flip, (DevInteraction *)out, n,
+                                       sq_min_r, precision, st));
+    return FCPWGB_OK;
+}
+
+// host-array entry points: stage through device buffers, run, read back, synchronise
+namespace {
+struct HostQuery {
+    fcpwgb_gpu_scene *s;
+    int begin(const void *in0, size_t b0, const void *in1, size_t b1, size_t outBytes) {
+        int rc;
+        if ((rc = s->qIn0.ensure(b0 > 0 ? b0 : 16))) return rc;
+        if (b1 && (rc = s->qIn1.ensure(b1))) return rc;
+        if ((rc = s->qOut.ensure(outBytes > 0 ? outBytes : 16))) return rc;
+        if (b0) FCPWGB_CUDA(cudaMemcpyAsync(s->qIn0.ptr, in0, b0, cudaMemcpyHostToDevice, s->stream));
+        if (b1) FCPWGB_CUDA(cudaMemcpyAsync(s->qIn1.ptr, in1, b1, cudaMemcpyHostToDevice, s->stream));
+        return FCPWGB_OK;
+    }
+    int finish(void *out, size_t outBytes) {
+        uint32_t err[4] = {0, 0, 0, 0};
+        if (outBytes) FCPWGB_CUDA(cudaMemcpyAsync(out, s->qOut.ptr, outBytes, cudaMemcpyDeviceToHost, s->stream));
+        FCPWGB_CUDA(cudaMemcpyAsync(err, s->errorWord.ptr, sizeof(err), cudaMemcpyDeviceToHost, s->stream));
+        FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+        if (err[0]) {
+            cudaMemsetAsync(s->errorWord.ptr, 0, sizeof(err), s->stream);
+            cudaStreamSynchronize(s->stream);
+            return setError(FCPWGB_ERR_TRAVERSAL, "device traversal error word " + std::to_string(err[0]));
+        }
+        return FCPWGB_OK;
+    }
+};
+}  // namespace
+
+extern "C" int fcpwgb_find_closest_points(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                          fcpwgb_interaction *out, uint32_t n, int record_normals) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n == 0) return FCPWGB_OK;
+    if (!spheres || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return s->closestPointsHost(spheres, out, n, record_normals);
+}
+
+extern "C" int fcpwgb_intersect_rays(fcpwgb_gpu_scene *s, const fcpwgb_ray *rays, fcpwgb_interaction *out,
+                                     uint32_t n, int occl) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n == 0) return FCPWGB_OK;
+    if (!rays || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    HostQuery h{s};
+    size_t ob = (size_t)n * sizeof(DevInteraction);
+    if ((rc = h.begin(rays, (size_t)n * sizeof(DevRay), nullptr, 0, ob))) return rc;
+    if ((rc = s->rays((const DevRay *)s->qIn0.ptr, (DevInteraction *)s->qOut.ptr, n, occl, s->stream))) return rc;
+    return h.finish(out, ob);
+}
+
+extern "C" int fcpwgb_intersect_spheres(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                        const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out, uint32_t n) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n == 0) return FCPWGB_OK;
+    if (!spheres || !rand_nums || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    HostQuery h{s};
+    size_t ob = (size_t)n * sizeof(DevInteraction);
+    if ((rc = h.begin(spheres, (size_t)n * 16, rand_nums, (size_t)n * 12, ob))) return rc;
+    FCPWGB_CUDA(launchSphereSampleBinary(s->view(), (const DevSphere *)s->qIn0.ptr, (const float3 *)s->qIn1.ptr,
+                                         (DevInteraction *)s->qOut.ptr, n, s->stream));
+    return h.finish(out, ob);
+}
+
+extern "C" int fcpwgb_find_closest_silhouette_points(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                     const uint32_t *flip, fcpwgb_interaction *out, uint32_t n,
+                                                     float sq_min_r, float precision) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n == 0) return FCPWGB_OK;
+    if (!spheres || !flip || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    HostQuery h{s};
+    size_t ob = (size_t)n * sizeof(DevInteraction);
+    if ((rc = h.begin(spheres, (size_t)n * 16, flip, (size_t)n * 4, ob))) return rc;
+    rc = fcpwgb_find_closest_silhouette_points_device(s, (const fcpwgb_bounding_sphere *)s->qIn0.ptr,
+                                                      (const uint32_t *)s->qIn1.ptr,
+                                                      (fcpwgb_interaction *)s->qOut.ptr, n, sq_min_r, precision,
+                                                      s->stream);
+    if (rc) return rc;
+    return h.finish(out, ob);
+}
+
+extern "C" int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                     fcpwgb_interaction *out, uint32_t n, uint64_t *stats) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (!stats) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL stats");
+    if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    DeviceBuffer counters;
+    if ((rc = counters.ensure(4 * sizeof(unsigned long long)))) return rc;
+    FCPWGB_CUDA(cudaMemsetAsync(counters.ptr, 0, 4 * sizeof(unsigned long long), s->stream));
+    if ((rc = s->closestPointsStats((const DevSphere *)spheres, (DevInteraction *)out, n,
+                                    (unsigned long long *)counters.ptr, s->stream)))
+        return rc;
+    unsigned long long h[4] = {0, 0, 0, 0};
+    FCPWGB_CUDA(cudaMemcpyAsync(h, counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+    stats[0] = n;
+    stats[1] = h[0];
+    stats[2] = h[1];
+    stats[3] = h[2];
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_check_errors(fcpwgb_gpu_scene *s, uint32_t *error_word) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    int rc = s->activate();
+    if (rc) return rc;
+    uint32_t err[4] = {0, 0, 0, 0};
+    FCPWGB_CUDA(cudaMemcpyAsync(err, s->errorWord.ptr, sizeof(err), cudaMemcpyDeviceToHost, s->stream));
+    FCPWGB_CUDA(cudaMemsetAsync(s->errorWord.ptr, 0, sizeof(err), s->stream));
+    FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+    if (error_word) *error_word = err[0];
+    return FCPWGB_OK;
+}

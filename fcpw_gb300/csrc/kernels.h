@@ -1,0 +1,57 @@
+// Launch interface between the C ABI (capi.cu) and the kernel translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+
+namespace fcpwgb {
+
+// Device view of one transferred binary tree.
+struct SceneView {
+    int dim = 3;
+    bool snch = false;
+    const unsigned char *nodes = nullptr;  // 32 B (BVH) or 64 B (SNCH) records
+    const unsigned char *prims = nullptr;  // 40 B triangles or 24 B 2D segments
+    const unsigned char *sils = nullptr;   // 56 B edges or 32 B 2D vertices
+    uint32_t nNodes = 0, nPrims = 0, nSils = 0, maxDepth = 0;
+    uint32_t *errorWord = nullptr;
+};
+
+// binary-tree query kernels (k_binary.cu)
+cudaError_t launchClosestPointBinary(const SceneView &v, const DevSphere *spheres, DevInteraction *out,
+                                     uint32_t n, int recordNormal, cudaStream_t s);
+// counting variant: stats[0..2] += popped nodes, expanded inner nodes, primitive tests
+cudaError_t launchClosestPointBinaryStats(const SceneView &v, const DevSphere *spheres, DevInteraction *out,
+                                          uint32_t n, unsigned long long *stats, cudaStream_t s);
+cudaError_t launchRayBinary(const SceneView &v, const DevRay *rays, DevInteraction *out, uint32_t n, int occl,
+                            cudaStream_t s);
+cudaError_t launchSphereSampleBinary(const SceneView &v, const DevSphere *spheres, const float3 *randNums,
+                                     DevInteraction *out, uint32_t n, cudaStream_t s);
+cudaError_t launchSilhouetteBinary(const SceneView &v, const DevSphere *spheres, const uint32_t *flip,
+                                   DevInteraction *out, uint32_t n, float sqMinR, float precision,
+                                   cudaStream_t s);
+cudaError_t launchFillDefault(DevInteraction *out, uint32_t n, cudaStream_t s);
+
+// refit (k_refit.cu)
+struct RefitView {
+    int dim = 3;
+    bool snch = false;
+    unsigned char *nodes = nullptr;      // mutable node records
+    const unsigned char *prims = nullptr;
+    const unsigned char *sils = nullptr;
+    const int32_t *parents = nullptr;    // parent node of every node, -1 for the root
+    const uint32_t *leaves = nullptr;    // node index of every leaf
+    uint32_t nLeaves = 0, nNodes = 0;
+    uint32_t *counters = nullptr;        // scratch: one arrival counter per node, zero on entry
+};
+cudaError_t launchRefit(const RefitView &v, cudaStream_t s);
+
+// device-side geometry regather from caller-order vertex positions (k_refit.cu)
+cudaError_t launchGatherPrimitives(int dim, const float *positions, const int32_t *primVerts, uint32_t nPrims,
+                                   unsigned char *prims, cudaStream_t s);
+cudaError_t launchGatherSilhouettes(int dim, const float *positions, const int32_t *silVerts, uint32_t nSils,
+                                    unsigned char *sils, cudaStream_t s);
+
+}  // namespace fcpwgb

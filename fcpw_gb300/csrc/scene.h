@@ -1,0 +1,97 @@
+// Host-side state of one GPU scene (the object behind fcpwgb_gpu_scene *).
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "fcpw_gb300.h"
+#include "kernels.h"
+#include "wide.h"
+
+namespace fcpwgb {
+
+int setError(int code, const std::string &msg);
+int cudaFail(cudaError_t e, const char *where);
+
+// Grow-only device allocation owned by a scene.
+struct DeviceBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    ~DeviceBuffer() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    int ensure(size_t n) {
+        if (n <= bytes) return 0;
+        release();
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            cudaGetLastError();
+            return cudaFail(e, "cudaMalloc");
+        }
+        bytes = n;
+        return 0;
+    }
+    int upload(const void *src, size_t n, cudaStream_t s) {
+        int rc = ensure(n > 0 ? n : 16);
+        if (rc) return rc;
+        if (n == 0) return 0;
+        cudaError_t e = cudaMemcpyAsync(ptr, src, n, cudaMemcpyHostToDevice, s);
+        return e == cudaSuccess ? 0 : cudaFail(e, "cudaMemcpyAsync");
+    }
+};
+
+struct GpuScene {
+    int dim = 3;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+
+    // transferred binary tree
+    bool transferred = false;
+    int bvhType = 0;
+    bool snch = false;
+    uint32_t nNodes = 0, nPrims = 0, nSils = 0, nLeaves = 0, maxDepth = 0, nVertices = 0;
+    uint64_t treeVersion = 0;
+    DeviceBuffer nodes, prims, sils, parents, leaves, counters, primVerts, silVerts, errorWord;
+
+    // derived wide / quantised tree (built on demand, see wide.h)
+    WideConfig wideConfig;
+    WideTree wide;
+
+    // staging for the host-array entry points
+    DeviceBuffer qIn0, qIn1, qOut;
+
+    int activate() const;
+    SceneView view() const;
+    cudaStream_t pick(void *s) const;
+    void resetTree() {
+        transferred = false;
+        wide.clear();
+    }
+
+    // query dispatch (variant chosen by wideConfig)
+    int closestPoints(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t st);
+    int closestPointsStats(const DevSphere *spheres, DevInteraction *out, uint32_t n, unsigned long long *stats,
+                           cudaStream_t st);
+    int rays(const DevRay *rays, DevInteraction *out, uint32_t n, int occl, cudaStream_t st);
+    int closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_interaction *out, uint32_t n,
+                          int recordNormal);
+    // keeps derived trees in step after the binary tree was refit on stream st
+    int afterRefit(cudaStream_t st);
+};
+
+}  // namespace fcpwgb
+
+struct fcpwgb_gpu_scene : fcpwgb::GpuScene {};
+
+namespace fcpwgb {
+int runRefit(fcpwgb_gpu_scene *s, cudaStream_t st);
+}

@@ -1,0 +1,384 @@
+"""``GPUScene2D`` / ``GPUScene3D``: the reference's Python GPU classes
+(python/fcpw_bindings.cpp:493-673) on top of the C ABI.
+
+Method names, keyword names, defaults and overloads follow the reference:
+``transfer_to_gpu``, ``refit``, ``intersect`` (rays or spheres, arrays or
+lists), ``find_closest_points`` and ``find_closest_silhouette_points``. Results
+land in a ``GPUInteractionList`` passed by the caller, as in the reference.
+Tensor methods (``*_tensor``) take CUDA tensors and return device tensors
+without host copies.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from collections import namedtuple
+
+import numpy as np
+
+from . import records as R
+from ._lib import check, lib, ptr
+from .scene import Scene2D, Scene3D, _Scene
+
+
+# ---------------------------------------------------------------- structs
+class GPUFloat2:
+    def __init__(self, x: float = 0.0, y: float = 0.0):
+        self.x, self.y = float(x), float(y)
+
+
+class GPUFloat3:
+    def __init__(self, x: float = 0.0, y: float = 0.0, z: float = 0.0):
+        self.x, self.y, self.z = float(x), float(y), float(z)
+
+
+def _f3(v) -> tuple:
+    if isinstance(v, GPUFloat3):
+        return (v.x, v.y, v.z)
+    return tuple(float(a) for a in v)
+
+
+class GPURay:
+    def __init__(self, o=None, d=None, tMax: float = float(R.FLT_MAX)):
+        self.o = o if o is not None else GPUFloat3()
+        self.d = d if d is not None else GPUFloat3()
+        dd = _f3(self.d)
+        with np.errstate(divide="ignore"):
+            inv = np.float32(1.0) / np.asarray(dd, np.float32)
+        self.inv_d = GPUFloat3(*inv)
+        self.t_max = float(tMax)
+
+
+class GPUBoundingSphere:
+    def __init__(self, c=None, r2: float = 0.0):
+        self.c = c if c is not None else GPUFloat3()
+        self.r2 = float(r2)
+
+
+class GPUInteraction:
+    def __init__(self, rec=None):
+        rec = rec if rec is not None else R.default_interactions(1)[0]
+        self.p = GPUFloat3(*rec["p"])
+        self.n = GPUFloat3(*rec["n"])
+        self.uv = GPUFloat2(*rec["uv"])
+        self.d = float(rec["d"])
+        self.index = int(rec["index"])
+
+
+# ------------------------------------------------------------------ lists
+class _RecordList:
+    """A growable array of interop records with a list-like interface."""
+    DTYPE = None
+
+    def __init__(self, items=None):
+        self._a = np.zeros(0, self.DTYPE)
+        if items is not None:
+            for it in items:
+                self.append(it)
+
+    @classmethod
+    def from_array(cls, arr: np.ndarray):
+        obj = cls()
+        obj._a = np.ascontiguousarray(arr, cls.DTYPE)
+        return obj
+
+    def array(self) -> np.ndarray:
+        return self._a
+
+    def __len__(self):
+        return len(self._a)
+
+    def resize(self, n: int):
+        a = np.zeros(n, self.DTYPE)
+        m = min(n, len(self._a))
+        a[:m] = self._a[:m]
+        self._a = a
+
+    def clear(self):
+        self._a = np.zeros(0, self.DTYPE)
+
+    def append(self, item):
+        rec = np.zeros(1, self.DTYPE)
+        self._fill(rec[0], item)
+        self._a = np.concatenate([self._a, rec])
+
+
+class GPUFloat3List(_RecordList):
+    DTYPE = np.dtype(("<f4", (3,)))
+
+    def _fill(self, rec, item):
+        rec[...] = _f3(item)
+
+    def __getitem__(self, i):
+        return GPUFloat3(*self._a[i])
+
+
+class GPURayList(_RecordList):
+    DTYPE = R.RAY
+
+    def _fill(self, rec, r: GPURay):
+        rec["o"], rec["d"], rec["dInv"], rec["tMax"] = _f3(r.o), _f3(r.d), _f3(r.inv_d), r.t_max
+
+
+class GPUBoundingSphereList(_RecordList):
+    DTYPE = R.SPHERE
+
+    def _fill(self, rec, s: GPUBoundingSphere):
+        rec["c"], rec["r2"] = _f3(s.c), s.r2
+
+
+class Uint32List(_RecordList):
+    DTYPE = np.dtype("<u4")
+
+    def _fill(self, rec, v):
+        rec[...] = int(v)
+
+
+class GPUInteractionList(_RecordList):
+    DTYPE = R.INTERACTION
+
+    def _fill(self, rec, it: GPUInteraction):
+        rec["p"], rec["n"] = _f3(it.p), _f3(it.n)
+        rec["uv"] = (it.uv.x, it.uv.y)
+        rec["d"], rec["index"] = it.d, it.index
+
+    def __getitem__(self, i):
+        return GPUInteraction(self._a[i])
+
+    # bulk extraction, python/fcpw_bindings.cpp:536-584
+    def get_distances(self):
+        return self._a["d"].copy()
+
+    def get_positions(self):
+        return self._a["p"].copy()
+
+    def get_normals(self):
+        return self._a["n"].copy()
+
+    def get_uvs(self):
+        return self._a["uv"].copy()
+
+    def get_indices(self):
+        return self._a["index"].copy()
+
+
+TensorInteractions = namedtuple("TensorInteractions", "p n uv d index raw")
+
+
+def _split_records(raw):
+    """Views of a (N, 10) float32 tensor holding interaction records."""
+    import torch
+    return TensorInteractions(raw[:, 0:3], raw[:, 3:6], raw[:, 6:8], raw[:, 8], raw[:, 9].view(torch.int32), raw)
+
+
+# ------------------------------------------------------------ GPU scenes
+class _GPUScene:
+    DIM = 3
+
+    def __init__(self, fcpw_directory_path: str = "", print_logs: bool = False, device: int = 0):
+        # the directory argument of the reference locates Slang shaders; kernels here are precompiled
+        self.print_logs = bool(print_logs)
+        self.device = int(device)
+        handle = C.c_void_p()
+        check(lib().fcpwgb_gpu_scene_create(self.DIM, self.device, C.byref(handle)))
+        self._h = handle
+        self._cpu_bvh = None
+        self._n_vertices = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().fcpwgb_gpu_scene_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- transfer / refit --------------------------------------------------
+    def transfer_to_gpu(self, scene: _Scene, device_backend: str = "default") -> None:
+        """GPUScene::transferToGPU (include/fcpw/fcpw_gpu.h:21)."""
+        if device_backend not in ("default", "cuda"):
+            raise ValueError(f"unsupported device backend {device_backend!r}: this build runs on CUDA only")
+        if scene.DIM != self.DIM:
+            raise ValueError("scene dimension does not match the GPU scene")
+        if scene._vectorized:
+            raise ValueError("transfer_to_gpu needs a scene built with vectorize=False "
+                             "(include/fcpw/fcpw_gpu.h:17-20)")
+        bvh = scene.cpu_bvh
+        check(lib().fcpwgb_gpu_scene_transfer_cpu_bvh(self._h, bvh.handle))
+        self._cpu_bvh = bvh
+        self._n_vertices = bvh.info.n_vertices
+
+    def transfer_arrays(self, bvh_type: int, nodes, primitives, silhouettes=None, prim_vertices=None,
+                        n_vertices: int = 0) -> None:
+        """Uploads an already flattened tree in the interop layouts."""
+        nodes = np.ascontiguousarray(nodes)
+        primitives = np.ascontiguousarray(primitives)
+        sils = np.ascontiguousarray(silhouettes) if silhouettes is not None else None
+        pv = np.ascontiguousarray(prim_vertices, np.int32) if prim_vertices is not None else None
+        check(lib().fcpwgb_gpu_scene_transfer(self._h, int(bvh_type), ptr(nodes), len(nodes), ptr(primitives),
+                                              len(primitives), ptr(sils) if sils is not None and len(sils) else None,
+                                              len(sils) if sils is not None else 0, ptr(pv), int(n_vertices)))
+        self._n_vertices = int(n_vertices)
+
+    def refit(self, scene: _Scene, update_geometry: bool = True) -> None:
+        """GPUScene::refit (include/fcpw/fcpw_gpu.h:27): with update_geometry the moved
+        primitives (and silhouettes) are re-extracted from the scene and uploaded."""
+        if not update_geometry:
+            check(lib().fcpwgb_gpu_scene_refit(self._h, None, None))
+            return
+        bvh = scene.cpu_bvh
+        bvh.update_positions(scene.positions(0))
+        _, prims, sils = bvh.export()
+        check(lib().fcpwgb_gpu_scene_refit(self._h, ptr(prims), ptr(sils) if sils is not None and len(sils) else None))
+
+    def update_vertices_tensor(self, positions) -> None:
+        """Moves the vertices to ``positions`` (a CUDA float32 tensor (V, DIM) in the
+        caller's vertex order) and refits on the device, on the current torch stream."""
+        import torch
+        if positions.dtype != torch.float32 or not positions.is_cuda or not positions.is_contiguous():
+            raise ValueError("positions must be a contiguous float32 CUDA tensor")
+        stream = torch.cuda.current_stream(positions.device).cuda_stream
+        check(lib().fcpwgb_gpu_scene_update_vertices_device(self._h, positions.data_ptr(), positions.shape[0],
+                                                            C.c_void_p(stream)))
+
+    # -- queries -----------------------------------------------------------
+    def _out(self, interactions: GPUInteractionList, n: int) -> np.ndarray:
+        if not isinstance(interactions, GPUInteractionList):
+            raise TypeError("interactions must be a GPUInteractionList")
+        interactions._a = R.default_interactions(n)
+        return interactions._a
+
+    def intersect(self, *args, **kwargs) -> None:
+        """The four ``intersect`` overloads of python/fcpw_bindings.cpp:597-613."""
+        a0 = args[0] if args else kwargs.get("rays", kwargs.get("ray_origins", kwargs.get(
+            "bounding_spheres", kwargs.get("sphere_centers"))))
+        if isinstance(a0, GPURayList):
+            self._intersect_rays_list(*args, **kwargs)
+        elif isinstance(a0, GPUBoundingSphereList):
+            self._intersect_spheres_list(*args, **kwargs)
+        elif ("ray_origins" in kwargs) or (len(args) >= 3 and np.asarray(args[1]).ndim == 2
+                                           and np.asarray(args[2]).ndim == 1):
+            self._intersect_rays_arrays(*args, **kwargs)
+        else:
+            self._intersect_spheres_arrays(*args, **kwargs)
+
+    def _intersect_rays_arrays(self, ray_origins, ray_directions, ray_distance_bounds, interactions,
+                               check_for_occlusion: bool = False):
+        rays = R.make_rays(ray_origins, ray_directions, ray_distance_bounds)
+        self._run_rays(rays, interactions, check_for_occlusion)
+
+    def _intersect_rays_list(self, rays: GPURayList, interactions, check_for_occlusion: bool = False):
+        self._run_rays(rays.array(), interactions, check_for_occlusion)
+
+    def _run_rays(self, rays, interactions, occl):
+        out = self._out(interactions, len(rays))
+        check(lib().fcpwgb_intersect_rays(self._h, ptr(rays), ptr(out), len(rays), int(bool(occl))))
+
+    def _intersect_spheres_arrays(self, sphere_centers, sphere_squared_radii, rand_nums, interactions):
+        spheres = R.make_spheres(sphere_centers, sphere_squared_radii)
+        rn = np.zeros((len(spheres), 3), np.float32)
+        r = np.asarray(rand_nums, np.float32)
+        rn[:, : r.shape[1]] = r
+        self._run_spheres(spheres, rn, interactions)
+
+    def _intersect_spheres_list(self, bounding_spheres: GPUBoundingSphereList, rand_nums: GPUFloat3List,
+                                interactions):
+        self._run_spheres(bounding_spheres.array(), np.ascontiguousarray(rand_nums.array(), np.float32),
+                          interactions)
+
+    def _run_spheres(self, spheres, rn, interactions):
+        out = self._out(interactions, len(spheres))
+        check(lib().fcpwgb_intersect_spheres(self._h, ptr(spheres), ptr(rn), ptr(out), len(spheres)))
+
+    def find_closest_points(self, *args, **kwargs) -> None:
+        """python/fcpw_bindings.cpp:614-621"""
+        a0 = args[0] if args else kwargs.get("bounding_spheres", kwargs.get("query_points"))
+        if isinstance(a0, GPUBoundingSphereList):
+            return self._closest_list(*args, **kwargs)
+        return self._closest_arrays(*args, **kwargs)
+
+    def _closest_arrays(self, query_points, squared_max_radii, interactions, record_normals: bool = False):
+        spheres = R.make_spheres(query_points, squared_max_radii)
+        self._run_closest(spheres, interactions, record_normals)
+
+    def _closest_list(self, bounding_spheres, interactions, record_normals: bool = False):
+        self._run_closest(bounding_spheres.array(), interactions, record_normals)
+
+    def _run_closest(self, spheres, interactions, record_normals):
+        out = self._out(interactions, len(spheres))
+        check(lib().fcpwgb_find_closest_points(self._h, ptr(spheres), ptr(out), len(spheres),
+                                               int(bool(record_normals))))
+
+    def find_closest_silhouette_points(self, *args, **kwargs) -> None:
+        """python/fcpw_bindings.cpp:622-629"""
+        a0 = args[0] if args else kwargs.get("bounding_spheres", kwargs.get("query_points"))
+        if isinstance(a0, GPUBoundingSphereList):
+            return self._silhouette_list(*args, **kwargs)
+        return self._silhouette_arrays(*args, **kwargs)
+
+    def _silhouette_arrays(self, query_points, squared_max_radii, flip_normal_orientation, interactions,
+                           squared_min_radius: float = 0.0, precision: float = 1e-3):
+        spheres = R.make_spheres(query_points, squared_max_radii)
+        flip = np.ascontiguousarray(np.asarray(flip_normal_orientation).astype(np.uint32))
+        self._run_silhouette(spheres, flip, interactions, squared_min_radius, precision)
+
+    def _silhouette_list(self, bounding_spheres, flip_normal_orientation, interactions,
+                         squared_min_radius: float = 0.0, precision: float = 1e-3):
+        flip = flip_normal_orientation.array() if isinstance(flip_normal_orientation, Uint32List) else \
+            np.ascontiguousarray(np.asarray(flip_normal_orientation).astype(np.uint32))
+        self._run_silhouette(bounding_spheres.array(), flip, interactions, squared_min_radius, precision)
+
+    def _run_silhouette(self, spheres, flip, interactions, sq_min_r, precision):
+        if len(flip) != len(spheres):
+            raise ValueError("flip_normal_orientation must have one entry per query")
+        out = self._out(interactions, len(spheres))
+        check(lib().fcpwgb_find_closest_silhouette_points(self._h, ptr(spheres), ptr(flip), ptr(out), len(spheres),
+                                                          float(sq_min_r), float(precision)))
+
+    # -- zero-copy tensor entry points ---------------------------------------
+    @staticmethod
+    def _stream(t):
+        import torch
+        return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+
+    def _check_tensor(self, t, cols):
+        import torch
+        if t.dtype != torch.float32 or not t.is_cuda or not t.is_contiguous() or t.dim() != 2 or t.shape[1] != cols:
+            raise ValueError(f"expected a contiguous float32 CUDA tensor of shape (N, {cols})")
+
+    def find_closest_points_tensor(self, spheres, record_normals: bool = False, out=None) -> TensorInteractions:
+        """``spheres``: (N, 4) float32 CUDA tensor of (x, y, z, r2). Returns device views."""
+        import torch
+        self._check_tensor(spheres, 4)
+        n = spheres.shape[0]
+        raw = out if out is not None else torch.empty((n, 10), dtype=torch.float32, device=spheres.device)
+        check(lib().fcpwgb_find_closest_points_device(self._h, spheres.data_ptr(), raw.data_ptr(), n,
+                                                      int(bool(record_normals)), self._stream(spheres)))
+        return _split_records(raw)
+
+    def intersect_tensor(self, rays, check_for_occlusion: bool = False, out=None) -> TensorInteractions:
+        """``rays``: (N, 10) float32 CUDA tensor of (o, d, 1/d, tMax) records."""
+        import torch
+        self._check_tensor(rays, 10)
+        n = rays.shape[0]
+        raw = out if out is not None else torch.empty((n, 10), dtype=torch.float32, device=rays.device)
+        check(lib().fcpwgb_intersect_rays_device(self._h, rays.data_ptr(), raw.data_ptr(), n,
+                                                 int(bool(check_for_occlusion)), self._stream(rays)))
+        return _split_records(raw)
+
+    def check_errors(self) -> int:
+        w = C.c_uint32(0)
+        check(lib().fcpwgb_gpu_scene_check_errors(self._h, C.byref(w)))
+        return int(w.value)
+
+
+class GPUScene2D(_GPUScene):
+    DIM = 2
+
+
+class GPUScene3D(_GPUScene):
+    DIM = 3

@@ -1,0 +1,178 @@
+"""Host-side scene description and BVH producer: the subset of the reference's
+``fcpw.Scene2D/3D`` (python/fcpw_bindings.cpp:217-491) that the GPU path needs.
+
+A scene holds one object (vertex positions + line segments or triangles). ``build``
+runs the native binary SAH builder, which reproduces ``Scene<DIM>::build`` with
+``vectorize=False`` for a single object (include/fcpw/fcpw.inl:1053-1126).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from enum import IntEnum
+
+import numpy as np
+
+from . import records as R
+from ._lib import BvhInfo, check, lib, ptr
+
+
+class AggregateType(IntEnum):
+    """include/fcpw/utilities/scene_data.h:17-24"""
+    Baseline = 0
+    Bvh_LongestAxisCenter = 1
+    Bvh_OverlapSurfaceArea = 2
+    Bvh_SurfaceArea = 3
+    Bvh_OverlapVolume = 4
+    Bvh_Volume = 5
+
+
+class PrimitiveType(IntEnum):
+    LineSegment = 0
+    Triangle = 1
+
+
+class CpuBvh:
+    """Owner of a native host-built BVH (fcpwgb_cpu_bvh)."""
+
+    def __init__(self, dim: int, positions: np.ndarray, indices: np.ndarray, aggregate_type: int,
+                 with_silhouettes: bool):
+        positions = np.ascontiguousarray(positions, np.float32)
+        indices = np.ascontiguousarray(indices, np.int32)
+        if positions.ndim != 2 or positions.shape[1] != dim:
+            raise ValueError(f"positions must have shape (V, {dim})")
+        if indices.ndim != 2 or indices.shape[1] != dim:
+            raise ValueError(f"indices must have shape (N, {dim})")
+        handle = C.c_void_p()
+        check(lib().fcpwgb_cpu_bvh_build(dim, ptr(positions), positions.shape[0], ptr(indices), indices.shape[0],
+                                         int(aggregate_type), int(bool(with_silhouettes)), C.byref(handle)))
+        self._h = handle
+        self.dim = dim
+        info = BvhInfo()
+        check(lib().fcpwgb_cpu_bvh_info(self._h, C.byref(info)))
+        self.info = info
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().fcpwgb_cpu_bvh_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def snch(self) -> bool:
+        return self.info.bvh_type in (R.LINE_SEGMENT_SNCH, R.TRIANGLE_SNCH)
+
+    def export(self):
+        """Flattened tree in the interop layouts: (nodes, primitives, silhouettes)."""
+        i = self.info
+        nodes = np.zeros(i.n_nodes, R.SNCH_NODE if self.snch else R.BVH_NODE)
+        prims = np.zeros(i.n_primitives, R.TRIANGLE if self.dim == 3 else R.LINE_SEGMENT)
+        sils = np.zeros(i.n_silhouettes, R.EDGE if self.dim == 3 else R.VERTEX) if self.snch else None
+        check(lib().fcpwgb_cpu_bvh_export(self._h, ptr(nodes), ptr(prims), ptr(sils) if sils is not None and len(sils) else None))
+        return nodes, prims, sils
+
+    def topology(self):
+        """(index_map, prim_vertices (leaf order, caller numbering), prim_index, sil_vertices)"""
+        i = self.info
+        index_map = np.zeros(i.n_vertices, np.int32)
+        prim_vertices = np.zeros((i.n_primitives, self.dim), np.int32)
+        prim_index = np.zeros(i.n_primitives, np.uint32)
+        sil_vertices = np.zeros((i.n_silhouettes, self.dim + 1), np.int32) if self.snch else None
+        check(lib().fcpwgb_cpu_bvh_export_topology(self._h, ptr(index_map), ptr(prim_vertices), ptr(prim_index),
+                                                   ptr(sil_vertices) if sil_vertices is not None and len(sil_vertices) else None))
+        return index_map, prim_vertices, prim_index, sil_vertices
+
+    def update_positions(self, positions: np.ndarray) -> None:
+        positions = np.ascontiguousarray(positions, np.float32)
+        if positions.shape != (self.info.n_vertices, self.dim):
+            raise ValueError("positions must keep the vertex count")
+        check(lib().fcpwgb_cpu_bvh_update_positions(self._h, ptr(positions)))
+
+
+class _Scene:
+    DIM = 3
+
+    def __init__(self):
+        self._positions: list = []
+        self._indices: list = []
+        self._silhouettes = False
+        self._bvh: CpuBvh | None = None
+        self._vectorized = False
+        self._aggregate_type = None
+
+    # -- geometry ---------------------------------------------------------
+    def set_object_count(self, n_objects: int) -> None:
+        self._positions = [None] * int(n_objects)
+        self._indices = [None] * int(n_objects)
+        self._bvh = None
+
+    def set_object_vertices(self, positions, object_index: int) -> None:
+        p = np.asarray(positions, np.float32)
+        if p.ndim != 2 or p.shape[1] != self.DIM:
+            raise ValueError(f"positions must have shape (V, {self.DIM})")
+        self._positions[object_index] = np.ascontiguousarray(p)
+
+    def _set_indices(self, indices, object_index: int) -> None:
+        ix = np.asarray(indices, np.int32)
+        if ix.ndim != 2 or ix.shape[1] != self.DIM:
+            raise ValueError(f"indices must have shape (N, {self.DIM})")
+        self._indices[object_index] = np.ascontiguousarray(ix)
+
+    def compute_silhouettes(self, ignore_silhouette=None) -> None:
+        """Scene::computeSilhouettes (fcpw.inl:428-521). Custom ignore callbacks are not supported."""
+        if ignore_silhouette is not None:
+            raise NotImplementedError("ignore_silhouette callbacks are not supported by the GPU producer")
+        self._silhouettes = True
+
+    def build(self, aggregate_type, vectorize: bool, print_stats: bool = False,
+              reduce_memory_footprint: bool = False) -> None:
+        if len(self._positions) != 1 or self._positions[0] is None or self._indices[0] is None:
+            raise ValueError("the GPU path supports scenes with exactly one object "
+                             "(include/fcpw/fcpw_gpu.h:17-20)")
+        self._vectorized = bool(vectorize)
+        self._aggregate_type = AggregateType(int(aggregate_type))
+        self._bvh = CpuBvh(self.DIM, self._positions[0], self._indices[0], int(aggregate_type), self._silhouettes)
+        if print_stats:
+            i = self._bvh.info
+            print(f"BVH stats: {i.n_nodes} nodes, {i.n_leaves} leaves, {i.max_depth} max depth, "
+                  f"{i.n_primitives} primitives, {i.n_silhouettes} silhouetteRefs")
+
+    def update_object_vertex(self, position, vertex_index: int, object_index: int) -> None:
+        self._positions[object_index][vertex_index] = np.asarray(position, np.float32)[: self.DIM]
+
+    def update_object_vertices(self, positions, object_index: int) -> None:
+        p = np.asarray(positions, np.float32)
+        self._positions[object_index][: len(p)] = p
+
+    # -- accessors used by GPUScene ---------------------------------------
+    @property
+    def cpu_bvh(self) -> CpuBvh:
+        if self._bvh is None:
+            raise RuntimeError("Scene.build has not been called")
+        return self._bvh
+
+    def positions(self, object_index: int = 0) -> np.ndarray:
+        return self._positions[object_index]
+
+    def indices(self, object_index: int = 0) -> np.ndarray:
+        return self._indices[object_index]
+
+
+class Scene2D(_Scene):
+    DIM = 2
+
+    def set_object_line_segments(self, indices, object_index: int) -> None:
+        self._set_indices(indices, object_index)
+
+
+class Scene3D(_Scene):
+    DIM = 3
+
+    def set_object_triangles(self, indices, object_index: int) -> None:
+        self._set_indices(indices, object_index)

@@ -1,0 +1,235 @@
+/*
+ * fcpw_gb300 — C ABI of the GB300-native GPU query path for FCPW scenes.
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (FCPWGB_OK on success). A human-readable message for the last failure on the
+ * calling thread is available from fcpwgb_last_error().
+ *
+ * The record types below are byte-identical to the interop structs of the
+ * reference GPU path (include/fcpw/gpu/bvh_interop_structures.h:14-28,55-162,
+ * 730-774), so arrays built for the reference's GPUScene can be passed as-is.
+ *
+ * Threading: like the reference ("GPU queries are not thread-safe",
+ * include/fcpw/fcpw_gpu.h:30) a scene handle must not be used from two host
+ * threads at once. Different handles are independent.
+ */
+#ifndef FCPW_GB300_H
+#define FCPW_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#define FCPWGB_ALIGN8 alignas(8)
+#else
+#define FCPWGB_ALIGN8 _Alignas(8)
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define FCPWGB_OK                   0
+#define FCPWGB_ERR_INVALID_ARGUMENT 1
+#define FCPWGB_ERR_CUDA             2
+#define FCPWGB_ERR_NOT_TRANSFERRED  3
+#define FCPWGB_ERR_UNSUPPORTED      4
+#define FCPWGB_ERR_OUT_OF_MEMORY    5
+#define FCPWGB_ERR_TRAVERSAL        6 /* a device traversal overflowed its stack or step budget */
+
+/* FCPW_GPU_UINT_MAX, include/fcpw/gpu/bvh_interop_structures.h:10 */
+#define FCPWGB_UINT_MAX 4294967295u
+
+/* BVH flavours, same numbering as FCPW_BVH_TYPE (include/fcpw/fcpw_gpu.inl:3-6) */
+#define FCPWGB_LINE_SEGMENT_BVH  1
+#define FCPWGB_TRIANGLE_BVH      2
+#define FCPWGB_LINE_SEGMENT_SNCH 3
+#define FCPWGB_TRIANGLE_SNCH     4
+
+/* AggregateType numbering (include/fcpw/utilities/scene_data.h:17-24) */
+#define FCPWGB_AGGREGATE_BASELINE              0
+#define FCPWGB_AGGREGATE_BVH_LONGEST_AXIS      1
+#define FCPWGB_AGGREGATE_BVH_OVERLAP_SURFACE   2
+#define FCPWGB_AGGREGATE_BVH_SURFACE_AREA      3
+#define FCPWGB_AGGREGATE_BVH_OVERLAP_VOLUME    4
+#define FCPWGB_AGGREGATE_BVH_VOLUME            5
+
+/* ------------------------------------------------------- record layouts */
+typedef struct { FCPWGB_ALIGN8 float x; float y; } fcpwgb_float2;        /* 8 B, align 8 */
+typedef struct { float x, y, z; } fcpwgb_float3;                          /* 12 B */
+
+typedef struct { fcpwgb_float3 pMin, pMax; } fcpwgb_bounding_box;         /* 24 B */
+typedef struct { fcpwgb_float3 axis; float halfAngle, radius; } fcpwgb_bounding_cone; /* 20 B */
+
+typedef struct {                                                          /* 32 B, GPUBvhNode */
+    fcpwgb_bounding_box box;
+    uint32_t nPrimitives;
+    uint32_t offset;          /* leaf: first primitive; inner: right-child offset (left = i + 1) */
+} fcpwgb_bvh_node;
+
+typedef struct {                                                          /* 60 B, GPUSnchNode */
+    fcpwgb_bounding_box box;
+    fcpwgb_bounding_cone cone;
+    uint32_t nPrimitives;
+    uint32_t offset;
+    uint32_t nSilhouettes;
+    uint32_t silhouetteOffset;
+} fcpwgb_snch_node;
+
+typedef struct { fcpwgb_float3 pa, pb; uint32_t index; } fcpwgb_line_segment;      /* 28 B */
+typedef struct { fcpwgb_float3 pa, pb, pc; uint32_t index; } fcpwgb_triangle;      /* 40 B */
+typedef struct { fcpwgb_float3 p, n0, n1; uint32_t index, hasOneAdjacentFace; } fcpwgb_vertex; /* 44 B */
+typedef struct { fcpwgb_float3 pa, pb, n0, n1; uint32_t index, hasOneAdjacentFace; } fcpwgb_edge; /* 56 B */
+
+typedef struct { fcpwgb_float3 o, d, dInv; float tMax; } fcpwgb_ray;               /* 40 B, GPURay */
+typedef struct { fcpwgb_float3 c; float r2; } fcpwgb_bounding_sphere;              /* 16 B */
+
+typedef struct {                                                          /* 40 B, GPUInteraction */
+    fcpwgb_float3 p;
+    fcpwgb_float3 n;
+    fcpwgb_float2 uv;
+    float d;
+    uint32_t index;
+} fcpwgb_interaction;
+
+/* ------------------------------------------------------------- library */
+const char *fcpwgb_last_error(void);
+const char *fcpwgb_version(void);
+/* number of CUDA devices visible (0 when none); never fails */
+int fcpwgb_device_count(void);
+
+/* ------------------------------------------------ CPU-side BVH producer
+ * Builds the binary SAH BVH on the host exactly as the reference's
+ * Scene<DIM>::build(aggregateType, vectorize=false) does for a single object
+ * (include/fcpw/fcpw.inl:796-867,1053-1126; include/fcpw/aggregates/bvh.inl:40-234),
+ * including the leaf-order vertex renumbering (fcpw.inl:613-758) and, when
+ * with_silhouettes is set, the SNCH silhouette references and bounding cones
+ * (fcpw.inl:405-521, bvh.inl:236-425). dim is 2 (line segments, indices has
+ * 2 ints per primitive) or 3 (triangles, 3 ints per primitive). positions has
+ * dim floats per vertex in the caller's vertex order.
+ */
+typedef struct fcpwgb_cpu_bvh fcpwgb_cpu_bvh;
+
+typedef struct {
+    int dim;
+    int bvh_type;            /* FCPWGB_*_BVH / FCPWGB_*_SNCH */
+    uint32_t n_nodes;
+    uint32_t n_leaves;
+    uint32_t max_depth;
+    uint32_t n_primitives;
+    uint32_t n_silhouettes;  /* silhouette references (SNCH only) */
+    uint32_t n_vertices;
+} fcpwgb_bvh_info;
+
+int fcpwgb_cpu_bvh_build(int dim, const float *positions, uint32_t n_vertices,
+                         const int32_t *indices, uint32_t n_primitives,
+                         int aggregate_type, int with_silhouettes,
+                         fcpwgb_cpu_bvh **out);
+void fcpwgb_cpu_bvh_destroy(fcpwgb_cpu_bvh *bvh);
+int fcpwgb_cpu_bvh_info(const fcpwgb_cpu_bvh *bvh, fcpwgb_bvh_info *info);
+/* Writes the flattened tree in the reference interop layouts
+ * (extractBvhNodes / extractSnchNodes / extractTriangles / extractLineSegments /
+ * extractSilhouetteEdges / extractSilhouetteVertices,
+ * bvh_interop_structures.h:172-298). nodes receives n_nodes fcpwgb_bvh_node
+ * (BVH) or fcpwgb_snch_node (SNCH); primitives n_primitives triangles or
+ * segments; silhouettes n_silhouettes edges or vertices (may be NULL for BVH).
+ * Any output pointer may be NULL to skip it. */
+int fcpwgb_cpu_bvh_export(const fcpwgb_cpu_bvh *bvh, void *nodes, void *primitives,
+                          void *silhouettes);
+/* index_map[v] = leaf-order position of caller vertex v (PolygonSoup::indexMap,
+ * -1 for unreferenced vertices); prim_vertices[k*dim + j] = caller vertex
+ * index of corner j of the k-th primitive in leaf order; prim_index[k] =
+ * original primitive index; sil_vertices[s*(dim+1) + j] = caller vertex index
+ * j of silhouette reference s (SilhouetteEdge::indices[4] /
+ * SilhouetteVertex::indices[3], -1 where a face is missing). */
+int fcpwgb_cpu_bvh_export_topology(const fcpwgb_cpu_bvh *bvh, int32_t *index_map,
+                                   int32_t *prim_vertices, uint32_t *prim_index,
+                                   int32_t *sil_vertices);
+/* updateObjectVertices (fcpw.inl:1129-1143): replaces the vertex positions
+ * (caller vertex order) so that a following export yields the moved
+ * primitives and silhouettes. The tree itself is left unchanged. */
+int fcpwgb_cpu_bvh_update_positions(fcpwgb_cpu_bvh *bvh, const float *positions);
+
+/* ------------------------------------------------------------ GPU scene
+ * Replaces fcpw::GPUScene<DIM> (include/fcpw/fcpw_gpu.h:8-91). One scene owns
+ * one CUDA stream and its device buffers, reused across calls. */
+typedef struct fcpwgb_gpu_scene fcpwgb_gpu_scene;
+
+/* GPUScene ctor, fcpw_gpu.h:12 (the shader directory has no meaning here). */
+int fcpwgb_gpu_scene_create(int dim, int device, fcpwgb_gpu_scene **out);
+void fcpwgb_gpu_scene_destroy(fcpwgb_gpu_scene *scene);
+
+/* transferToGPU, fcpw_gpu.h:21 / bvh_interop_structures.h:694-728: uploads a
+ * flattened binary tree in the interop layouts. prim_vertices (optional, may
+ * be NULL) lists the caller vertex index of every primitive corner in leaf
+ * order, which enables fcpwgb_gpu_scene_update_vertices_device. */
+int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *scene, int bvh_type,
+                              const void *nodes, uint32_t n_nodes,
+                              const void *primitives, uint32_t n_primitives,
+                              const void *silhouettes, uint32_t n_silhouettes,
+                              const int32_t *prim_vertices, uint32_t n_vertices);
+/* convenience: transferToGPU straight from a host-built BVH */
+int fcpwgb_gpu_scene_transfer_cpu_bvh(fcpwgb_gpu_scene *scene, const fcpwgb_cpu_bvh *bvh);
+
+/* refit, fcpw_gpu.h:27 / bvh_interop_structures.h:891-934. When primitives
+ * (and, for SNCH, silhouettes) are non-NULL they replace the device copies
+ * first (updateGeometry=true); with NULL the device geometry is refit as is
+ * (updateGeometry=false). Bottom-up in a single launch. Synchronous. */
+int fcpwgb_gpu_scene_refit(fcpwgb_gpu_scene *scene, const void *primitives,
+                           const void *silhouettes);
+/* Device-side geometry update + refit for differentiable pipelines: positions
+ * is a device array of n_vertices*dim floats in caller vertex order. The
+ * primitive (and silhouette) records are regathered on the device and the
+ * tree refit; asynchronous on stream (a cudaStream_t, NULL = scene stream). */
+int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *scene, const float *positions,
+                                            uint32_t n_vertices, void *stream);
+
+/* ----- queries with HOST arrays (synchronous, as the reference) ----- */
+/* findClosestPoints, fcpw_gpu.h:60-62 */
+int fcpwgb_find_closest_points(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                               fcpwgb_interaction *interactions, uint32_t n, int record_normals);
+/* intersect(rays), fcpw_gpu.h:38-40 */
+int fcpwgb_intersect_rays(fcpwgb_gpu_scene *scene, const fcpwgb_ray *rays,
+                          fcpwgb_interaction *interactions, uint32_t n, int check_for_occlusion);
+/* intersect(spheres, randNums), fcpw_gpu.h:50-52 */
+int fcpwgb_intersect_spheres(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                             const fcpwgb_float3 *rand_nums, fcpwgb_interaction *interactions,
+                             uint32_t n);
+/* findClosestSilhouettePoints, fcpw_gpu.h:73-76 */
+int fcpwgb_find_closest_silhouette_points(fcpwgb_gpu_scene *scene,
+                                          const fcpwgb_bounding_sphere *spheres,
+                                          const uint32_t *flip_normal_orientation,
+                                          fcpwgb_interaction *interactions, uint32_t n,
+                                          float squared_min_radius, float precision);
+
+/* ----- queries with DEVICE arrays (asynchronous on stream; NULL = scene stream) ----- */
+int fcpwgb_find_closest_points_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                      fcpwgb_interaction *interactions, uint32_t n,
+                                      int record_normals, void *stream);
+int fcpwgb_intersect_rays_device(fcpwgb_gpu_scene *scene, const fcpwgb_ray *rays,
+                                 fcpwgb_interaction *interactions, uint32_t n,
+                                 int check_for_occlusion, void *stream);
+int fcpwgb_intersect_spheres_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                    const fcpwgb_float3 *rand_nums,
+                                    fcpwgb_interaction *interactions, uint32_t n, void *stream);
+int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *scene,
+                                                 const fcpwgb_bounding_sphere *spheres,
+                                                 const uint32_t *flip_normal_orientation,
+                                                 fcpwgb_interaction *interactions, uint32_t n,
+                                                 float squared_min_radius, float precision,
+                                                 void *stream);
+
+/* Runs the closest point query of the scene's current variant over device
+ * spheres in counting mode and returns, synchronously, stats[0] = queries,
+ * stats[1] = popped (loaded) nodes, stats[2] = expanded inner nodes,
+ * stats[3] = primitive tests, summed over all queries. Used to compute the
+ * algorithmic bytes of a launch; results are written to interactions. */
+int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                          fcpwgb_interaction *interactions, uint32_t n, uint64_t *stats);
+
+/* Reads and clears the device error word of the scene (stack overflow or
+ * step budget exhausted in a traversal). Synchronises the scene stream. */
+int fcpwgb_gpu_scene_check_errors(fcpwgb_gpu_scene *scene, uint32_t *error_word);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FCPW_GB300_H */

@@ -1,0 +1,143 @@
+"""ctypes wrapper of the C oracle (TEST INFRASTRUCTURE ONLY).
+
+Used by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg as
+the checker; the product never imports this module. Every function takes and
+returns numpy arrays in the interop record layouts of fcpw_gb300.records.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import ORACLE_LIB, build_oracle
+
+_lib = None
+P = C.c_void_p
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = build_oracle()
+        _lib = C.CDLL(str(path))
+        i, u, f = C.c_int, C.c_uint32, C.c_float
+        sig = {
+            "oracle_closest_points_bvh": [i, i, P, P, P, u, i, P, P, i],
+            "oracle_closest_points_brute": [i, P, u, P, u, P, i],
+            "oracle_closest_points_brute_f64": [i, P, u, P, u, P, P, i],
+            "oracle_intersect_rays_bvh": [i, i, P, P, P, u, i, P, P, i],
+            "oracle_intersect_rays_brute_f64": [i, P, u, P, u, P, P, i],
+            "oracle_silhouettes_bvh": [i, P, P, P, P, u, f, f, P, i],
+            "oracle_sphere_sample_bvh": [i, i, P, P, P, P, u, P, P, i],
+            "oracle_refit": [i, i, P, P, P],
+            "oracle_prim_distance_f64": [i, P, u, P, P, u, P],
+            "oracle_record_sizes": [P],
+        }
+        for name, args in sig.items():
+            fn = getattr(_lib, name)
+            fn.restype = C.c_int
+            fn.argtypes = args
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def threads(n: int | None = None) -> int:
+    return n if n else (os.cpu_count() or 1)
+
+
+def _records():
+    from fcpw_gb300 import records as R
+    return R
+
+
+def closest_points_bvh(dim, nodes, prims, spheres, record_normals=False, nthreads=None, visited=False):
+    R = _records()
+    snch = nodes.dtype == R.SNCH_NODE
+    out = R.default_interactions(len(spheres))
+    nv = np.zeros(len(spheres), np.uint32) if visited else None
+    _load().oracle_closest_points_bvh(dim, int(snch), _p(nodes), _p(prims), _p(spheres), len(spheres),
+                                      int(record_normals), _p(out), _p(nv), threads(nthreads))
+    return (out, nv) if visited else out
+
+
+def closest_points_brute(dim, prims, spheres, nthreads=None):
+    R = _records()
+    out = R.default_interactions(len(spheres))
+    _load().oracle_closest_points_brute(dim, _p(prims), len(prims), _p(spheres), len(spheres), _p(out),
+                                        threads(nthreads))
+    return out
+
+
+def closest_points_brute_f64(dim, prims, spheres, nthreads=None):
+    d = np.zeros(len(spheres), np.float64)
+    idx = np.zeros(len(spheres), np.uint32)
+    _load().oracle_closest_points_brute_f64(dim, _p(prims), len(prims), _p(spheres), len(spheres), _p(d), _p(idx),
+                                            threads(nthreads))
+    return d, idx
+
+
+def intersect_rays_bvh(dim, nodes, prims, rays, occlusion=False, nthreads=None):
+    R = _records()
+    snch = nodes.dtype == R.SNCH_NODE
+    out = R.default_interactions(len(rays))
+    hit = np.zeros(len(rays), np.int32)
+    _load().oracle_intersect_rays_bvh(dim, int(snch), _p(nodes), _p(prims), _p(rays), len(rays), int(occlusion),
+                                      _p(out), _p(hit), threads(nthreads))
+    return out, hit.astype(bool)
+
+
+def intersect_rays_brute_f64(dim, prims, rays, nthreads=None):
+    t = np.zeros(len(rays), np.float64)
+    idx = np.zeros(len(rays), np.uint32)
+    _load().oracle_intersect_rays_brute_f64(dim, _p(prims), len(prims), _p(rays), len(rays), _p(t), _p(idx),
+                                            threads(nthreads))
+    return t, idx
+
+
+def silhouettes_bvh(dim, snch_nodes, sils, spheres, flip, squared_min_radius=0.0, precision=1e-3, nthreads=None):
+    R = _records()
+    out = R.default_interactions(len(spheres))
+    flip = np.ascontiguousarray(flip, np.uint32)
+    _load().oracle_silhouettes_bvh(dim, _p(snch_nodes), _p(sils), _p(spheres), _p(flip), len(spheres),
+                                   float(squared_min_radius), float(precision), _p(out), threads(nthreads))
+    return out
+
+
+def sphere_sample_bvh(dim, nodes, prims, spheres, rand_nums, nthreads=None):
+    R = _records()
+    snch = nodes.dtype == R.SNCH_NODE
+    out = R.default_interactions(len(spheres))
+    hit = np.zeros(len(spheres), np.int32)
+    rn = np.ascontiguousarray(rand_nums, np.float32)
+    _load().oracle_sphere_sample_bvh(dim, int(snch), _p(nodes), _p(prims), _p(spheres), _p(rn), len(spheres),
+                                     _p(out), _p(hit), threads(nthreads))
+    return out, hit.astype(bool)
+
+
+def refit(dim, nodes, prims, sils=None):
+    R = _records()
+    nodes = nodes.copy()
+    _load().oracle_refit(dim, int(nodes.dtype == R.SNCH_NODE), _p(nodes), _p(prims), _p(sils))
+    return nodes
+
+
+def prim_distance_f64(dim, prims, positions_in_array, points):
+    """FP64 distance from points[q] to prims[positions_in_array[q]]."""
+    pos = np.ascontiguousarray(positions_in_array, np.uint32)
+    x = np.zeros((len(pos), 3), np.float32)
+    pts = np.asarray(points, np.float32)
+    x[:, : pts.shape[1]] = pts
+    out = np.zeros(len(pos), np.float64)
+    _load().oracle_prim_distance_f64(dim, _p(prims), len(prims), _p(pos), _p(x), len(pos), _p(out))
+    return out
+
+
+def record_sizes():
+    s = (C.c_int * 9)()
+    _load().oracle_record_sizes(s)
+    return list(s)

@@ -1,0 +1,294 @@
+"""GPU parity tests of the binary-tree kernels through the C ABI, against the C
+oracle (the reference CPU algorithms restated) and an FP64 brute force."""
+import numpy as np
+import pytest
+
+import fcpw_gb300 as F
+from fcpw_gb300 import records as R
+from fcpw_gb300 import workloads as W
+from helpers import EPS32, build_scene, compare_closest, distance_tolerance
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sphere20k():
+    v, f = W.perturbed_sphere(32, W.SEED_BASE + 1)
+    s = build_scene(3, v, f)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    return s, g
+
+
+@pytest.fixture(scope="module")
+def stars2d():
+    v, sg = W.star_polylines(64, 128, W.SEED_BASE + 3)
+    s = build_scene(2, v, sg, silhouettes=True)
+    g = F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    return s, g
+
+
+def _closest(g, pts, r2, record_normals=False):
+    out = F.GPUInteractionList()
+    g.find_closest_points(pts, np.broadcast_to(np.float32(r2), (len(pts),)).copy(), out, record_normals)
+    return out.array()
+
+
+def test_closest_point_icosphere_infinite_radius(sphere20k):
+    s, g = sphere20k
+    pts = W.uniform_points(1 << 18, 3, -1.5, 1.5, 11)
+    got = _closest(g, pts, R.FLT_MAX)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref = O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts, R.FLT_MAX))
+    st = compare_closest(3, prims, pts, got, ref)
+    assert st["found"] == len(pts)
+    assert g.check_errors() == 0
+
+
+def test_closest_point_against_fp64_brute_force(sphere20k):
+    s, g = sphere20k
+    pts = W.uniform_points(2048, 3, -1.5, 1.5, 12)
+    got = _closest(g, pts, R.FLT_MAX)
+    _, prims, _ = s.cpu_bvh.export()
+    d64, _ = O.closest_points_brute_f64(3, prims, R.make_spheres(pts, R.FLT_MAX))
+    tol = distance_tolerance(pts, got["p"], d64)
+    assert np.all(np.abs(got["d"] - d64) <= tol)
+
+
+def test_closest_point_finite_radius_and_normals(sphere20k):
+    s, g = sphere20k
+    pts = W.uniform_points(50000, 3, -1.5, 1.5, 13)
+    r2 = (0.1 * W.rng(14).uniform(0, 1, len(pts)) * 3.0).astype(np.float32)  # 0.1*U*|extent| as in tests/gpu_tests.cpp:65
+    out = F.GPUInteractionList()
+    g.find_closest_points(pts, r2, out, True)
+    got = out.array()
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref = O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts, r2), record_normals=True)
+    compare_closest(3, prims, pts, got, ref)
+    m = ref["index"] != R.UINT_MAX
+    assert 0 < m.sum() < len(pts)
+    same = got["index"] == ref["index"]
+    assert np.allclose(got["n"][same], ref["n"][same], atol=1e-6)
+    assert np.allclose(np.linalg.norm(got["n"][m], axis=1), 1.0, atol=1e-5)
+    # misses keep the reference defaults
+    miss = ~m
+    assert np.all(got["d"][miss] == R.FLT_MAX) and np.all(got["index"][miss] == R.UINT_MAX)
+
+
+def test_closest_point_device_tensor_matches_host(sphere20k):
+    import torch
+    s, g = sphere20k
+    pts = W.uniform_points(100000, 3, -1.5, 1.5, 15)
+    host = _closest(g, pts, R.FLT_MAX)
+    sph = torch.zeros((len(pts), 4), dtype=torch.float32, device="cuda")
+    sph[:, :3] = torch.from_numpy(pts).cuda()
+    sph[:, 3] = float(R.FLT_MAX)
+    res = g.find_closest_points_tensor(sph)
+    torch.cuda.synchronize()
+    raw = res.raw.cpu().numpy().view(R.INTERACTION).reshape(-1)
+    assert np.array_equal(raw["index"], host["index"])
+    assert np.array_equal(raw["d"], host["d"])
+
+
+def test_closest_point_2d_segments(stars2d):
+    s, g = stars2d
+    pts = W.uniform_points(100000, 2, -3, 3, 16)
+    got = _closest(g, pts, R.FLT_MAX)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref = O.closest_points_bvh(2, nodes, prims, R.make_spheres(pts, R.FLT_MAX))
+    compare_closest(2, prims, pts, got, ref)
+    assert np.all(got["p"][:, 2] == 0.0)
+
+
+def _ray_compare(got, ref_out, ref_hit, occl=False):
+    g_hit = got["index"] != R.UINT_MAX
+    mism = g_hit != ref_hit
+    # grazing rays through shared edges/vertices may flip between FP32 implementations
+    assert mism.sum() <= max(2, int(1e-4 * len(got))), f"{mism.sum()} hit/miss disagreements"
+    both = g_hit & ref_hit
+    if not occl:
+        tol = 1e-5 * np.maximum(ref_out["d"][both], 1.0)
+        assert np.all(np.abs(got["d"][both] - ref_out["d"][both]) <= tol)
+        same = got["index"][both] == ref_out["index"][both]
+        assert same.mean() > 0.999
+
+
+def test_rays_torus():
+    v, f = W.torus(128, 64, W.SEED_BASE + 2)
+    s = build_scene(3, v, f)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    n = 100000
+    o = W.uniform_points(n, 3, -2, 2, 17)
+    d = W.uniform_directions(n, 3, 18)
+    tmax = np.full(n, R.FLT_MAX, np.float32)
+    out = F.GPUInteractionList()
+    g.intersect(o, d, tmax, out)
+    got = out.array()
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref, hit = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax))
+    _ray_compare(got, ref, hit)
+    assert 0.2 < hit.mean() < 0.9
+    # occlusion variant
+    out2 = F.GPUInteractionList()
+    g.intersect(o, d, tmax, out2, True)
+    ref2, hit2 = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax), occlusion=True)
+    _ray_compare(out2.array(), ref2, hit2, occl=True)
+    # FP64 brute force agreement on a sample
+    t64, i64 = O.intersect_rays_brute_f64(3, prims, R.make_rays(o[:2000], d[:2000], tmax[:2000]))
+    h64 = np.isfinite(t64)
+    gh = got["index"][:2000] != R.UINT_MAX
+    assert (h64 != gh).sum() <= 2
+    both = h64 & gh
+    assert np.all(np.abs(got["d"][:2000][both] - t64[both]) <= 1e-5 * np.maximum(t64[both], 1))
+
+
+def test_rays_2d(stars2d):
+    s, g = stars2d
+    n = 50000
+    o = W.uniform_points(n, 2, -3, 3, 19)
+    d = W.uniform_directions(n, 2, 20)
+    tmax = np.full(n, R.FLT_MAX, np.float32)
+    out = F.GPUInteractionList()
+    g.intersect(o, d, tmax, out)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref, hit = O.intersect_rays_bvh(2, nodes, prims, R.make_rays(o, d, tmax))
+    _ray_compare(out.array(), ref, hit)
+
+
+def test_silhouettes_2d(stars2d):
+    s, g = stars2d
+    n = 50000
+    pts = W.uniform_points(n, 2, -3, 3, 21)
+    flip = (W.rng(22).uniform(0, 1, n) < 0.5).astype(np.uint32)
+    out = F.GPUInteractionList()
+    g.find_closest_silhouette_points(pts, np.full(n, R.FLT_MAX, np.float32), flip, out, 0.0, 1e-3)
+    got = out.array()
+    nodes, _, sils = s.cpu_bvh.export()
+    ref = O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts, R.FLT_MAX), flip)
+    fg, fr = got["index"] != R.UINT_MAX, ref["index"] != R.UINT_MAX
+    assert (fg != fr).sum() <= max(2, int(1e-4 * n))
+    both = fg & fr
+    tol = distance_tolerance(pts[both], ref["p"][both][:, :2], ref["d"][both])
+    assert np.all(np.abs(got["d"][both] - ref["d"][both]) <= 1e-3 * ref["d"][both] + tol)
+
+
+def test_silhouettes_3d():
+    v, f = W.torus(64, 32, W.SEED_BASE + 2)
+    s = build_scene(3, v, f, silhouettes=True)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    n = 20000
+    pts = W.uniform_points(n, 3, -2, 2, 23)
+    flip = np.zeros(n, np.uint32)
+    out = F.GPUInteractionList()
+    g.find_closest_silhouette_points(pts, np.full(n, R.FLT_MAX, np.float32), flip, out)
+    got = out.array()
+    nodes, _, sils = s.cpu_bvh.export()
+    ref = O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pts, R.FLT_MAX), flip)
+    fg, fr = got["index"] != R.UINT_MAX, ref["index"] != R.UINT_MAX
+    assert (fg != fr).sum() <= max(2, int(1e-4 * n))
+    both = fg & fr
+    # silhouette test uses a precision threshold (1e-3), as in tests/aggregate_tests.cpp:610
+    assert np.all(np.abs(got["d"][both] - ref["d"][both]) <= 1e-3 * np.maximum(ref["d"][both], 1e-3))
+    # closest point queries still work on an SNCH tree
+    cp = _closest(g, pts, R.FLT_MAX)
+    nodes, prims, _ = s.cpu_bvh.export()
+    compare_closest(3, prims, pts, cp, O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts, R.FLT_MAX)))
+
+
+def test_sphere_sampling(sphere20k):
+    s, g = sphere20k
+    n = 50000
+    c = W.uniform_points(n, 3, -1.2, 1.2, 24)
+    r2 = (W.rng(25).uniform(0.01, 0.3, n) ** 2).astype(np.float32)
+    rn = W.rng(26).uniform(0, 1, (n, 3)).astype(np.float32)
+    out = F.GPUInteractionList()
+    g.intersect(c, r2, rn, out)
+    got = out.array()
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref, hit = O.sphere_sample_bvh(3, nodes, prims, R.make_spheres(c, r2), rn)
+    gh = got["index"] != R.UINT_MAX
+    assert (gh != hit).sum() <= max(2, int(1e-4 * n))
+    both = gh & hit
+    same = got["index"][both] == ref["index"][both]
+    assert same.mean() > 0.999
+    assert np.allclose(got["d"][both][same], ref["d"][both][same], rtol=1e-4)
+    assert np.allclose(got["p"][both][same], ref["p"][both][same], atol=1e-5)
+
+
+def _moved(v, seed, amp=0.02):
+    return (v + amp * W.rng(seed).standard_normal(v.shape)).astype(np.float32)
+
+
+def test_refit_host_update_matches_oracle():
+    v, f = W.perturbed_sphere(16, W.SEED_BASE + 5)
+    s = build_scene(3, v, f)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    v2 = _moved(v, 27)
+    s.update_object_vertices(v2, 0)
+    g.refit(s, True)
+    nodes, prims, _ = s.cpu_bvh.export()  # prims re-extracted from the moved positions
+    ref_nodes = O.refit(3, nodes, prims)
+    pts = W.uniform_points(20000, 3, -1.5, 1.5, 28)
+    got = _closest(g, pts, R.FLT_MAX)
+    ref = O.closest_points_bvh(3, ref_nodes, prims, R.make_spheres(pts, R.FLT_MAX))
+    compare_closest(3, prims, pts, got, ref)
+
+
+def test_update_vertices_device_matches_host_refit():
+    import torch
+    v, f = W.perturbed_sphere(16, W.SEED_BASE + 6)
+    s = build_scene(3, v, f)
+    g_host, g_dev = F.GPUScene3D(), F.GPUScene3D()
+    g_host.transfer_to_gpu(s)
+    g_dev.transfer_to_gpu(s)
+    v2 = _moved(v, 29)
+    g_dev.update_vertices_tensor(torch.from_numpy(v2).cuda())
+    torch.cuda.synchronize()
+    s.update_object_vertices(v2, 0)
+    g_host.refit(s, True)
+    pts = W.uniform_points(20000, 3, -1.5, 1.5, 30)
+    a, b = _closest(g_host, pts, R.FLT_MAX), _closest(g_dev, pts, R.FLT_MAX)
+    assert np.array_equal(a["index"], b["index"]) and np.array_equal(a["d"], b["d"])
+
+
+def test_refit_snch_keeps_silhouette_results():
+    v, sg = W.star_polylines(16, 64, W.SEED_BASE + 7)
+    s = build_scene(2, v, sg, silhouettes=True)
+    g = F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    v2 = _moved(v, 31, amp=0.002)
+    s.update_object_vertices(v2, 0)
+    g.refit(s, True)
+    nodes, prims, sils = s.cpu_bvh.export()
+    ref_nodes = O.refit(2, nodes, prims, sils)
+    n = 20000
+    pts = W.uniform_points(n, 2, -3, 3, 32)
+    flip = np.zeros(n, np.uint32)
+    out = F.GPUInteractionList()
+    g.find_closest_silhouette_points(pts, np.full(n, R.FLT_MAX, np.float32), flip, out)
+    ref = O.silhouettes_bvh(2, ref_nodes, sils, R.make_spheres(pts, R.FLT_MAX), flip)
+    got = out.array()
+    fg, fr = got["index"] != R.UINT_MAX, ref["index"] != R.UINT_MAX
+    assert (fg != fr).sum() <= 2
+    both = fg & fr
+    assert np.all(np.abs(got["d"][both] - ref["d"][both]) <= 1e-3 * np.maximum(ref["d"][both], 1e-3))
+
+
+def test_empty_query_batches(sphere20k):
+    s, g = sphere20k
+    out = F.GPUInteractionList()
+    g.find_closest_points(np.zeros((0, 3), np.float32), np.zeros(0, np.float32), out)
+    assert len(out) == 0
+    g.intersect(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros(0, np.float32), out)
+    assert len(out) == 0
+
+
+def test_queries_before_transfer_raise():
+    g = F.GPUScene3D()
+    with pytest.raises(F.FcpwError):
+        g.find_closest_points(np.zeros((4, 3), np.float32), np.ones(4, np.float32), F.GPUInteractionList())
