@@ -144,7 +144,8 @@ SceneView GpuScene::view() const {
     return v;
 }
 
-cudaStream_t GpuScene::pick(void *s) const { return s ? (cudaStream_t)s : stream; }
+// device entry points run on the stream they are given; NULL is the CUDA default stream
+cudaStream_t GpuScene::pick(void *s) const { return (cudaStream_t)s; }
 
 }  // namespace fcpwgb
 
@@ -601,6 +602,31 @@ extern "C" int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *s, const 
     stats[1] = h[0];
     stats[2] = h[1];
     stats[3] = h[2];
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_export_nodes(fcpwgb_gpu_scene *s, void *nodes) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (!nodes) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL nodes");
+    size_t stride = s->snch ? 64 : 32;
+    std::vector<unsigned char> h((size_t)s->nNodes * stride);
+    FCPWGB_CUDA(cudaMemcpyAsync(h.data(), s->nodes.ptr, h.size(), cudaMemcpyDeviceToHost, s->stream));
+    FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+    for (uint32_t i = 0; i < s->nNodes; i++) {
+        const unsigned char *d = h.data() + (size_t)i * stride;
+        if (s->snch) {
+            fcpwgb_snch_node &o = ((fcpwgb_snch_node *)nodes)[i];
+            std::memcpy(&o.box, d, 24);
+            std::memcpy(&o.nPrimitives, d + 24, 4);
+            std::memcpy(&o.offset, d + 28, 4);
+            std::memcpy(&o.cone, d + 32, 20);
+            std::memcpy(&o.nSilhouettes, d + 52, 4);
+            std::memcpy(&o.silhouetteOffset, d + 56, 4);
+        } else {
+            std::memcpy((unsigned char *)nodes + (size_t)i * 32, d, 32);
+        }
+    }
     return FCPWGB_OK;
 }
 

@@ -183,6 +183,8 @@ class _GPUScene:
         self._h = handle
         self._cpu_bvh = None
         self._n_vertices = 0
+        self._n_nodes = 0
+        self._snch = False
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -211,6 +213,8 @@ class _GPUScene:
         check(lib().fcpwgb_gpu_scene_transfer_cpu_bvh(self._h, bvh.handle))
         self._cpu_bvh = bvh
         self._n_vertices = bvh.info.n_vertices
+        self._n_nodes = bvh.info.n_nodes
+        self._snch = bvh.snch
 
     def transfer_arrays(self, bvh_type: int, nodes, primitives, silhouettes=None, prim_vertices=None,
                         n_vertices: int = 0) -> None:
@@ -223,6 +227,8 @@ class _GPUScene:
                                               len(primitives), ptr(sils) if sils is not None and len(sils) else None,
                                               len(sils) if sils is not None else 0, ptr(pv), int(n_vertices)))
         self._n_vertices = int(n_vertices)
+        self._n_nodes = len(nodes)
+        self._snch = nodes.dtype == R.SNCH_NODE
 
     def refit(self, scene: _Scene, update_geometry: bool = True) -> None:
         """GPUScene::refit (include/fcpw/fcpw_gpu.h:27): with update_geometry the moved
@@ -234,6 +240,13 @@ class _GPUScene:
         bvh.update_positions(scene.positions(0))
         _, prims, sils = bvh.export()
         check(lib().fcpwgb_gpu_scene_refit(self._h, ptr(prims), ptr(sils) if sils is not None and len(sils) else None))
+
+    def refit_arrays(self, primitives=None, silhouettes=None) -> None:
+        """refit with already extracted records (interop layouts); None refits the
+        device geometry as it is (update_geometry=False)."""
+        p = np.ascontiguousarray(primitives) if primitives is not None else None
+        s = np.ascontiguousarray(silhouettes) if silhouettes is not None and len(silhouettes) else None
+        check(lib().fcpwgb_gpu_scene_refit(self._h, ptr(p), ptr(s)))
 
     def update_vertices_tensor(self, positions) -> None:
         """Moves the vertices to ``positions`` (a CUDA float32 tensor (V, DIM) in the
@@ -369,6 +382,12 @@ class _GPUScene:
         check(lib().fcpwgb_intersect_rays_device(self._h, rays.data_ptr(), raw.data_ptr(), n,
                                                  int(bool(check_for_occlusion)), self._stream(rays)))
         return _split_records(raw)
+
+    def export_nodes(self) -> np.ndarray:
+        """The device tree (after any refit) in the interop node layout."""
+        nodes = np.zeros(self._n_nodes, R.SNCH_NODE if self._snch else R.BVH_NODE)
+        check(lib().fcpwgb_gpu_scene_export_nodes(self._h, ptr(nodes)))
+        return nodes
 
     def check_errors(self) -> int:
         w = C.c_uint32(0)

@@ -178,7 +178,7 @@ int fcpwgb_gpu_scene_refit(fcpwgb_gpu_scene *scene, const void *primitives,
 /* Device-side geometry update + refit for differentiable pipelines: positions
  * is a device array of n_vertices*dim floats in caller vertex order. The
  * primitive (and silhouette) records are regathered on the device and the
- * tree refit; asynchronous on stream (a cudaStream_t, NULL = scene stream). */
+ * tree refit; asynchronous on stream (a cudaStream_t; NULL is the CUDA default stream). */
 int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *scene, const float *positions,
                                             uint32_t n_vertices, void *stream);
 
@@ -200,7 +200,8 @@ int fcpwgb_find_closest_silhouette_points(fcpwgb_gpu_scene *scene,
                                           fcpwgb_interaction *interactions, uint32_t n,
                                           float squared_min_radius, float precision);
 
-/* ----- queries with DEVICE arrays (asynchronous on stream; NULL = scene stream) ----- */
+/* ----- queries with DEVICE arrays: asynchronous on stream (a cudaStream_t, used as
+ * given; NULL is the CUDA default stream, as for any CUDA runtime call) ----- */
 int fcpwgb_find_closest_points_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                       fcpwgb_interaction *interactions, uint32_t n,
                                       int record_normals, void *stream);
@@ -224,6 +225,11 @@ int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *scene,
  * algorithmic bytes of a launch; results are written to interactions. */
 int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                           fcpwgb_interaction *interactions, uint32_t n, uint64_t *stats);
+
+/* Copies the scene's current (possibly refit) binary tree back to the host in
+ * the interop layout it was transferred in (fcpwgb_bvh_node or
+ * fcpwgb_snch_node records, n_nodes of them). Synchronous. */
+int fcpwgb_gpu_scene_export_nodes(fcpwgb_gpu_scene *scene, void *nodes);
 
 /* Reads and clears the device error word of the scene (stack overflow or
  * step budget exhausted in a traversal). Synchronises the scene stream. */

@@ -1,0 +1,110 @@
+"""ctypes wrapper of oracle/_ref/libfcpw_ref.so, the reference's own CPU Scene
+compiled from its sources (TEST INFRASTRUCTURE ONLY; available only where the
+reference checkout exists, i.e. never on the GPU machine)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .build import REF_LIB, build_reference
+
+_lib = None
+P = C.c_void_p
+
+
+def available() -> bool:
+    try:
+        return build_reference() is not None
+    except RuntimeError:
+        return False
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = build_reference()
+        if path is None:
+            raise RuntimeError("the reference checkout is not available on this machine")
+        _lib = C.CDLL(str(path))
+        i, f = C.c_int, C.c_float
+        _lib.ref_scene_create.restype = P
+        _lib.ref_scene_create.argtypes = [i, P, i, P, i, i, i]
+        _lib.ref_scene_destroy.argtypes = [P]
+        for name, args in {"ref_export": [P, P, P, P, P], "ref_closest_points": [P, P, i, i, P, P],
+                           "ref_intersect_rays": [P, P, i, i, P, P], "ref_silhouettes": [P, P, P, i, f, f, P],
+                           "ref_sphere_sample": [P, P, P, i, P, P], "ref_update_and_refit": [P, P, i]}.items():
+            fn = getattr(_lib, name)
+            fn.restype = i
+            fn.argtypes = args
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class RefScene:
+    """The reference Scene<DIM> with one object, built with vectorize=False."""
+
+    def __init__(self, dim, positions, indices, aggregate_type=3, silhouettes=False):
+        self.dim = dim
+        self.silhouettes = bool(silhouettes)
+        self.positions = np.ascontiguousarray(positions, np.float32)
+        self.indices = np.ascontiguousarray(indices, np.int32)
+        self._h = _load().ref_scene_create(dim, _p(self.positions), len(self.positions), _p(self.indices),
+                                           len(self.indices), int(aggregate_type), int(self.silhouettes))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _load().ref_scene_destroy(self._h)
+            self._h = None
+
+    def export(self):
+        from fcpw_gb300 import records as R
+        info = np.zeros(5, np.int32)
+        _load().ref_export(self._h, None, None, None, _p(info))
+        nodes = np.zeros(info[0], R.SNCH_NODE if self.silhouettes else R.BVH_NODE)
+        prims = np.zeros(info[3], R.TRIANGLE if self.dim == 3 else R.LINE_SEGMENT)
+        sils = np.zeros(info[4], R.EDGE if self.dim == 3 else R.VERTEX) if self.silhouettes else None
+        _load().ref_export(self._h, _p(nodes), _p(prims), _p(sils), _p(info))
+        return nodes, prims, sils, {"n_nodes": int(info[0]), "n_leaves": int(info[1]), "max_depth": int(info[2])}
+
+    @staticmethod
+    def _sph(spheres):
+        return np.ascontiguousarray(spheres).view(np.float32)
+
+    def closest_points(self, spheres, record_normals=False, visited=False):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        nv = np.zeros(len(spheres), np.int32) if visited else None
+        _load().ref_closest_points(self._h, _p(self._sph(spheres)), len(spheres), int(record_normals), _p(out), _p(nv))
+        return (out, nv) if visited else out
+
+    def intersect_rays(self, rays, occlusion=False):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(rays), R.INTERACTION)
+        hit = np.zeros(len(rays), np.int32)
+        r = np.ascontiguousarray(rays).view(np.float32)
+        _load().ref_intersect_rays(self._h, _p(r), len(rays), int(occlusion), _p(out), _p(hit))
+        return out, hit.astype(bool)
+
+    def silhouettes_query(self, spheres, flip, squared_min_radius=0.0, precision=1e-3):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        fl = np.ascontiguousarray(flip, np.uint32)
+        _load().ref_silhouettes(self._h, _p(self._sph(spheres)), _p(fl), len(spheres), float(squared_min_radius),
+                                float(precision), _p(out))
+        return out
+
+    def sphere_sample(self, spheres, rand_nums):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        hit = np.zeros(len(spheres), np.int32)
+        rn = np.ascontiguousarray(rand_nums, np.float32)
+        _load().ref_sphere_sample(self._h, _p(self._sph(spheres)), _p(rn), len(spheres), _p(out), _p(hit))
+        return out, hit.astype(bool)
+
+    def update_and_refit(self, positions):
+        pos = np.ascontiguousarray(positions, np.float32)
+        _load().ref_update_and_refit(self._h, _p(pos), len(pos))

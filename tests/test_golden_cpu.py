@@ -1,0 +1,97 @@
+"""Pins the host BVH producer and the oracle to the golden fixtures generated
+from the reference itself (tests/golden/make_golden.py)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import fcpw_gb300 as F
+from fcpw_gb300 import records as R
+from helpers import build_scene
+from oracle import oracle as O
+
+GOLDEN = sorted((Path(__file__).resolve().parent / "golden").glob("*.npz"))
+
+
+def load(p):
+    return dict(np.load(p, allow_pickle=False))
+
+
+@pytest.fixture(params=GOLDEN, ids=[p.stem for p in GOLDEN])
+def fx(request):
+    return load(request.param)
+
+
+def test_fixtures_present():
+    assert len(GOLDEN) >= 5
+
+
+def test_builder_reproduces_reference_tree(fx):
+    dim = int(fx["dim"])
+    s = build_scene(dim, fx["positions"], fx["indices"], bool(fx["silhouettes"]), F.AggregateType(int(fx["aggregate"])))
+    nodes, prims, sils = s.cpu_bvh.export()
+    assert nodes.tobytes() == fx["nodes"].tobytes(), "flattened nodes differ from the reference"
+    assert prims.tobytes() == fx["prims"].tobytes(), "leaf-ordered primitives differ from the reference"
+    if "sils" in fx:
+        assert sils.tobytes() == fx["sils"].tobytes(), "silhouette records differ from the reference"
+    assert s.cpu_bvh.info.n_leaves == int(fx["n_leaves"])
+    assert s.cpu_bvh.info.max_depth == int(fx["max_depth"])
+    # updateObjectVertices: re-extracted primitives equal the reference's after its refit
+    s.cpu_bvh.update_positions(fx["refit_positions"])
+    _, prims2, sils2 = s.cpu_bvh.export()
+    assert prims2.tobytes() == fx["refit_prims"].tobytes()
+    if "refit_sils" in fx:
+        assert sils2.tobytes() == fx["refit_sils"].tobytes()
+
+
+def _same(a, b, fields=("d", "index", "p", "uv")):
+    for f in fields:
+        assert np.array_equal(a[f], b[f]), f"field {f} differs"
+
+
+def test_oracle_closest_points_bit_exact(fx):
+    dim = int(fx["dim"])
+    sp = R.make_spheres(fx["cp_points"], R.FLT_MAX)
+    out, nv = O.closest_points_bvh(dim, fx["nodes"], fx["prims"], sp, visited=True)
+    _same(out, fx["cp_out"])
+    assert np.array_equal(nv.astype(np.int64), fx["cp_visited"].astype(np.int64)), "nodesVisited differs"
+    spr = R.make_spheres(fx["cpr_points"], fx["cpr_r2"])
+    _same(O.closest_points_bvh(dim, fx["nodes"], fx["prims"], spr, record_normals=True), fx["cpr_out"],
+          ("d", "index", "p", "uv", "n"))
+
+
+def test_oracle_rays_bit_exact(fx):
+    dim = int(fx["dim"])
+    rays = R.make_rays(fx["ray_o"], fx["ray_d"], R.FLT_MAX)
+    out, hit = O.intersect_rays_bvh(dim, fx["nodes"], fx["prims"], rays)
+    assert np.array_equal(hit, fx["ray_hit"])
+    _same(out, fx["ray_out"], ("d", "index", "p", "uv", "n"))
+    _, ohit = O.intersect_rays_bvh(dim, fx["nodes"], fx["prims"], rays, occlusion=True)
+    assert np.array_equal(ohit, fx["occ_hit"])
+
+
+def test_oracle_sphere_sampling_bit_exact(fx):
+    dim = int(fx["dim"])
+    out, hit = O.sphere_sample_bvh(dim, fx["nodes"], fx["prims"], R.make_spheres(fx["ss_c"], fx["ss_r2"]),
+                                   fx["ss_rand"])
+    assert np.array_equal(hit, fx["ss_hit"])
+    _same(out[hit], fx["ss_out"][hit], ("d", "index", "p", "uv", "n"))
+
+
+def test_oracle_silhouettes_bit_exact(fx):
+    if "sil_out" not in fx:
+        pytest.skip("fixture without silhouettes")
+    dim = int(fx["dim"])
+    out = O.silhouettes_bvh(dim, fx["nodes"], fx["sils"], R.make_spheres(fx["sil_points"], R.FLT_MAX),
+                            fx["sil_flip"])
+    # the CPU marks silhouette uv with -1 (silhouette_*.inl), the GPU records (t, 0); compare the rest
+    _same(out, fx["sil_out"], ("d", "index", "p"))
+
+
+def test_oracle_refit_boxes_bit_exact(fx):
+    dim = int(fx["dim"])
+    got = O.refit(dim, fx["nodes"], fx["refit_prims"], fx.get("refit_sils"))
+    ref = fx["refit_nodes"]
+    assert np.array_equal(got["pMin"], ref["pMin"]) and np.array_equal(got["pMax"], ref["pMax"])
+    sp = R.make_spheres(fx["cp_points"], R.FLT_MAX)
+    _same(O.closest_points_bvh(dim, got, fx["refit_prims"], sp), fx["refit_cp_out"])

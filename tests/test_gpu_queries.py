@@ -130,7 +130,7 @@ def test_rays_torus():
     nodes, prims, _ = s.cpu_bvh.export()
     ref, hit = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax))
     _ray_compare(got, ref, hit)
-    assert 0.2 < hit.mean() < 0.9
+    assert 0.05 < hit.mean() < 0.9
     # occlusion variant
     out2 = F.GPUInteractionList()
     g.intersect(o, d, tmax, out2, True)
