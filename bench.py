@@ -175,6 +175,7 @@ def run_ours(args):
     import fcpw_gb300 as F
     from fcpw_gb300 import records as R
     from fcpw_gb300._lib import check, lib
+    from fcpw_gb300.autotune import autotune_closest_points
 
     rank, world, local = dist_env()
     if world > 1:
@@ -202,36 +203,63 @@ def run_ours(args):
     def step():
         check(L.fcpwgb_find_closest_points_device(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, 0, sptr))
 
-    # traversal statistics -> algorithmic bytes of one launch (untimed)
-    stats = (C.c_uint64 * 4)()
-    check(L.fcpwgb_closest_points_traversal_stats(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, stats))
-    n_q, n_pop, n_inner, n_prim = [int(x) for x in stats]
-    s_node, s_prim, s_in, s_out, w = 32, 40, 16, 40, 2
-    alg_bytes = n_q * (s_in + s_out) + s_node * (n_q + w * n_inner) + s_prim * n_prim
+    def traversal_stats(node_bytes, prim_bytes, in_bytes):
+        stats = (C.c_uint64 * 4)()
+        check(L.fcpwgb_closest_points_traversal_stats(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, stats))
+        n_q, n_pop, n_inner, n_prim = [int(x) for x in stats]
+        if node_bytes == 32:  # binary: every expansion loads two 32 B child records, plus the root
+            nb = 32 * (n_q + 2 * n_inner)
+        else:  # wide: every expansion loads one node record holding all child boxes
+            nb = node_bytes * n_inner
+        return {"bytes": n_q * (in_bytes + 40) + nb + prim_bytes * n_prim,
+                "per_query": {"nodes_popped": n_pop / n_q if node_bytes == 32 else n_inner / n_q,
+                              "inner_expanded": n_inner / n_q, "prim_tests": n_prim / n_q}}
 
-    for _ in range(args.warmup):
-        flush.zero_()
-        step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    def timed(steps, warmup):
+        for _ in range(warmup):
+            flush.zero_()
+            step()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        check(L.fcpwgb_gpu_scene_enable_kernel_timing(gpu.handle, 1))
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for i in range(steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+        ktot, kn = C.c_double(0), C.c_uint32(0)
+        check(L.fcpwgb_gpu_scene_kernel_time(gpu.handle, C.byref(ktot), C.byref(kn)))
+        check(L.fcpwgb_gpu_scene_enable_kernel_timing(gpu.handle, 0))
+        if world > 1:
+            dist.barrier()
+        ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / steps
+        return ms, ktot.value / max(kn.value, 1)
 
+    # 1) plain: the binary tree in the reference GPU traversal order
+    gpu.set_traversal(0)
+    plain_ms, plain_kms = timed(max(3, args.steps // 4), 2)
+    plain_stats = traversal_stats(32, 40, 16)
+
+    # 2) fast path: wide tree with quantised child boxes, queries sorted, persistent blocks, FP64 final distance
+    sample = spheres[: min(n, 1 << 20)]
+    if args.variant == "auto":
+        best, table = autotune_closest_points(gpu, sample)
+    else:  # fixed "branching,bits,persistent", e.g. for profiling one kernel
+        b, q, p = (int(x) for x in args.variant.split(","))
+        best = {"branching": b, "bits": q, "persistent": bool(p), "sort_queries": True, "precise": True}
+        gpu.set_traversal(**best)
+        table = []
+    from fcpw_gb300.wide_format import layout
+    node_bytes = layout(best["branching"], best["bits"])["size"]
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    torch.cuda.synchronize()
-    for i in range(args.steps):
-        flush.zero_()
-        starts[i].record(stream)
-        step()
-        ends[i].record(stream)
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = sum(step_ms) / len(step_ms)
+    ms, kms = timed(args.steps, args.warmup)
+    fast_stats = traversal_stats(node_bytes, 48, 20)  # sorted sphere + permutation index per query
     ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
     if world > 1:
         dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
@@ -256,37 +284,43 @@ def run_ours(args):
         dist.all_reduce(e2e_t_t, op=dist.ReduceOp.MAX)
     e2e_value = world * n / float(e2e_t_t.item())
 
-    # accuracy against the FP64 brute force on a sample (rank 0)
-    accuracy = None
     result = None
     if rank == 0:
         from oracle import oracle as O
-        res = out.cpu().numpy().view(R.INTERACTION).reshape(-1)
+        res = h_out.numpy().view(R.INTERACTION).reshape(-1)
         _, prims, _ = scene.cpu_bvh.export()
         k = 256
         d64, _ = O.closest_points_brute_f64(3, prims, R.make_spheres(pts[:k], R.FLT_MAX))
         rel = np.abs(res["d"][:k].astype(np.float64) - d64) / d64
-        accuracy = {"samples": k, "max_rel_err_vs_fp64": float(rel.max()), "mean_rel_err_vs_fp64": float(rel.mean())}
+        accuracy = {"samples": k, "max_rel_err_vs_fp64": float(rel.max()), "mean_rel_err_vs_fp64": float(rel.mean()),
+                    "variant": "fast path (precise)"}
 
         peak, peak_kind = peaks()
-        achieved = alg_bytes / (ms / 1e3) / 1e9
-        traffic = profiled_traffic("binary")
+        achieved = fast_stats["bytes"] / (kms / 1e3) / 1e9
+        variant = f"wide{best['branching']}_q{best['bits']}" + ("_persistent" if best["persistent"] else "")
+        traffic = profiled_traffic(variant)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded torus + uniform queries)",
             "config": {"workload": "closest point, seeded torus 1,048,576 triangles, 4,194,304 queries "
-                                   "uniform in [-2,2]^3 per GPU, r2 = FLT_MAX, binary SAH BVH",
-                       "variant": "binary (reference traversal order)", "queries_per_gpu": n,
-                       "triangles": int(len(f)), "l2": "flushed (256 MiB write) before every timed step",
-                       "bvh_build_s": round(build_s, 3), "transfer_s": round(transfer_s, 3)},
+                                   "uniform in [-2,2]^3 per GPU, r2 = FLT_MAX, SAH BVH",
+                       "variant": variant, "traversal": best, "queries_per_gpu": n, "triangles": int(len(f)),
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "bvh_build_s": round(build_s, 3), "transfer_s": round(transfer_s, 3),
+                       "plain": {"variant": "binary tree, reference traversal order (bvh.slang:395-502)",
+                                 "queries_per_s": world * n / (plain_ms / 1e3), "ms_per_step": plain_ms,
+                                 "kernel_ms": plain_kms, "per_query": plain_stats["per_query"],
+                                 "achieved_gbs": plain_stats["bytes"] / (plain_kms / 1e3) / 1e9},
+                       "speedup_vs_plain": plain_ms / ms,
+                       "autotune_ms": [[c["branching"], c["bits"], int(c["persistent"]), round(t, 4)]
+                                       for c, t in table]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 40},
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * 4,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"hbm_gbs ({peak_kind})",
-                         "algorithmic_bytes_per_launch": alg_bytes,
-                         "per_query": {"nodes_popped": n_pop / n_q, "inner_expanded": n_inner / n_q,
-                                       "prim_tests": n_prim / n_q}},
+                         "kernel": "kWideClosestPoint", "kernel_ms": kms,
+                         "algorithmic_bytes_per_launch": fast_stats["bytes"], "per_query": fast_stats["per_query"]},
             "clocks": clocks, "accuracy": accuracy,
         }
         if world == 1 and not args.no_cpu_baseline:

@@ -26,6 +26,7 @@ SIGNATURES = {
     "fcpwgb_cpu_bvh_export": (c_int, [P, P, P, P]),
     "fcpwgb_cpu_bvh_export_topology": (c_int, [P, P, P, P, P]),
     "fcpwgb_cpu_bvh_update_positions": (c_int, [P, P]),
+    "fcpwgb_cpu_bvh_export_wide": (c_int, [P, c_int, c_int, P, P, C.POINTER(c_uint32), C.POINTER(c_uint32)]),
     "fcpwgb_gpu_scene_create": (c_int, [c_int, c_int, C.POINTER(c_void_p)]),
     "fcpwgb_gpu_scene_destroy": (None, [P]),
     "fcpwgb_gpu_scene_transfer": (c_int, [P, c_int, P, c_uint32, P, c_uint32, P, c_uint32, P, c_uint32]),
@@ -42,6 +43,10 @@ SIGNATURES = {
     "fcpwgb_find_closest_silhouette_points_device": (c_int, [P, P, P, P, c_uint32, c_float, c_float, P]),
     "fcpwgb_closest_points_traversal_stats": (c_int, [P, P, P, c_uint32, P]),
     "fcpwgb_gpu_scene_export_nodes": (c_int, [P, P]),
+    "fcpwgb_gpu_scene_enable_kernel_timing": (c_int, [P, c_int]),
+    "fcpwgb_gpu_scene_kernel_time": (c_int, [P, C.POINTER(C.c_double), C.POINTER(c_uint32)]),
+    "fcpwgb_gpu_scene_set_traversal": (c_int, [P, P]),
+    "fcpwgb_gpu_scene_get_traversal": (c_int, [P, P]),
     "fcpwgb_gpu_scene_check_errors": (c_int, [P, C.POINTER(c_uint32)]),
 }
 
@@ -50,6 +55,11 @@ class BvhInfo(C.Structure):
     _fields_ = [("dim", c_int), ("bvh_type", c_int), ("n_nodes", c_uint32), ("n_leaves", c_uint32),
                 ("max_depth", c_uint32), ("n_primitives", c_uint32), ("n_silhouettes", c_uint32),
                 ("n_vertices", c_uint32)]
+
+
+class TraversalConfig(C.Structure):
+    _fields_ = [("branching", c_int), ("bits", c_int), ("block_size", c_int), ("sort_queries", c_int),
+                ("persistent", c_int), ("precise", c_int)]
 
 
 class FcpwError(RuntimeError):

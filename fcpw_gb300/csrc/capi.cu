@@ -114,6 +114,39 @@ extern "C" int fcpwgb_cpu_bvh_export_topology(const fcpwgb_cpu_bvh *b, int32_t *
     return FCPWGB_OK;
 }
 
+extern "C" int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *b, int branching, int bits, void *nodes,
+                                          int32_t *child_binary, uint32_t *n_nodes, uint32_t *node_bytes) {
+    if (!b || !n_nodes || !node_bytes) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    const HostBvh &h = *b->bvh;
+    uint32_t n = h.nNodes();
+    bool snch = h.hasSilhouettes();
+    std::vector<unsigned char> raw((size_t)n * (snch ? sizeof(fcpwgb_snch_node) : sizeof(fcpwgb_bvh_node)));
+    h.exportNodes(raw.data());
+    std::vector<uint32_t> nP(n), off(n);
+    std::vector<float> boxes((size_t)n * 6);
+    for (uint32_t i = 0; i < n; i++) {
+        const fcpwgb_bounding_box *bx;
+        if (snch) {
+            const fcpwgb_snch_node &nd = ((const fcpwgb_snch_node *)raw.data())[i];
+            bx = &nd.box; nP[i] = nd.nPrimitives; off[i] = nd.offset;
+        } else {
+            const fcpwgb_bvh_node &nd = ((const fcpwgb_bvh_node *)raw.data())[i];
+            bx = &nd.box; nP[i] = nd.nPrimitives; off[i] = nd.offset;
+        }
+        std::memcpy(&boxes[(size_t)i * 6], bx, 24);
+    }
+    WideHost w;
+    if (!(branching == 2 || branching == 4 || branching == 8) || !(bits == 8 || bits == 16 || bits == 32))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "branching must be 2/4/8 and bits 8/16/32");
+    if (!buildWideTree(branching, bits, nP, off, boxes, w))
+        return setError(FCPWGB_ERR_UNSUPPORTED, "this tree cannot be collapsed into the requested wide layout");
+    *n_nodes = w.nNodes;
+    *node_bytes = (uint32_t)wideNodeBytes(branching, bits);
+    if (nodes) std::memcpy(nodes, w.nodes.data(), w.nodes.size());
+    if (child_binary) std::memcpy(child_binary, w.childBinary.data(), w.childBinary.size() * sizeof(int32_t));
+    return FCPWGB_OK;
+}
+
 extern "C" int fcpwgb_cpu_bvh_update_positions(fcpwgb_cpu_bvh *b, const float *positions) {
     if (!b || !positions) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
     b->bvh->updatePositions(positions);
@@ -338,6 +371,12 @@ extern "C" int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *s, int bvh_type, cons
     s->nSils = snch ? n_silhouettes : 0;
     s->nLeaves = (uint32_t)leaves.size();
     s->maxDepth = maxDepth;
+    s->hostNP = nP;
+    s->hostOff = off;
+    s->hostBoxes.resize((size_t)n_nodes * 6);
+    for (uint32_t i = 0; i < n_nodes; i++)
+        std::memcpy(&s->hostBoxes[(size_t)i * 6], hNodes.data() + (size_t)i * (snch ? 64 : 32), 24);
+    std::memcpy(s->rootBox, s->hostBoxes.data(), 24);
     s->transferred = true;
     s->treeVersion++;
     return FCPWGB_OK;
@@ -602,6 +641,59 @@ extern "C" int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *s, const 
     stats[1] = h[0];
     stats[2] = h[1];
     stats[3] = h[2];
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *s, const fcpwgb_traversal_config *c) {
+    if (!s || !c) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!(c->branching == 0 || c->branching == 2 || c->branching == 4 || c->branching == 8))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "branching must be 0, 2, 4 or 8");
+    if (!(c->bits == 8 || c->bits == 16 || c->bits == 32))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "bits must be 8, 16 or 32");
+    if (c->block_size != 128) return setError(FCPWGB_ERR_UNSUPPORTED, "the wide kernels run 128-thread blocks");
+    WideConfig w;
+    w.branching = c->branching;
+    w.bits = c->bits;
+    w.blockSize = c->block_size;
+    w.sortQueries = c->sort_queries != 0;
+    w.persistent = c->persistent != 0;
+    w.precise = c->precise != 0;
+    s->wideConfig = w;
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *s, fcpwgb_traversal_config *c) {
+    if (!s || !c) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    c->branching = s->wideConfig.branching;
+    c->bits = s->wideConfig.bits;
+    c->block_size = s->wideConfig.blockSize;
+    c->sort_queries = s->wideConfig.sortQueries;
+    c->persistent = s->wideConfig.persistent;
+    c->precise = s->wideConfig.precise;
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_enable_kernel_timing(fcpwgb_gpu_scene *s, int enable) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    s->timing = enable != 0;
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_kernel_time(fcpwgb_gpu_scene *s, double *total_ms, uint32_t *launches) {
+    if (!s || !total_ms || !launches) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
+    int rc = s->activate();
+    if (rc) return rc;
+    double sum = 0.0;
+    for (auto &p : s->timedEvents) {
+        FCPWGB_CUDA(cudaEventSynchronize(p.second));
+        float ms = 0.0f;
+        FCPWGB_CUDA(cudaEventElapsedTime(&ms, p.first, p.second));
+        sum += ms;
+    }
+    *total_ms = sum;
+    *launches = (uint32_t)s->timedEvents.size();
+    s->freeEvents.insert(s->freeEvents.end(), s->timedEvents.begin(), s->timedEvents.end());
+    s->timedEvents.clear();
     return FCPWGB_OK;
 }
 

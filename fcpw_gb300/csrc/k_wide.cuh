@@ -1,0 +1,326 @@
+// Closest-point traversal of the wide / quantised trees (wide.h), plus the
+// device re-quantisation after a refit. Templates only; instantiated per
+// branching factor in k_wide_w{2,4,8}.cu.
+#pragma once
+
+#include "kernels.h"
+#include "wide_common.cuh"
+
+namespace fcpwgb {
+
+// 48 B triangle record of the wide kernels: (pa, index), (pb, 0), (pc, 0)
+struct Tri48Prim {
+    float3 pa, pb, pc;
+    uint32_t index;
+    FCPWGB_D static Tri48Prim load(const unsigned char *prims, uint32_t k) {
+        const unsigned char *p = prims + (size_t)k * 48;
+        float4 a = ldg4(p), b = ldg4(p + 16), c = ldg4(p + 32);
+        Tri48Prim t;
+        t.pa = make_float3(a.x, a.y, a.z);
+        t.pb = make_float3(b.x, b.y, b.z);
+        t.pc = make_float3(c.x, c.y, c.z);
+        t.index = __float_as_uint(a.w);
+        return t;
+    }
+    FCPWGB_D float closestPoint(float3 x, float3 &p, float2 &uv) const {
+        return closestPointTriangle(pa, pb, pc, x, p, uv);
+    }
+    FCPWGB_D float3 normal() const { return normalize3(cross3(pb - pa, pc - pa)); }
+    // FP64 distance and closest point, vertices taken relative to the query
+    FCPWGB_D double refine(float3 x, float3 &pOut) const {
+        double ax = (double)pa.x - x.x, ay = (double)pa.y - x.y, az = (double)pa.z - x.z;
+        double bx = (double)pb.x - x.x, by = (double)pb.y - x.y, bz = (double)pb.z - x.z;
+        double cx = (double)pc.x - x.x, cy = (double)pc.y - x.y, cz = (double)pc.z - x.z;
+        double abx = bx - ax, aby = by - ay, abz = bz - az, acx = cx - ax, acy = cy - ay, acz = cz - az;
+        double px, py, pz;
+        double d1 = -(abx * ax + aby * ay + abz * az), d2 = -(acx * ax + acy * ay + acz * az);
+        double d3 = -(abx * bx + aby * by + abz * bz), d4 = -(acx * bx + acy * by + acz * bz);
+        double d5 = -(abx * cx + aby * cy + abz * cz), d6 = -(acx * cx + acy * cy + acz * cz);
+        double vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+        if (d1 <= 0 && d2 <= 0) { px = ax; py = ay; pz = az; }
+        else if (d3 >= 0 && d4 <= d3) { px = bx; py = by; pz = bz; }
+        else if (d6 >= 0 && d5 <= d6) { px = cx; py = cy; pz = cz; }
+        else if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+            double v = d1 / (d1 - d3);
+            px = ax + abx * v; py = ay + aby * v; pz = az + abz * v;
+        } else if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+            double w = d2 / (d2 - d6);
+            px = ax + acx * w; py = ay + acy * w; pz = az + acz * w;
+        } else if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
+            double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+            px = bx + (cx - bx) * w; py = by + (cy - by) * w; pz = bz + (cz - bz) * w;
+        } else {
+            // face region: project the query (the origin) onto the plane
+            double nx = aby * acz - abz * acy, ny = abz * acx - abx * acz, nz = abx * acy - aby * acx;
+            double nn = nx * nx + ny * ny + nz * nz;
+            double t = (ax * nx + ay * ny + az * nz) / nn;
+            px = nx * t; py = ny * t; pz = nz * t;
+        }
+        pOut = make_float3((float)(x.x + px), (float)(x.y + py), (float)(x.z + pz));
+        return sqrt(px * px + py * py + pz * pz);
+    }
+};
+
+// 2D segments keep the 24 B record (SegPrim) and gain an FP64 refinement
+struct Seg24Prim : SegPrim {
+    FCPWGB_D static Seg24Prim load(const unsigned char *prims, uint32_t k) {
+        Seg24Prim s;
+        SegPrim b = SegPrim::load(prims, k);
+        s.pa = b.pa; s.pb = b.pb; s.index = b.index;
+        return s;
+    }
+    FCPWGB_D double refine(float3 x, float3 &pOut) const {
+        double ax = (double)pa.x - x.x, ay = (double)pa.y - x.y;
+        double ux = (double)pb.x - pa.x, uy = (double)pb.y - pa.y;
+        double c1 = -(ux * ax + uy * ay), c2 = ux * ux + uy * uy, px, py;
+        if (c1 <= 0) { px = ax; py = ay; }
+        else if (c2 <= c1) { px = ax + ux; py = ay + uy; }
+        else { double t = c1 / c2; px = ax + ux * t; py = ay + uy * t; }
+        pOut = make_float3((float)(x.x + px), (float)(x.y + py), 0.0f);
+        return sqrt(px * px + py * py);
+    }
+};
+
+template<int W, int BITS> struct WideNodeRegs {
+    using L = WideLayout<W, BITS>;
+    static constexpr int kWords = L::kSize / 4;
+    uint32_t w[kWords];
+
+    FCPWGB_D void load(const unsigned char *nodes, uint32_t idx) {
+        const uint4 *p = reinterpret_cast<const uint4 *>(nodes + (size_t)idx * L::kSize);
+#pragma unroll
+        for (int i = 0; i < kWords / 4; i++) {
+            uint4 v = __ldg(p + i);
+            w[4 * i] = v.x; w[4 * i + 1] = v.y; w[4 * i + 2] = v.z; w[4 * i + 3] = v.w;
+        }
+    }
+    FCPWGB_D uint32_t byteAt(int off) const { return (w[off >> 2] >> (8 * (off & 3))) & 0xffu; }
+    FCPWGB_D uint32_t halfAt(int off) const { return (w[off >> 2] >> (8 * (off & 3))) & 0xffffu; }
+    FCPWGB_D uint32_t ref(int c) const { return w[(L::kRefs >> 2) + c]; }
+    FCPWGB_D uint32_t cnt(int c) const { return byteAt(L::kCnt + c); }
+    FCPWGB_D float origin(int a) const { return __uint_as_float(w[a]); }
+    FCPWGB_D float scale(int a) const { return exp2i((int)byteAt(12 + a) - 127); }
+    // bound k = 0..2 lo(x,y,z), 3..5 hi(x,y,z) of child c
+    FCPWGB_D float bound(int k, int c) const {
+        if (BITS == 32) return __uint_as_float(w[(L::kBounds >> 2) + k * W + c]);
+        int a = k % 3;
+        uint32_t q = BITS == 16 ? halfAt(L::kBounds + 2 * (k * W + c)) : byteAt(L::kBounds + k * W + c);
+        return __fmaf_rn((float)q, scale(a), origin(a));
+    }
+};
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+FCPWGB_D uint32_t packLeaf(uint32_t off, uint32_t cnt) { return kLeafBit | (cnt << 27) | off; }
+
+// Closest point of one query on a wide tree (bvh.slang:395-502 semantics:
+// inclusive d2Min <= r2 pruning, r2 shrunk by child d2Max, primitives accepted
+// when d*d <= r2, the later of equal distances wins).
+template<int W, int BITS, class Prim>
+FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigned char *__restrict__ prims,
+                          float3 c, float r2, DevInteraction &best, uint32_t &selected, uint32_t *errorWord,
+                          uint32_t &nExpanded, uint32_t &nTests) {
+    uint32_t stRef[kWideStack];
+    float stD[kWideStack];
+    int sp = 0;
+    uint32_t cur = 0;  // wide node 0 (always an inner record)
+    bool found = false;
+    WideNodeRegs<W, BITS> node;
+    for (;;) {
+        if (!(cur & kLeafBit)) {
+            node.load(nodes, cur);
+            nExpanded++;
+            float dmin[W];
+            uint32_t key[W];
+#pragma unroll
+            for (int k = 0; k < W; k++) {
+                uint32_t n = node.cnt(k);
+                float lo0 = node.bound(0, k), lo1 = node.bound(1, k), lo2 = node.bound(2, k);
+                float hi0 = node.bound(3, k), hi1 = node.bound(4, k), hi2 = node.bound(5, k);
+                float d2Min, d2Max;
+                boxSphereDist(make_float3(lo0, lo1, lo2), make_float3(hi0, hi1, hi2), c, d2Min, d2Max);
+                if (n == kWideEmpty) { d2Min = kFltMax; d2Max = kFltMax; }
+                r2 = fminf(r2, d2Max);
+                dmin[k] = n == kWideEmpty ? INFINITY : d2Min;
+                key[k] = n == 0 ? node.ref(k) : packLeaf(node.ref(k), n);
+            }
+            // ascending by distance (insertion sort, unrolled)
+#pragma unroll
+            for (int i = 1; i < W; i++) {
+#pragma unroll
+                for (int j = i; j > 0; j--) {
+                    bool sw = dmin[j] < dmin[j - 1];
+                    float td = sw ? dmin[j] : dmin[j - 1];
+                    dmin[j] = sw ? dmin[j - 1] : dmin[j];
+                    dmin[j - 1] = td;
+                    uint32_t tk = sw ? key[j] : key[j - 1];
+                    key[j] = sw ? key[j - 1] : key[j];
+                    key[j - 1] = tk;
+                }
+            }
+            int nh = 0;
+#pragma unroll
+            for (int k = 0; k < W; k++) nh += dmin[k] <= r2 ? 1 : 0;
+            if (nh > 0) {
+                if (sp + nh - 1 > kWideStack) {
+                    atomicOr(errorWord, kErrStackOverflow);
+                    return found;
+                }
+#pragma unroll
+                for (int k = W - 1; k >= 1; k--) {
+                    if (k < nh) {
+                        stRef[sp] = key[k];
+                        stD[sp] = dmin[k];
+                        sp++;
+                    }
+                }
+                cur = key[0];
+                continue;
+            }
+        } else {
+            uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+            nTests += cnt;
+            for (uint32_t p = 0; p < cnt; p++) {
+                Prim prim = Prim::load(prims, off + p);
+                float3 pt;
+                float2 uv;
+                float d = prim.closestPoint(c, pt, uv);
+                if (d * d <= r2) {
+                    r2 = fminf(r2, d * d);
+                    best.p = pt;
+                    best.n = make_float3(0.f, 0.f, 0.f);
+                    best.uv = uv;
+                    best.d = d;
+                    best.index = prim.index;
+                    selected = off + p;
+                    found = true;
+                }
+            }
+        }
+        bool next = false;
+        while (sp > 0) {
+            sp--;
+            if (stD[sp] <= r2) {
+                cur = stRef[sp];
+                next = true;
+                break;
+            }
+        }
+        if (!next) break;
+    }
+    return found;
+}
+
+// One thread per query; with `counter` non-NULL blocks are persistent and
+// warps fetch 32-query chunks from it; with `perm` non-NULL the queries are
+// read in sorted order and results scattered back to out[perm[i]]; with
+// `stats` non-NULL expansions and primitive tests are summed into stats[1..2].
+template<int W, int BITS, class Prim, bool PRECISE>
+__global__ void __launch_bounds__(128) kWideClosestPoint(const unsigned char *__restrict__ nodes,
+                                                         const unsigned char *__restrict__ prims,
+                                                         const DevSphere *__restrict__ spheres,
+                                                         const uint32_t *__restrict__ perm,
+                                                         DevInteraction *__restrict__ out, uint32_t n,
+                                                         int recordNormal, uint32_t *counter, uint32_t *errorWord,
+                                                         unsigned long long *stats) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+    uint32_t tExp = 0, tTests = 0;
+    for (;;) {
+        if (counter) {
+            uint32_t b = 0;
+            if (lane == 0) b = atomicAdd(counter, 32u);
+            base = __shfl_sync(0xffffffffu, b, 0);
+        }
+        if (base >= n) break;
+        uint32_t i = base + lane;
+        if (i < n) {
+            float4 s4 = ldg4(spheres + i);
+            float3 c = make_float3(s4.x, s4.y, s4.z);
+            DevInteraction best = defaultInteraction();
+            uint32_t selected = kUintMax;
+            bool found = wideClosest<W, BITS, Prim>(nodes, prims, c, s4.w, best, selected, errorWord, tExp, tTests);
+            if (found) {
+                Prim prim = Prim::load(prims, selected);
+                if (PRECISE) {
+                    float3 p;
+                    double d = prim.refine(c, p);
+                    best.d = (float)d;
+                    best.p = p;
+                }
+                if (recordNormal) best.n = prim.normal();
+            }
+            out[perm ? __ldg(perm + i) : i] = best;
+        }
+        if (!counter) break;
+        __syncwarp();
+    }
+    if (stats) {
+        atomicAdd(stats + 1, (unsigned long long)tExp);
+        atomicAdd(stats + 2, (unsigned long long)tTests);
+    }
+}
+
+// Re-quantises every wide node from the (refit) binary boxes behind its slots.
+template<int W, int BITS>
+__global__ void kRequantize(unsigned char *wideNodes, const int32_t *childBinary, const unsigned char *binNodes,
+                            int binStride, uint32_t nWide, uint32_t *errorWord) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nWide) return;
+    float lo[W * 3], hi[W * 3];
+    bool valid[W];
+    for (int c = 0; c < W; c++) {
+        int32_t b = childBinary[(size_t)i * W + c];
+        valid[c] = b >= 0;
+        for (int a = 0; a < 3; a++) { lo[c * 3 + a] = 0.0f; hi[c * 3 + a] = 0.0f; }
+        if (b >= 0) {
+            const float *f = reinterpret_cast<const float *>(binNodes + (size_t)b * binStride);
+            for (int a = 0; a < 3; a++) { lo[c * 3 + a] = f[a]; hi[c * 3 + a] = f[3 + a]; }
+        }
+    }
+    unsigned char rec[WideLayout<W, BITS>::kSize];
+    unsigned char *dst = wideNodes + (size_t)i * WideLayout<W, BITS>::kSize;
+    for (int k = 0; k < WideLayout<W, BITS>::kSize; k++) rec[k] = dst[k];
+    if (!quantizeWideNode<W, BITS>(lo, hi, valid, rec)) {
+        atomicOr(errorWord, kErrBadIndex);
+        return;
+    }
+    for (int k = 0; k < WideLayout<W, BITS>::kSize; k++) dst[k] = rec[k];
+}
+
+template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
+template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes, const int32_t *childBinary,
+                                              const unsigned char *binNodes, int binStride, uint32_t nWide,
+                                              uint32_t *errorWord, cudaStream_t s);
+
+#define FCPWGB_WIDE_INSTANTIATE(W)                                                                                \
+    template<> cudaError_t launchWideClosestT<W>(int bits, int dim, bool precise, const WideLaunch &l,             \
+                                                 cudaStream_t s) {                                                 \
+        dim3 g(l.grid), b(128);                                                                                    \
+        _Pragma("nv_diag_suppress 177")                                                                            \
+        auto go = [&](auto kern) {                                                                                 \
+            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.out, l.n, l.recordNormal, l.counter,       \
+                                 l.errorWord, l.stats);                                                            \
+        };                                                                                                         \
+        if (dim == 3) {                                                                                            \
+            if (bits == 8) { if (precise) go(kWideClosestPoint<W, 8, Tri48Prim, true>); else go(kWideClosestPoint<W, 8, Tri48Prim, false>); } \
+            else if (bits == 16) { if (precise) go(kWideClosestPoint<W, 16, Tri48Prim, true>); else go(kWideClosestPoint<W, 16, Tri48Prim, false>); } \
+            else { if (precise) go(kWideClosestPoint<W, 32, Tri48Prim, true>); else go(kWideClosestPoint<W, 32, Tri48Prim, false>); } \
+        } else {                                                                                                   \
+            if (bits == 8) { if (precise) go(kWideClosestPoint<W, 8, Seg24Prim, true>); else go(kWideClosestPoint<W, 8, Seg24Prim, false>); } \
+            else if (bits == 16) { if (precise) go(kWideClosestPoint<W, 16, Seg24Prim, true>); else go(kWideClosestPoint<W, 16, Seg24Prim, false>); } \
+            else { if (precise) go(kWideClosestPoint<W, 32, Seg24Prim, true>); else go(kWideClosestPoint<W, 32, Seg24Prim, false>); } \
+        }                                                                                                          \
+        return cudaGetLastError();                                                                                 \
+    }                                                                                                              \
+    template<> cudaError_t launchRequantizeT<W>(int bits, unsigned char *wideNodes, const int32_t *childBinary,    \
+                                                const unsigned char *binNodes, int binStride, uint32_t nWide,      \
+                                                uint32_t *errorWord, cudaStream_t s) {                             \
+        if (nWide == 0) return cudaSuccess;                                                                        \
+        dim3 g((nWide + 127) / 128), b(128);                                                                       \
+        if (bits == 8) kRequantize<W, 8><<<g, b, 0, s>>>(wideNodes, childBinary, binNodes, binStride, nWide, errorWord); \
+        else if (bits == 16) kRequantize<W, 16><<<g, b, 0, s>>>(wideNodes, childBinary, binNodes, binStride, nWide, errorWord); \
+        else kRequantize<W, 32><<<g, b, 0, s>>>(wideNodes, childBinary, binNodes, binStride, nWide, errorWord); \
+        return cudaGetLastError();                                                                                 \
+    }
+
+}  // namespace fcpwgb

@@ -1,0 +1,6 @@
+// Instantiation of the wide-tree kernels for branching factor 4 (see k_wide.cuh).
+#include "k_wide.cuh"
+
+namespace fcpwgb {
+FCPWGB_WIDE_INSTANTIATE(4)
+}  // namespace fcpwgb

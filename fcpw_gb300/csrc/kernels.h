@@ -34,6 +34,32 @@ cudaError_t launchSilhouetteBinary(const SceneView &v, const DevSphere *spheres,
                                    cudaStream_t s);
 cudaError_t launchFillDefault(DevInteraction *out, uint32_t n, cudaStream_t s);
 
+// wide / quantised closest point (k_wide.cuh, k_wide_w{2,4,8}.cu)
+struct WideLaunch {
+    const unsigned char *nodes = nullptr;  // wide node records
+    const unsigned char *prims = nullptr;  // 48 B triangles (3D) or 24 B segments (2D)
+    const DevSphere *spheres = nullptr;    // queries (sorted when perm is set)
+    const uint32_t *perm = nullptr;        // sorted position -> caller query index, or NULL
+    DevInteraction *out = nullptr;
+    uint32_t n = 0;
+    int recordNormal = 0;
+    uint32_t *counter = nullptr;           // work counter (zero on entry) for persistent blocks, or NULL
+    uint32_t *errorWord = nullptr;
+    unsigned long long *stats = nullptr;   // traversal statistics, or NULL
+    uint32_t grid = 0;
+};
+template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
+template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes, const int32_t *childBinary,
+                                              const unsigned char *binNodes, int binStride, uint32_t nWide,
+                                              uint32_t *errorWord, cudaStream_t s);
+
+// query reordering and record packing (k_sort.cu)
+constexpr uint32_t kSortCellBits = 18;  // 2^18 cells: 64^3 in 3D, 512^2 in 2D
+struct SortGrid { float3 lo; float3 invCell; int dim; };
+cudaError_t launchSortQueries(const SortGrid &g, const DevSphere *spheres, uint32_t n, uint32_t *cells,
+                              DevSphere *sorted, uint32_t *perm, cudaStream_t s);
+cudaError_t launchPackTri48(const DevTriangle *tris, uint32_t n, float4 *out, cudaStream_t s);
+
 // refit (k_refit.cu)
 struct RefitView {
     int dim = 3;

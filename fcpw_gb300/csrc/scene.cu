@@ -1,17 +1,151 @@
-// Query dispatch of a GPU scene: picks the traversal variant and runs the
-// host-array path.
+// Query dispatch of a GPU scene: the binary reference-order kernels or the
+// wide/quantised fast path, the host-array path, and keeping the derived wide
+// tree in step with refits.
+#include <algorithm>
+
 #include "scene.h"
 
 namespace fcpwgb {
 
+namespace {
+cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s) {
+    switch (W) {
+        case 2: return launchWideClosestT<2>(bits, dim, precise, l, s);
+        case 4: return launchWideClosestT<4>(bits, dim, precise, l, s);
+        default: return launchWideClosestT<8>(bits, dim, precise, l, s);
+    }
+}
+cudaError_t launchRequant(int W, int bits, unsigned char *wn, const int32_t *cb, const unsigned char *bn, int stride,
+                          uint32_t n, uint32_t *err, cudaStream_t s) {
+    switch (W) {
+        case 2: return launchRequantizeT<2>(bits, wn, cb, bn, stride, n, err, s);
+        case 4: return launchRequantizeT<4>(bits, wn, cb, bn, stride, n, err, s);
+        default: return launchRequantizeT<8>(bits, wn, cb, bn, stride, n, err, s);
+    }
+}
+}  // namespace
+
+int GpuScene::ensureWide(cudaStream_t st) {
+    const WideConfig &c = wideConfig;
+    if (wide.valid && wide.branching == c.branching && wide.bits == c.bits) return 0;
+    WideHost h;
+    if (!buildWideTree(c.branching, c.bits, hostNP, hostOff, hostBoxes, h))
+        return setError(FCPWGB_ERR_UNSUPPORTED, "this tree cannot be collapsed into the requested wide layout");
+    int rc;
+    if ((rc = wideNodes.upload(h.nodes.data(), h.nodes.size(), st))) return rc;
+    if ((rc = wideChildBinary.upload(h.childBinary.data(), h.childBinary.size() * sizeof(int32_t), st))) return rc;
+    cudaError_t e;
+    if (dim == 3) {
+        if ((rc = widePrims.ensure((size_t)nPrims * 48))) return rc;
+        if ((e = launchPackTri48((const DevTriangle *)prims.ptr, nPrims, (float4 *)widePrims.ptr, st)) != cudaSuccess)
+            return cudaFail(e, "pack triangles");
+    }
+    // the host boxes are those of the transfer; the device tree may have been refit since
+    if ((e = launchRequant(c.branching, c.bits, (unsigned char *)wideNodes.ptr, (const int32_t *)wideChildBinary.ptr,
+                           (const unsigned char *)nodes.ptr, snch ? 64 : 32, h.nNodes, (uint32_t *)errorWord.ptr,
+                           st)) != cudaSuccess)
+        return cudaFail(e, "requantize");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "wide build");
+    wide.valid = true;
+    wide.branching = c.branching;
+    wide.bits = c.bits;
+    wide.nNodes = h.nNodes;
+    wide.depth = h.depth;
+    wide.builtFromVersion = treeVersion;
+    if (numSMs == 0) {
+        cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device);
+        if (numSMs <= 0) numSMs = 1;
+    }
+    return 0;
+}
+
+int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal,
+                          unsigned long long *stats, cudaStream_t st) {
+    int rc = ensureWide(st);
+    if (rc) return rc;
+    if (n == 0) return 0;
+    const WideConfig &c = wideConfig;
+    WideLaunch l;
+    l.nodes = (const unsigned char *)wideNodes.ptr;
+    l.prims = dim == 3 ? (const unsigned char *)widePrims.ptr : (const unsigned char *)prims.ptr;
+    l.spheres = spheres;
+    l.out = out;
+    l.n = n;
+    l.recordNormal = recordNormal;
+    l.errorWord = (uint32_t *)errorWord.ptr;
+    l.stats = stats;
+    cudaError_t e;
+    if (c.sortQueries && n >= 4096) {
+        if ((rc = sortCells.ensure(sizeof(uint32_t) << kSortCellBits))) return rc;
+        if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
+        if ((rc = sortSpheres.ensure((size_t)n * sizeof(DevSphere)))) return rc;
+        // grid over the scene box grown by its extent on every side
+        SortGrid g;
+        float lo[3], ext[3];
+        for (int a = 0; a < 3; a++) {
+            float e0 = std::max(rootBox[3 + a] - rootBox[a], 1e-6f);
+            lo[a] = rootBox[a] - e0;
+            ext[a] = 3.0f * e0;
+        }
+        float cells = dim == 3 ? 64.0f : 512.0f;
+        g.lo = make_float3(lo[0], lo[1], lo[2]);
+        g.invCell = make_float3(cells / ext[0], cells / ext[1], cells / ext[2]);
+        g.dim = dim;
+        if ((e = launchSortQueries(g, spheres, n, (uint32_t *)sortCells.ptr, (DevSphere *)sortSpheres.ptr,
+                                   (uint32_t *)sortPerm.ptr, st)) != cudaSuccess)
+            return cudaFail(e, "sort queries");
+        l.spheres = (const DevSphere *)sortSpheres.ptr;
+        l.perm = (const uint32_t *)sortPerm.ptr;
+    }
+    uint32_t blocks = (n + 127) / 128;
+    if (c.persistent) {
+        if ((rc = workCounter.ensure(16))) return rc;
+        if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
+        l.counter = (uint32_t *)workCounter.ptr;
+        blocks = std::min<uint32_t>(blocks, (uint32_t)numSMs * 16u);
+    }
+    l.grid = blocks;
+    if (!stats && (rc = timeStart(st))) return rc;
+    if ((e = launchWide(c.branching, c.bits, dim, c.precise != 0, l, st)) != cudaSuccess)
+        return cudaFail(e, "wide closest point launch");
+    return stats ? 0 : timeEnd(st);
+}
+
+int GpuScene::timeStart(cudaStream_t st) {
+    if (!timing) return 0;
+    std::pair<cudaEvent_t, cudaEvent_t> p;
+    if (!freeEvents.empty()) {
+        p = freeEvents.back();
+        freeEvents.pop_back();
+    } else {
+        cudaError_t e = cudaEventCreate(&p.first);
+        if (e == cudaSuccess) e = cudaEventCreate(&p.second);
+        if (e != cudaSuccess) return cudaFail(e, "cudaEventCreate");
+    }
+    timedEvents.push_back(p);
+    cudaError_t e = cudaEventRecord(p.first, st);
+    return e == cudaSuccess ? 0 : cudaFail(e, "cudaEventRecord");
+}
+
+int GpuScene::timeEnd(cudaStream_t st) {
+    if (!timing || timedEvents.empty()) return 0;
+    cudaError_t e = cudaEventRecord(timedEvents.back().second, st);
+    return e == cudaSuccess ? 0 : cudaFail(e, "cudaEventRecord");
+}
+
 int GpuScene::closestPoints(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal,
                             cudaStream_t st) {
+    if (useWide()) return wideClosest(spheres, out, n, recordNormal, nullptr, st);
+    int rc = timeStart(st);
+    if (rc) return rc;
     cudaError_t e = launchClosestPointBinary(view(), spheres, out, n, recordNormal, st);
-    return e == cudaSuccess ? 0 : cudaFail(e, "closest point launch");
+    if (e != cudaSuccess) return cudaFail(e, "closest point launch");
+    return timeEnd(st);
 }
 
 int GpuScene::closestPointsStats(const DevSphere *spheres, DevInteraction *out, uint32_t n,
                                  unsigned long long *stats, cudaStream_t st) {
+    if (useWide()) return wideClosest(spheres, out, n, 0, stats, st);
     cudaError_t e = launchClosestPointBinaryStats(view(), spheres, out, n, stats, st);
     return e == cudaSuccess ? 0 : cudaFail(e, "closest point stats launch");
 }
@@ -47,8 +181,15 @@ int GpuScene::closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_in
 }
 
 int GpuScene::afterRefit(cudaStream_t st) {
-    (void)st;
-    wide.clear();
+    if (!wide.valid) return 0;
+    cudaError_t e;
+    if (dim == 3 && (e = launchPackTri48((const DevTriangle *)prims.ptr, nPrims, (float4 *)widePrims.ptr, st)) !=
+                        cudaSuccess)
+        return cudaFail(e, "pack triangles");
+    if ((e = launchRequant(wide.branching, wide.bits, (unsigned char *)wideNodes.ptr,
+                           (const int32_t *)wideChildBinary.ptr, (const unsigned char *)nodes.ptr, snch ? 64 : 32,
+                           wide.nNodes, (uint32_t *)errorWord.ptr, st)) != cudaSuccess)
+        return cudaFail(e, "requantize");
     return 0;
 }
 

@@ -3,6 +3,8 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -62,9 +64,28 @@ struct GpuScene {
     uint64_t treeVersion = 0;
     DeviceBuffer nodes, prims, sils, parents, leaves, counters, primVerts, silVerts, errorWord;
 
+    // host copy of the transferred topology (input of the wide collapse)
+    std::vector<uint32_t> hostNP, hostOff;
+    std::vector<float> hostBoxes;  // pMin[3], pMax[3] per node, as transferred
+    float rootBox[6] = {0, 0, 0, 0, 0, 0};
+
     // derived wide / quantised tree (built on demand, see wide.h)
     WideConfig wideConfig;
     WideTree wide;
+    DeviceBuffer wideNodes, wideChildBinary, widePrims;
+    // scratch of the fast path: query sort cells / permutation / sorted copy, work counter
+    DeviceBuffer sortCells, sortPerm, sortSpheres, workCounter;
+    int numSMs = 0;
+
+    // optional event timing of traversal launches
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timedEvents, freeEvents;
+    int timeStart(cudaStream_t st);
+    int timeEnd(cudaStream_t st);
+    ~GpuScene() {
+        for (auto &p : timedEvents) { cudaEventDestroy(p.first); cudaEventDestroy(p.second); }
+        for (auto &p : freeEvents) { cudaEventDestroy(p.first); cudaEventDestroy(p.second); }
+    }
 
     // staging for the host-array entry points
     DeviceBuffer qIn0, qIn1, qOut;
@@ -86,6 +107,11 @@ struct GpuScene {
                           int recordNormal);
     // keeps derived trees in step after the binary tree was refit on stream st
     int afterRefit(cudaStream_t st);
+    // builds (or rebuilds) the wide tree the current config asks for
+    int ensureWide(cudaStream_t st);
+    bool useWide() const { return wideConfig.branching > 0; }
+    int wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal,
+                    unsigned long long *stats, cudaStream_t st);
 };
 
 }  // namespace fcpwgb

@@ -199,6 +199,23 @@ class _GPUScene:
     def handle(self):
         return self._h
 
+    # -- traversal variant -------------------------------------------------
+    def set_traversal(self, branching: int = 0, bits: int = 32, sort_queries: bool = True,
+                      persistent: bool = True, precise: bool = True) -> None:
+        """Selects the closest point traversal (see fcpwgb_traversal_config):
+        branching 0 is the reference-order binary traversal; 2/4/8 use a wide
+        tree with 32-, 16- or 8-bit child boxes."""
+        from ._lib import TraversalConfig
+        cfg = TraversalConfig(int(branching), int(bits), 128, int(bool(sort_queries)), int(bool(persistent)),
+                              int(bool(precise)))
+        check(lib().fcpwgb_gpu_scene_set_traversal(self._h, C.byref(cfg)))
+
+    def get_traversal(self) -> dict:
+        from ._lib import TraversalConfig
+        cfg = TraversalConfig()
+        check(lib().fcpwgb_gpu_scene_get_traversal(self._h, C.byref(cfg)))
+        return {f: getattr(cfg, f) for f, _ in TraversalConfig._fields_}
+
     # -- transfer / refit --------------------------------------------------
     def transfer_to_gpu(self, scene: _Scene, device_backend: str = "default") -> None:
         """GPUScene::transferToGPU (include/fcpw/fcpw_gpu.h:21)."""

@@ -143,6 +143,15 @@ int fcpwgb_cpu_bvh_export(const fcpwgb_cpu_bvh *bvh, void *nodes, void *primitiv
 int fcpwgb_cpu_bvh_export_topology(const fcpwgb_cpu_bvh *bvh, int32_t *index_map,
                                    int32_t *prim_vertices, uint32_t *prim_index,
                                    int32_t *sil_vertices);
+/* Collapses the host tree into the wide layout the GPU fast path uses
+ * (branching 2/4/8, child boxes at 32/16/8 bits; the record format is
+ * documented in fcpw_gb300/csrc/wide.h). Call with nodes == NULL to query
+ * *n_nodes and *node_bytes; then pass buffers of n_nodes * node_bytes bytes
+ * and n_nodes * branching int32 (child_binary: binary node behind every slot,
+ * -1 for an empty slot). Returns FCPWGB_ERR_UNSUPPORTED when the tree cannot
+ * be encoded. */
+int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *bvh, int branching, int bits, void *nodes,
+                               int32_t *child_binary, uint32_t *n_nodes, uint32_t *node_bytes);
 /* updateObjectVertices (fcpw.inl:1129-1143): replaces the vertex positions
  * (caller vertex order) so that a following export yields the moved
  * primitives and silhouettes. The tree itself is left unchanged. */
@@ -181,6 +190,27 @@ int fcpwgb_gpu_scene_refit(fcpwgb_gpu_scene *scene, const void *primitives,
  * tree refit; asynchronous on stream (a cudaStream_t; NULL is the CUDA default stream). */
 int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *scene, const float *positions,
                                             uint32_t n_vertices, void *stream);
+
+/* Traversal variant used by the closest point entry points of a scene. With
+ * branching 0 the transferred binary tree is traversed in the reference GPU
+ * order (bvh.slang:395-502). With branching 2, 4 or 8 a wide tree is derived
+ * from it (children of largest surface area expanded first) whose child boxes
+ * are stored in 32-bit floats or conservatively quantised to 16 or 8 bits;
+ * sort_queries reorders each batch spatially before traversal, persistent
+ * runs one resident block set that fetches query chunks from a counter, and
+ * precise recomputes the winning primitive's distance and point in FP64.
+ * Defaults: {0, 32, 128, 1, 1, 1}. Results differ from the binary order only
+ * on equidistant ties (and, with precise, by the FP32 rounding removed). */
+typedef struct {
+    int branching;     /* 0, 2, 4 or 8 */
+    int bits;          /* 32, 16 or 8 */
+    int block_size;    /* threads per block of the wide kernels (128) */
+    int sort_queries;  /* 0 or 1 */
+    int persistent;    /* 0 or 1 */
+    int precise;       /* 0 or 1 */
+} fcpwgb_traversal_config;
+int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *scene, const fcpwgb_traversal_config *config);
+int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *scene, fcpwgb_traversal_config *config);
 
 /* ----- queries with HOST arrays (synchronous, as the reference) ----- */
 /* findClosestPoints, fcpw_gpu.h:60-62 */
@@ -225,6 +255,13 @@ int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *scene,
  * algorithmic bytes of a launch; results are written to interactions. */
 int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                           fcpwgb_interaction *interactions, uint32_t n, uint64_t *stats);
+
+/* Kernel timing: when enabled, every closest point traversal launch of the
+ * scene is bracketed by CUDA events recorded on its stream.
+ * fcpwgb_gpu_scene_kernel_time synchronises on the recorded events and
+ * returns (then clears) the summed duration in ms and the number of launches. */
+int fcpwgb_gpu_scene_enable_kernel_timing(fcpwgb_gpu_scene *scene, int enable);
+int fcpwgb_gpu_scene_kernel_time(fcpwgb_gpu_scene *scene, double *total_ms, uint32_t *launches);
 
 /* Copies the scene's current (possibly refit) binary tree back to the host in
  * the interop layout it was transferred in (fcpwgb_bvh_node or

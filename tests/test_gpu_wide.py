@@ -1,0 +1,107 @@
+"""GPU parity of the wide / quantised closest-point kernels against the oracle
+(reference CPU order) and FP64, for every branching factor and box precision."""
+import numpy as np
+import pytest
+
+import fcpw_gb300 as F
+from fcpw_gb300 import records as R
+from fcpw_gb300 import workloads as W
+from helpers import build_scene, compare_closest, relative_error
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torus():
+    v, f = W.torus(256, 128, W.SEED_BASE + 2)
+    s = build_scene(3, v, f)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    pts = W.uniform_points(120000, 3, -2, 2, 41)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref = O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts, R.FLT_MAX))
+    return s, g, pts, ref, prims
+
+
+def _run(g, pts, r2=None):
+    out = F.GPUInteractionList()
+    r2 = np.full(len(pts), R.FLT_MAX, np.float32) if r2 is None else r2
+    g.find_closest_points(pts, r2, out)
+    return out.array()
+
+
+@pytest.mark.parametrize("branching", [2, 4, 8])
+@pytest.mark.parametrize("bits", [32, 16, 8])
+def test_wide_variants_match_oracle(torus, branching, bits):
+    s, g, pts, ref, prims = torus
+    g.set_traversal(branching, bits, sort_queries=True, persistent=True, precise=False)
+    got = _run(g, pts)
+    compare_closest(3, prims, pts, got, ref, f"wide {branching}/{bits}")
+    assert g.check_errors() == 0
+
+
+@pytest.mark.parametrize("sort_queries,persistent", [(False, False), (True, False), (False, True)])
+def test_wide_scheduling_options_agree(torus, sort_queries, persistent):
+    s, g, pts, ref, prims = torus
+    g.set_traversal(4, 8, sort_queries=sort_queries, persistent=persistent, precise=False)
+    got = _run(g, pts)
+    compare_closest(3, prims, pts, got, ref, "wide scheduling")
+
+
+def test_precise_mode_within_1e6_of_fp64(torus):
+    s, g, pts, ref, prims = torus
+    g.set_traversal(4, 8, precise=True)
+    sub = pts[:3000]
+    got = _run(g, sub)
+    d64, _ = O.closest_points_brute_f64(3, prims, R.make_spheres(sub, R.FLT_MAX))
+    rel = relative_error(got["d"], d64)
+    assert rel.max() <= 1e-6, f"max relative error {rel.max():.3e}"
+    # plain FP32 (reference arithmetic) for comparison: larger near the surface
+    g.set_traversal(0)
+    plain = _run(g, sub)
+    assert relative_error(plain["d"], d64).max() >= rel.max()
+
+
+def test_wide_finite_radius_and_normals(torus):
+    s, g, pts, ref, prims = torus
+    r2 = (0.05 * W.rng(42).uniform(0, 1, len(pts))).astype(np.float32)
+    nodes, _, _ = s.cpu_bvh.export()
+    ref2 = O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts, r2), record_normals=True)
+    g.set_traversal(8, 16, precise=False)
+    out = F.GPUInteractionList()
+    g.find_closest_points(pts, r2, out, True)
+    got = out.array()
+    compare_closest(3, prims, pts, got, ref2, "wide finite radius")
+    same = (got["index"] == ref2["index"]) & (ref2["index"] != R.UINT_MAX)
+    assert np.allclose(got["n"][same], ref2["n"][same], atol=1e-6)
+
+
+def test_wide_after_refit(torus):
+    v, f = W.perturbed_sphere(24, W.SEED_BASE + 8)
+    s = build_scene(3, v, f)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    g.set_traversal(4, 8, precise=False)
+    pts = W.uniform_points(30000, 3, -1.5, 1.5, 43)
+    _run(g, pts)  # builds the wide tree
+    v2 = (v * 1.1 + 0.01 * W.rng(44).standard_normal(v.shape)).astype(np.float32)
+    s.update_object_vertices(v2, 0)
+    g.refit(s, True)
+    got = _run(g, pts)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref = O.closest_points_bvh(3, O.refit(3, nodes, prims), prims, R.make_spheres(pts, R.FLT_MAX))
+    compare_closest(3, prims, pts, got, ref, "wide after refit")
+
+
+def test_wide_2d_segments():
+    v, sg = W.star_polylines(64, 128, W.SEED_BASE + 3)
+    s = build_scene(2, v, sg)
+    g = F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    pts = W.uniform_points(60000, 2, -3, 3, 45)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref = O.closest_points_bvh(2, nodes, prims, R.make_spheres(pts, R.FLT_MAX))
+    for b, q in [(4, 8), (8, 16), (2, 32)]:
+        g.set_traversal(b, q, precise=False)
+        compare_closest(2, prims, pts, _run(g, pts), ref, f"2D wide {b}/{q}")
