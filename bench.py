@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--variant", default="auto")
     ap.add_argument("--queries", type=int, default=N_QUERIES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-loss", action="store_true", help="skip the fwd/fwd+bwd distance loss measurement")
     return ap.parse_args()
 
 
@@ -166,6 +167,56 @@ def profiled_traffic(variant: str):
         return None
     d = json.loads(p.read_text())
     return d.get(variant)
+
+
+def distance_loss_bench(device_index: int, steps: int = 20, warmup: int = 5):
+    """fwd vs fwd+bwd of loss = mean(d^2) on a 200,000-triangle perturbed sphere
+    (geodesic frequency 100) and 2^20 uniform queries, with the vertices moved
+    onto the device copy and the tree refit on the GPU in every forward."""
+    import torch
+    import fcpw_gb300 as F
+    from fcpw_gb300 import workloads as W
+    from fcpw_gb300.autograd import closest_point_distance
+    dev = torch.device("cuda", device_index)
+    v, f = W.perturbed_sphere(100, W.SEED_BASE + 4)
+    s = F.Scene3D()
+    s.set_object_count(1)
+    s.set_object_vertices(v, 0)
+    s.set_object_triangles(f, 0)
+    s.build(F.AggregateType.Bvh_SurfaceArea, False)
+    gpu = F.GPUScene3D("", False, device=device_index)
+    gpu.transfer_to_gpu(s)
+    gpu.set_traversal(4, 8, sort_queries=True, persistent=True, precise=True)
+    x = torch.from_numpy(W.uniform_points(1 << 20, 3, -1.5, 1.5, W.SEED_BASE + 4)).to(dev)
+    verts = torch.from_numpy(v).to(dev).requires_grad_(True)
+    stream = torch.cuda.current_stream(dev)
+
+    def fwd():
+        d = closest_point_distance(gpu, x, verts, refit=True)
+        return (d * d).mean()
+
+    def fwd_bwd():
+        verts.grad = None
+        fwd().backward()
+
+    def time_it(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / steps
+
+    with torch.no_grad():
+        fwd_ms = time_it(fwd)
+    fb_ms = time_it(fwd_bwd)
+    return {"workload": "loss = mean unsigned distance^2, perturbed sphere 200,000 triangles (geodesic frequency 100), "
+                        "2^20 queries uniform in [-1.5,1.5]^3, GPU refit every forward, backward to queries and vertices",
+            "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "ratio": fb_ms / fwd_ms, "target_ratio_max": 2.5}
 
 
 # ------------------------------------------------------------------ main
@@ -323,6 +374,8 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": fast_stats["bytes"], "per_query": fast_stats["per_query"]},
             "clocks": clocks, "accuracy": accuracy,
         }
+        if not args.no_loss:
+            result["distance_loss"] = distance_loss_bench(local)
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(scene, pts)
     if world > 1:

@@ -43,6 +43,8 @@ SIGNATURES = {
     "fcpwgb_find_closest_silhouette_points_device": (c_int, [P, P, P, P, c_uint32, c_float, c_float, P]),
     "fcpwgb_closest_points_traversal_stats": (c_int, [P, P, P, c_uint32, P]),
     "fcpwgb_gpu_scene_export_nodes": (c_int, [P, P]),
+    "fcpwgb_closest_point_backward_device": (c_int, [P, P, P, P, c_uint32, P, P, P]),
+    "fcpwgb_ray_backward_device": (c_int, [P, P, P, P, c_uint32, P, P, P, P]),
     "fcpwgb_gpu_scene_enable_kernel_timing": (c_int, [P, c_int]),
     "fcpwgb_gpu_scene_kernel_time": (c_int, [P, C.POINTER(C.c_double), C.POINTER(c_uint32)]),
     "fcpwgb_gpu_scene_set_traversal": (c_int, [P, P]),

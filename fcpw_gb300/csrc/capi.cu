@@ -357,10 +357,34 @@ extern "C" int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *s, int bvh_type, cons
     if ((rc = s->parents.upload(parents.data(), parents.size() * sizeof(int32_t), s->stream))) return rc;
     if ((rc = s->leaves.upload(leaves.data(), leaves.size() * sizeof(uint32_t), s->stream))) return rc;
     if ((rc = s->counters.ensure((size_t)n_nodes * sizeof(uint32_t)))) return rc;
+    std::vector<int32_t> origVerts;
+    std::vector<uint32_t> csrOff, csrCorner;
     if (prim_vertices) {
         if ((rc = s->primVerts.upload(prim_vertices, (size_t)n_primitives * s->dim * sizeof(int32_t), s->stream)))
             return rc;
         s->nVertices = n_vertices;
+        // corner table in original primitive order and the vertex -> corner CSR
+        // (corners of a vertex listed in increasing corner id: a fixed order)
+        int d = s->dim;
+        origVerts.assign((size_t)n_primitives * d, -1);
+        for (uint32_t k = 0; k < n_primitives; k++) {
+            uint32_t idx = d == 3 ? ((const fcpwgb_triangle *)primitives)[k].index
+                                  : ((const fcpwgb_line_segment *)primitives)[k].index;
+            if (idx >= n_primitives) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "primitive index out of range");
+            for (int j = 0; j < d; j++) origVerts[(size_t)idx * d + j] = prim_vertices[(size_t)k * d + j];
+        }
+        csrOff.assign((size_t)n_vertices + 1, 0);
+        for (int32_t v : origVerts) {
+            if (v < 0) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "primitive indices are not a permutation");
+            csrOff[(size_t)v + 1]++;
+        }
+        for (uint32_t v = 0; v < n_vertices; v++) csrOff[v + 1] += csrOff[v];
+        csrCorner.resize(origVerts.size());
+        std::vector<uint32_t> cursor(csrOff.begin(), csrOff.end() - 1);
+        for (uint32_t c = 0; c < (uint32_t)origVerts.size(); c++) csrCorner[cursor[origVerts[c]]++] = c;
+        if ((rc = s->origVerts.upload(origVerts.data(), origVerts.size() * sizeof(int32_t), s->stream))) return rc;
+        if ((rc = s->csrOff.upload(csrOff.data(), csrOff.size() * sizeof(uint32_t), s->stream))) return rc;
+        if ((rc = s->csrCorner.upload(csrCorner.data(), csrCorner.size() * sizeof(uint32_t), s->stream))) return rc;
     }
     FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
 
@@ -371,6 +395,8 @@ extern "C" int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *s, int bvh_type, cons
     s->nSils = snch ? n_silhouettes : 0;
     s->nLeaves = (uint32_t)leaves.size();
     s->maxDepth = maxDepth;
+    s->hasTopology = prim_vertices != nullptr;
+    if (!s->hasTopology) s->nVertices = 0;
     s->hostNP = nP;
     s->hostOff = off;
     s->hostBoxes.resize((size_t)n_nodes * 6);
@@ -476,7 +502,7 @@ extern "C" int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *s, cons
                                                        uint32_t n_vertices, void *stream) {
     int rc = requireTree(s);
     if (rc) return rc;
-    if (!s->primVerts.ptr)
+    if (!s->hasTopology)
         return setError(FCPWGB_ERR_UNSUPPORTED, "the tree was transferred without prim_vertices");
     if (!positions || n_vertices != s->nVertices)
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "positions must hold the transferred vertex count");
@@ -670,6 +696,52 @@ extern "C" int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *s, fcpwgb_
     c->sort_queries = s->wideConfig.sortQueries;
     c->persistent = s->wideConfig.persistent;
     c->precise = s->wideConfig.precise;
+    return FCPWGB_OK;
+}
+
+// ------------------------------------------------------------- gradients
+static int gradView(fcpwgb_gpu_scene *s, GradView &gv) {
+    if (!s->hasTopology)
+        return setError(FCPWGB_ERR_UNSUPPORTED, "gradients need the tree transferred with prim_vertices");
+    int rc;
+    if ((rc = s->gradCorners.ensure((size_t)s->nPrims * s->dim * 3 * sizeof(long long)))) return rc;
+    if ((rc = s->gradMax.ensure(16))) return rc;
+    gv.dim = s->dim;
+    gv.nPrims = s->nPrims;
+    gv.nVertices = s->nVertices;
+    gv.origVerts = (const int32_t *)s->origVerts.ptr;
+    gv.csrOff = (const uint32_t *)s->csrOff.ptr;
+    gv.csrCorner = (const uint32_t *)s->csrCorner.ptr;
+    gv.corners = (long long *)s->gradCorners.ptr;
+    gv.maxBits = (unsigned int *)s->gradMax.ptr;
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_closest_point_backward_device(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                    const fcpwgb_interaction *forward, const float *grad_d,
+                                                    uint32_t n, float *grad_x, float *grad_vertices, void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if ((n > 0 && (!spheres || !forward || !grad_d || !grad_x)) || !grad_vertices)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL array");
+    GradView gv;
+    if ((rc = gradView(s, gv))) return rc;
+    FCPWGB_CUDA(launchDistanceBackward(gv, (const DevSphere *)spheres, (const DevInteraction *)forward, grad_d, n,
+                                       grad_x, grad_vertices, s->pick(stream)));
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_ray_backward_device(fcpwgb_gpu_scene *s, const fcpwgb_ray *rays,
+                                          const fcpwgb_interaction *forward, const float *grad_t, uint32_t n,
+                                          float *grad_o, float *grad_dir, float *grad_vertices, void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if ((n > 0 && (!rays || !forward || !grad_t || !grad_o || !grad_dir)) || !grad_vertices)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL array");
+    GradView gv;
+    if ((rc = gradView(s, gv))) return rc;
+    FCPWGB_CUDA(launchRayBackward(gv, (const DevRay *)rays, (const DevInteraction *)forward, grad_t, n, grad_o,
+                                  grad_dir, grad_vertices, s->pick(stream)));
     return FCPWGB_OK;
 }
 

@@ -112,6 +112,28 @@ template<int W, int BITS> struct WideNodeRegs {
 constexpr uint32_t kLeafBit = 0x80000000u;
 FCPWGB_D uint32_t packLeaf(uint32_t off, uint32_t cnt) { return kLeafBit | (cnt << 27) | off; }
 
+// Sorting networks over packed keys (non-negative float bits with the child
+// slot in the low bits): integer min/max compare-exchanges. Optimal networks
+// for 2, 4 (5 comparators) and 8 (19 comparators) inputs.
+FCPWGB_D void cmpx(uint32_t &a, uint32_t &b) {
+    uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+template<int W> FCPWGB_D void sortNetwork(uint32_t (&k)[W]);
+template<> FCPWGB_D void sortNetwork<2>(uint32_t (&k)[2]) { cmpx(k[0], k[1]); }
+template<> FCPWGB_D void sortNetwork<4>(uint32_t (&k)[4]) {
+    cmpx(k[0], k[1]); cmpx(k[2], k[3]); cmpx(k[0], k[2]); cmpx(k[1], k[3]); cmpx(k[1], k[2]);
+}
+template<> FCPWGB_D void sortNetwork<8>(uint32_t (&k)[8]) {
+    cmpx(k[0], k[2]); cmpx(k[1], k[3]); cmpx(k[4], k[6]); cmpx(k[5], k[7]);
+    cmpx(k[0], k[4]); cmpx(k[1], k[5]); cmpx(k[2], k[6]); cmpx(k[3], k[7]);
+    cmpx(k[0], k[1]); cmpx(k[2], k[3]); cmpx(k[4], k[5]); cmpx(k[6], k[7]);
+    cmpx(k[2], k[4]); cmpx(k[3], k[5]);
+    cmpx(k[1], k[4]); cmpx(k[3], k[6]);
+    cmpx(k[1], k[2]); cmpx(k[3], k[4]); cmpx(k[5], k[6]);
+}
+
 // Closest point of one query on a wide tree (bvh.slang:395-502 semantics:
 // inclusive d2Min <= r2 pruning, r2 shrunk by child d2Max, primitives accepted
 // when d*d <= r2, the later of equal distances wins).
@@ -129,51 +151,56 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
         if (!(cur & kLeafBit)) {
             node.load(nodes, cur);
             nExpanded++;
-            float dmin[W];
-            uint32_t key[W];
+            constexpr uint32_t kSlotMask = W - 1;
+            float d2Min[W];
 #pragma unroll
             for (int k = 0; k < W; k++) {
-                uint32_t n = node.cnt(k);
                 float lo0 = node.bound(0, k), lo1 = node.bound(1, k), lo2 = node.bound(2, k);
                 float hi0 = node.bound(3, k), hi1 = node.bound(4, k), hi2 = node.bound(5, k);
-                float d2Min, d2Max;
-                boxSphereDist(make_float3(lo0, lo1, lo2), make_float3(hi0, hi1, hi2), c, d2Min, d2Max);
-                if (n == kWideEmpty) { d2Min = kFltMax; d2Max = kFltMax; }
-                r2 = fminf(r2, d2Max);
-                dmin[k] = n == kWideEmpty ? INFINITY : d2Min;
-                key[k] = n == 0 ? node.ref(k) : packLeaf(node.ref(k), n);
+                float d2Max;
+                boxSphereDist(make_float3(lo0, lo1, lo2), make_float3(hi0, hi1, hi2), c, d2Min[k], d2Max);
+                if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, d2Max);
             }
-            // ascending by distance (insertion sort, unrolled)
-#pragma unroll
-            for (int i = 1; i < W; i++) {
-#pragma unroll
-                for (int j = i; j > 0; j--) {
-                    bool sw = dmin[j] < dmin[j - 1];
-                    float td = sw ? dmin[j] : dmin[j - 1];
-                    dmin[j] = sw ? dmin[j - 1] : dmin[j];
-                    dmin[j - 1] = td;
-                    uint32_t tk = sw ? key[j] : key[j - 1];
-                    key[j] = sw ? key[j - 1] : key[j];
-                    key[j - 1] = tk;
-                }
-            }
+            // keys: distance bits with the slot in the low bits, truncating the
+            // distance downwards (visits are decided on d2Min <= r2, so a smaller
+            // stored distance can only add visits, never skip one)
+            uint32_t key[W];
             int nh = 0;
 #pragma unroll
-            for (int k = 0; k < W; k++) nh += dmin[k] <= r2 ? 1 : 0;
+            for (int k = 0; k < W; k++) {
+                bool hit = node.cnt(k) != kWideEmpty && d2Min[k] <= r2;
+                key[k] = hit ? ((__float_as_uint(d2Min[k]) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
+                nh += hit ? 1 : 0;
+            }
+            sortNetwork<W>(key);
             if (nh > 0) {
                 if (sp + nh - 1 > kWideStack) {
                     atomicOr(errorWord, kErrStackOverflow);
                     return found;
                 }
+                uint32_t firstRef = 0;
 #pragma unroll
-                for (int k = W - 1; k >= 1; k--) {
+                for (int k = W - 1; k >= 0; k--) {
                     if (k < nh) {
-                        stRef[sp] = key[k];
-                        stD[sp] = dmin[k];
-                        sp++;
+                        uint32_t slot = key[k] & kSlotMask, ref = 0, n = 0;
+#pragma unroll
+                        for (int s = 0; s < W; s++) {
+                            if (slot == (uint32_t)s) {
+                                ref = node.ref(s);
+                                n = node.cnt(s);
+                            }
+                        }
+                        uint32_t packed = n == 0 ? ref : packLeaf(ref, n);
+                        if (k == 0) {
+                            firstRef = packed;
+                        } else {
+                            stRef[sp] = packed;
+                            stD[sp] = __uint_as_float(key[k] & ~kSlotMask);
+                            sp++;
+                        }
                     }
                 }
-                cur = key[0];
+                cur = firstRef;
                 continue;
             }
         } else {
@@ -215,7 +242,7 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
 // read in sorted order and results scattered back to out[perm[i]]; with
 // `stats` non-NULL expansions and primitive tests are summed into stats[1..2].
 template<int W, int BITS, class Prim, bool PRECISE>
-__global__ void __launch_bounds__(128) kWideClosestPoint(const unsigned char *__restrict__ nodes,
+__global__ void __launch_bounds__(128, 8) kWideClosestPoint(const unsigned char *__restrict__ nodes,
                                                          const unsigned char *__restrict__ prims,
                                                          const DevSphere *__restrict__ spheres,
                                                          const uint32_t *__restrict__ perm,

@@ -60,6 +60,21 @@ cudaError_t launchSortQueries(const SortGrid &g, const DevSphere *spheres, uint3
                               DevSphere *sorted, uint32_t *perm, cudaStream_t s);
 cudaError_t launchPackTri48(const DevTriangle *tris, uint32_t n, float4 *out, cudaStream_t s);
 
+// backward of the differentiable queries (k_grad.cu)
+struct GradView {
+    int dim = 3;
+    uint32_t nPrims = 0, nVertices = 0;
+    const int32_t *origVerts = nullptr;   // caller vertex of every corner, original primitive order
+    const uint32_t *csrOff = nullptr;     // vertex -> corners (nVertices + 1 offsets)
+    const uint32_t *csrCorner = nullptr;  // corner ids (prim * dim + corner) in fixed order
+    long long *corners = nullptr;         // scratch: nPrims * dim * 3 fixed-point partial sums
+    unsigned int *maxBits = nullptr;      // scratch: max |dL/dout| as float bits
+};
+cudaError_t launchDistanceBackward(const GradView &gv, const DevSphere *spheres, const DevInteraction *fwd,
+                                   const float *gradD, uint32_t n, float *gradX, float *gradV, cudaStream_t s);
+cudaError_t launchRayBackward(const GradView &gv, const DevRay *rays, const DevInteraction *fwd, const float *gradT,
+                              uint32_t n, float *gradO, float *gradDir, float *gradV, cudaStream_t s);
+
 // refit (k_refit.cu)
 struct RefitView {
     int dim = 3;

@@ -87,6 +87,10 @@ struct GpuScene {
         for (auto &p : freeEvents) { cudaEventDestroy(p.first); cudaEventDestroy(p.second); }
     }
 
+    bool hasTopology = false;  // prim_vertices were given at transfer (device updates, gradients)
+    // differentiation: corner -> caller vertex table and the static vertex -> corner CSR
+    DeviceBuffer origVerts, csrOff, csrCorner, gradCorners, gradMax;
+
     // staging for the host-array entry points
     DeviceBuffer qIn0, qIn1, qOut;
 

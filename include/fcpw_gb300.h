@@ -256,6 +256,22 @@ int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *scene,
 int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                           fcpwgb_interaction *interactions, uint32_t n, uint64_t *stats);
 
+/* ----- differentiation (no counterpart in the reference; needs a tree
+ * transferred with prim_vertices). Device arrays, asynchronous on stream. ----- */
+/* Backward of the unsigned closest point distance d(x) = |x - p(x, V)| from
+ * the forward records of fcpwgb_find_closest_points_device: writes
+ * grad_x = dL/dx (n x dim) and grad_vertices = dL/dV (n_vertices x dim, the
+ * caller's vertex order), given grad_d = dL/dd. Queries without a hit or at
+ * distance 0 contribute nothing. The vertex reduction is deterministic. */
+int fcpwgb_closest_point_backward_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                         const fcpwgb_interaction *forward, const float *grad_d, uint32_t n,
+                                         float *grad_x, float *grad_vertices, void *stream);
+/* Backward of the ray hit distance t(o, dir, V) from the forward records of
+ * fcpwgb_intersect_rays_device: writes dL/do, dL/ddir (n x dim) and dL/dV. */
+int fcpwgb_ray_backward_device(fcpwgb_gpu_scene *scene, const fcpwgb_ray *rays, const fcpwgb_interaction *forward,
+                               const float *grad_t, uint32_t n, float *grad_o, float *grad_dir,
+                               float *grad_vertices, void *stream);
+
 /* Kernel timing: when enabled, every closest point traversal launch of the
  * scene is bracketed by CUDA events recorded on its stream.
  * fcpwgb_gpu_scene_kernel_time synchronises on the recorded events and
