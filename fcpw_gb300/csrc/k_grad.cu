@@ -64,9 +64,13 @@ __global__ void kDistanceGrad(int dim, const DevSphere *__restrict__ spheres,
     DevInteraction r = fwd[q];
     float3 x = make_float3(spheres[q].c.x, spheres[q].c.y, spheres[q].c.z);
     float g = gradD[q];
+    // u = (x - p) / |x - p|: the unit gradient of the distance, normalised by the
+    // length of the difference actually formed so that |u| = 1 to rounding
     float3 u = make_float3(0.f, 0.f, 0.f);
-    bool valid = r.index < nPrims && r.d > 0.0f && g == g;
-    if (valid) u = (x - r.p) / r.d;
+    float3 diff = x - r.p;
+    float len = len3(diff);
+    bool valid = r.index < nPrims && r.d > 0.0f && len > 0.0f && g == g;
+    if (valid) u = diff / len;
     gradX[dim * q] = valid ? g * u.x : 0.0f;
     gradX[dim * q + 1] = valid ? g * u.y : 0.0f;
     if (dim == 3) gradX[dim * q + 2] = valid ? g * u.z : 0.0f;

@@ -206,7 +206,7 @@ def test_optimisation_with_gpu_refit_reduces_loss_and_stays_consistent():
         loss = (d * d).mean()
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     assert losses[-1] < losses[0]
     # after the last refit the GPU tree answers like a host tree built on the moved vertices
     vnow = verts.detach().cpu().numpy()
