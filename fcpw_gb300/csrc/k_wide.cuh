@@ -104,10 +104,26 @@ template<int W, int BITS> struct WideNodeRegs {
     FCPWGB_D float bound(int k, int c) const {
         if (BITS == 32) return __uint_as_float(w[(L::kBounds >> 2) + k * W + c]);
         int a = k % 3;
+        return __fmaf_rn(qvalue(k, c), scale(a), origin(a));
+    }
+    // the quantised integer of bound k of child c as a float: q < 2^23 placed in
+    // the mantissa of 2^23 and the bias subtracted (exact, full-rate ALU ops)
+    FCPWGB_D float qvalue(int k, int c) const {
         uint32_t q = BITS == 16 ? halfAt(L::kBounds + 2 * (k * W + c)) : byteAt(L::kBounds + k * W + c);
-        return __fmaf_rn((float)q, scale(a), origin(a));
+        return __uint_as_float(0x4b000000u | q) - 8388608.0f;
     }
 };
+
+// Squared min/max distances from query c to the W children of a node, on the
+// dequantised boxes fmaf(q, 2^e, origin) — the exact values the quantiser
+// checked to contain each child.
+template<int W, int BITS>
+FCPWGB_D void childDistances(const WideNodeRegs<W, BITS> &node, float3 c, float (&d2Min)[W], float (&d2Max)[W]) {
+#pragma unroll
+    for (int k = 0; k < W; k++)
+        boxSphereDist(make_float3(node.bound(0, k), node.bound(1, k), node.bound(2, k)),
+                      make_float3(node.bound(3, k), node.bound(4, k), node.bound(5, k)), c, d2Min[k], d2Max[k]);
+}
 
 constexpr uint32_t kLeafBit = 0x80000000u;
 FCPWGB_D uint32_t packLeaf(uint32_t off, uint32_t cnt) { return kLeafBit | (cnt << 27) | off; }
@@ -152,14 +168,14 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
             node.load(nodes, cur);
             nExpanded++;
             constexpr uint32_t kSlotMask = W - 1;
-            float d2Min[W];
+            float d2Min[W], d2Max[W];
+            childDistances<W, BITS>(node, c, d2Min, d2Max);
+            // a child's far distance bounds the answer; once a primitive has been
+            // found r2 is a primitive distance and far distances rarely improve it
+            if (!found) {
 #pragma unroll
-            for (int k = 0; k < W; k++) {
-                float lo0 = node.bound(0, k), lo1 = node.bound(1, k), lo2 = node.bound(2, k);
-                float hi0 = node.bound(3, k), hi1 = node.bound(4, k), hi2 = node.bound(5, k);
-                float d2Max;
-                boxSphereDist(make_float3(lo0, lo1, lo2), make_float3(hi0, hi1, hi2), c, d2Min[k], d2Max);
-                if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, d2Max);
+                for (int k = 0; k < W; k++)
+                    if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, d2Max[k]);
             }
             // keys: distance bits with the slot in the low bits, truncating the
             // distance downwards (visits are decided on d2Min <= r2, so a smaller
