@@ -303,6 +303,182 @@ __global__ void __launch_bounds__(128, 8) kWideClosestPoint(const unsigned char 
     }
 }
 
+// Persistent variant with per-lane refill. The traversal advances in steps
+// (one node expansion or one leaf per step) in lockstep across the warp; a
+// lane whose query is finished takes the next query at once instead of idling
+// until the slowest query of its warp ends. Refills come from a warp-private
+// pool of kPool consecutive (sorted) queries, itself refilled from the global
+// work counter by one atomic per kPool queries, so lanes keep working on
+// neighbouring queries.
+template<int W, int BITS, class Prim, bool PRECISE>
+__global__ void __launch_bounds__(128, 8) kWideClosestPointRefill(const unsigned char *__restrict__ nodes,
+                                                                  const unsigned char *__restrict__ prims,
+                                                                  const DevSphere *__restrict__ spheres,
+                                                                  const uint32_t *__restrict__ perm,
+                                                                  DevInteraction *__restrict__ out, uint32_t n,
+                                                                  int recordNormal, uint32_t *counter,
+                                                                  uint32_t *errorWord, unsigned long long *stats) {
+    constexpr uint32_t kPool = 256;
+    constexpr uint32_t kNone = 0xffffffffu;
+    constexpr uint32_t kSlotMask = W - 1;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lanesBelow = (1u << lane) - 1u;
+    uint32_t stRef[kWideStack];
+    float stD[kWideStack];
+    uint32_t poolNext = 0, poolEnd = 0;  // warp-uniform
+    bool exhausted = false;
+
+    uint32_t q = kNone, cur = 0, selected = kUintMax;
+    int sp = 0;
+    float3 c = make_float3(0.f, 0.f, 0.f);
+    float r2 = 0.0f;
+    bool found = false;
+    DevInteraction best = defaultInteraction();
+    uint32_t tExp = 0, tTests = 0;
+    WideNodeRegs<W, BITS> node;
+
+    for (;;) {
+        // ---- refill idle lanes: first from the warp's current range, then from a
+        // freshly fetched range (all control flow here is warp-uniform)
+        uint32_t idle = __ballot_sync(0xffffffffu, q == kNone);
+        for (int phase = 0; phase < 2 && idle != 0 && !exhausted; phase++) {
+            if (poolNext >= poolEnd) {
+                uint32_t b = 0;
+                if (lane == 0) b = atomicAdd(counter, kPool);
+                b = __shfl_sync(0xffffffffu, b, 0);
+                if (b >= n) {
+                    exhausted = true;
+                    break;
+                }
+                poolNext = b;
+                poolEnd = min(b + kPool, n);
+            }
+            uint32_t take = min((uint32_t)__popc(idle), poolEnd - poolNext);
+            uint32_t rank = __popc(idle & lanesBelow);
+            if (q == kNone && rank < take) {
+                q = poolNext + rank;
+                float4 s4 = ldg4(spheres + q);
+                c = make_float3(s4.x, s4.y, s4.z);
+                r2 = s4.w;
+                cur = 0;
+                sp = 0;
+                found = false;
+                selected = kUintMax;
+                best = defaultInteraction();
+            }
+            poolNext += take;
+            idle = __ballot_sync(0xffffffffu, q == kNone);
+        }
+        if (__ballot_sync(0xffffffffu, q != kNone) == 0) break;
+
+        if (q != kNone) {
+            bool pop = true;
+            if (!(cur & kLeafBit)) {
+                node.load(nodes, cur);
+                tExp++;
+                float d2Min[W], d2Max[W];
+                childDistances<W, BITS>(node, c, d2Min, d2Max);
+                if (!found) {
+#pragma unroll
+                    for (int k = 0; k < W; k++)
+                        if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, d2Max[k]);
+                }
+                uint32_t key[W];
+                int nh = 0;
+#pragma unroll
+                for (int k = 0; k < W; k++) {
+                    bool hit = node.cnt(k) != kWideEmpty && d2Min[k] <= r2;
+                    key[k] = hit ? ((__float_as_uint(d2Min[k]) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
+                    nh += hit ? 1 : 0;
+                }
+                sortNetwork<W>(key);
+                if (nh > 0) {
+                    if (sp + nh - 1 > kWideStack) {
+                        atomicOr(errorWord, kErrStackOverflow);
+                        nh = 0;
+                        sp = 0;
+                    }
+                }
+                if (nh > 0) {
+                    uint32_t firstRef = 0;
+#pragma unroll
+                    for (int k = W - 1; k >= 0; k--) {
+                        if (k < nh) {
+                            uint32_t slot = key[k] & kSlotMask, ref = 0, cntv = 0;
+#pragma unroll
+                            for (int s = 0; s < W; s++) {
+                                if (slot == (uint32_t)s) {
+                                    ref = node.ref(s);
+                                    cntv = node.cnt(s);
+                                }
+                            }
+                            uint32_t packed = cntv == 0 ? ref : packLeaf(ref, cntv);
+                            if (k == 0) {
+                                firstRef = packed;
+                            } else {
+                                stRef[sp] = packed;
+                                stD[sp] = __uint_as_float(key[k] & ~kSlotMask);
+                                sp++;
+                            }
+                        }
+                    }
+                    cur = firstRef;
+                    pop = false;
+                }
+            } else {
+                uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+                tTests += cnt;
+                for (uint32_t p = 0; p < cnt; p++) {
+                    Prim prim = Prim::load(prims, off + p);
+                    float3 pt;
+                    float2 uv;
+                    float d = prim.closestPoint(c, pt, uv);
+                    if (d * d <= r2) {
+                        r2 = fminf(r2, d * d);
+                        best.p = pt;
+                        best.n = make_float3(0.f, 0.f, 0.f);
+                        best.uv = uv;
+                        best.d = d;
+                        best.index = prim.index;
+                        selected = off + p;
+                        found = true;
+                    }
+                }
+            }
+            if (pop) {
+                bool next = false;
+                while (sp > 0) {
+                    sp--;
+                    if (stD[sp] <= r2) {
+                        cur = stRef[sp];
+                        next = true;
+                        break;
+                    }
+                }
+                if (!next) {
+                    // query finished: final record, then the lane becomes idle
+                    if (found) {
+                        Prim prim = Prim::load(prims, selected);
+                        if (PRECISE) {
+                            float3 p;
+                            double d = prim.refine(c, p);
+                            best.d = (float)d;
+                            best.p = p;
+                        }
+                        if (recordNormal) best.n = prim.normal();
+                    }
+                    out[perm ? __ldg(perm + q) : q] = best;
+                    q = kNone;
+                }
+            }
+        }
+    }
+    if (stats) {
+        atomicAdd(stats + 1, (unsigned long long)tExp);
+        atomicAdd(stats + 2, (unsigned long long)tTests);
+    }
+}
+
 // Re-quantises every wide node from the (refit) binary boxes behind its slots.
 template<int W, int BITS>
 __global__ void kRequantize(unsigned char *wideNodes, const int32_t *childBinary, const unsigned char *binNodes,
@@ -344,14 +520,15 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
             kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.out, l.n, l.recordNormal, l.counter,       \
                                  l.errorWord, l.stats);                                                            \
         };                                                                                                         \
+        const bool rf = l.counter != nullptr;                                                                      \
         if (dim == 3) {                                                                                            \
-            if (bits == 8) { if (precise) go(kWideClosestPoint<W, 8, Tri48Prim, true>); else go(kWideClosestPoint<W, 8, Tri48Prim, false>); } \
-            else if (bits == 16) { if (precise) go(kWideClosestPoint<W, 16, Tri48Prim, true>); else go(kWideClosestPoint<W, 16, Tri48Prim, false>); } \
-            else { if (precise) go(kWideClosestPoint<W, 32, Tri48Prim, true>); else go(kWideClosestPoint<W, 32, Tri48Prim, false>); } \
+            if (bits == 8) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 8, Tri48Prim, true>); else go(kWideClosestPoint<W, 8, Tri48Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 8, Tri48Prim, false>); else go(kWideClosestPoint<W, 8, Tri48Prim, false>); } } \
+            else if (bits == 16) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 16, Tri48Prim, true>); else go(kWideClosestPoint<W, 16, Tri48Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 16, Tri48Prim, false>); else go(kWideClosestPoint<W, 16, Tri48Prim, false>); } } \
+            else { if (precise) { if (rf) go(kWideClosestPointRefill<W, 32, Tri48Prim, true>); else go(kWideClosestPoint<W, 32, Tri48Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 32, Tri48Prim, false>); else go(kWideClosestPoint<W, 32, Tri48Prim, false>); } } \
         } else {                                                                                                   \
-            if (bits == 8) { if (precise) go(kWideClosestPoint<W, 8, Seg24Prim, true>); else go(kWideClosestPoint<W, 8, Seg24Prim, false>); } \
-            else if (bits == 16) { if (precise) go(kWideClosestPoint<W, 16, Seg24Prim, true>); else go(kWideClosestPoint<W, 16, Seg24Prim, false>); } \
-            else { if (precise) go(kWideClosestPoint<W, 32, Seg24Prim, true>); else go(kWideClosestPoint<W, 32, Seg24Prim, false>); } \
+            if (bits == 8) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 8, Seg24Prim, true>); else go(kWideClosestPoint<W, 8, Seg24Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 8, Seg24Prim, false>); else go(kWideClosestPoint<W, 8, Seg24Prim, false>); } } \
+            else if (bits == 16) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 16, Seg24Prim, true>); else go(kWideClosestPoint<W, 16, Seg24Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 16, Seg24Prim, false>); else go(kWideClosestPoint<W, 16, Seg24Prim, false>); } } \
+            else { if (precise) { if (rf) go(kWideClosestPointRefill<W, 32, Seg24Prim, true>); else go(kWideClosestPoint<W, 32, Seg24Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 32, Seg24Prim, false>); else go(kWideClosestPoint<W, 32, Seg24Prim, false>); } } \
         }                                                                                                          \
         return cudaGetLastError();                                                                                 \
     }                                                                                                              \
