@@ -33,6 +33,7 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_transfer_cpu_bvh": (c_int, [P, P]),
     "fcpwgb_gpu_scene_refit": (c_int, [P, P, P]),
     "fcpwgb_gpu_scene_update_vertices_device": (c_int, [P, P, c_uint32, P]),
+    "fcpwgb_gpu_scene_update_vertices_device_static": (c_int, [P, P, c_uint32, P]),
     "fcpwgb_find_closest_points": (c_int, [P, P, P, c_uint32, c_int]),
     "fcpwgb_intersect_rays": (c_int, [P, P, P, c_uint32, c_int]),
     "fcpwgb_intersect_spheres": (c_int, [P, P, P, P, c_uint32]),

@@ -190,6 +190,18 @@ int fcpwgb_gpu_scene_refit(fcpwgb_gpu_scene *scene, const void *primitives,
  * tree refit; asynchronous on stream (a cudaStream_t; NULL is the CUDA default stream). */
 int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *scene, const float *positions,
                                             uint32_t n_vertices, void *stream);
+/* No counterpart in the reference. The same update + refit as
+ * fcpwgb_gpu_scene_update_vertices_device for callers that may not allocate
+ * device memory: the call performs no cudaMalloc/cudaFree and no other
+ * allocation; the refit's per-node arrival counters live in a static device
+ * array of 2^20 32-bit words (4 MiB, held on every GPU that loads the library
+ * until the process exits). Trees with more than 1,048,576 nodes are rejected
+ * with FCPWGB_ERR_INVALID_ARGUMENT. Each call clears the counters it uses;
+ * the array is shared by all calls on a device, so calls that overlap on the
+ * GPU (other streams, scenes or threads) race and must be ordered by the
+ * caller. Asynchronous on stream (NULL is the CUDA default stream). */
+int fcpwgb_gpu_scene_update_vertices_device_static(fcpwgb_gpu_scene *scene, const float *positions,
+                                                   uint32_t n_vertices, void *stream);
 
 /* Traversal variant used by the closest point entry points of a scene. With
  * branching 0 the transferred binary tree is traversed in the reference GPU
