@@ -51,6 +51,19 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_set_traversal": (c_int, [P, P]),
     "fcpwgb_gpu_scene_get_traversal": (c_int, [P, P]),
     "fcpwgb_gpu_scene_check_errors": (c_int, [P, C.POINTER(c_uint32)]),
+    "fcpwgb_closest_distances_f64_device": (c_int, [P, P, c_uint32, P, P]),
+    "fcpwgb_gpu_batch_create": (c_int, [c_int, c_int, C.POINTER(c_void_p)]),
+    "fcpwgb_gpu_batch_destroy": (None, [P]),
+    "fcpwgb_gpu_batch_set_scenes": (c_int, [P, P, c_uint32]),
+    "fcpwgb_gpu_batch_set_traversal": (c_int, [P, P]),
+    "fcpwgb_gpu_batch_get_traversal": (c_int, [P, P]),
+    "fcpwgb_gpu_batch_use_graph": (c_int, [P, c_int]),
+    "fcpwgb_gpu_batch_find_closest_points_device": (c_int, [P, P, P, c_uint32, P, c_int, P]),
+    "fcpwgb_gpu_batch_find_closest_points": (c_int, [P, P, P, c_uint32, P, c_int]),
+    "fcpwgb_gpu_batch_traversal_stats": (c_int, [P, P, P, c_uint32, P, P]),
+    "fcpwgb_gpu_batch_info": (c_int, [P, C.POINTER(c_uint32), C.POINTER(c_uint32), C.POINTER(c_uint32),
+                                      C.POINTER(c_uint32)]),
+    "fcpwgb_gpu_batch_check_errors": (c_int, [P, C.POINTER(c_uint32)]),
 }
 
 

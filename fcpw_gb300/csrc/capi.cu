@@ -52,9 +52,29 @@ extern "C" int fcpwgb_device_count(void) {
 }
 
 // ----------------------------------------------------------- CPU producer
-struct fcpwgb_cpu_bvh {
-    std::unique_ptr<HostBvh> bvh;
-};
+namespace fcpwgb {
+void binaryTreeArrays(const HostBvh &h, std::vector<uint32_t> &nP, std::vector<uint32_t> &off,
+                      std::vector<float> &boxes) {
+    uint32_t n = h.nNodes();
+    bool snch = h.hasSilhouettes();
+    std::vector<unsigned char> raw((size_t)n * (snch ? sizeof(fcpwgb_snch_node) : sizeof(fcpwgb_bvh_node)));
+    h.exportNodes(raw.data());
+    nP.resize(n);
+    off.resize(n);
+    boxes.resize((size_t)n * 6);
+    for (uint32_t i = 0; i < n; i++) {
+        const fcpwgb_bounding_box *bx;
+        if (snch) {
+            const fcpwgb_snch_node &nd = ((const fcpwgb_snch_node *)raw.data())[i];
+            bx = &nd.box; nP[i] = nd.nPrimitives; off[i] = nd.offset;
+        } else {
+            const fcpwgb_bvh_node &nd = ((const fcpwgb_bvh_node *)raw.data())[i];
+            bx = &nd.box; nP[i] = nd.nPrimitives; off[i] = nd.offset;
+        }
+        std::memcpy(&boxes[(size_t)i * 6], bx, 24);
+    }
+}
+}  // namespace fcpwgb
 
 extern "C" int fcpwgb_cpu_bvh_build(int dim, const float *positions, uint32_t n_vertices, const int32_t *indices,
                                     uint32_t n_primitives, int aggregate_type, int with_silhouettes,
@@ -117,24 +137,9 @@ extern "C" int fcpwgb_cpu_bvh_export_topology(const fcpwgb_cpu_bvh *b, int32_t *
 extern "C" int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *b, int branching, int bits, void *nodes,
                                           int32_t *child_binary, uint32_t *n_nodes, uint32_t *node_bytes) {
     if (!b || !n_nodes || !node_bytes) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
-    const HostBvh &h = *b->bvh;
-    uint32_t n = h.nNodes();
-    bool snch = h.hasSilhouettes();
-    std::vector<unsigned char> raw((size_t)n * (snch ? sizeof(fcpwgb_snch_node) : sizeof(fcpwgb_bvh_node)));
-    h.exportNodes(raw.data());
-    std::vector<uint32_t> nP(n), off(n);
-    std::vector<float> boxes((size_t)n * 6);
-    for (uint32_t i = 0; i < n; i++) {
-        const fcpwgb_bounding_box *bx;
-        if (snch) {
-            const fcpwgb_snch_node &nd = ((const fcpwgb_snch_node *)raw.data())[i];
-            bx = &nd.box; nP[i] = nd.nPrimitives; off[i] = nd.offset;
-        } else {
-            const fcpwgb_bvh_node &nd = ((const fcpwgb_bvh_node *)raw.data())[i];
-            bx = &nd.box; nP[i] = nd.nPrimitives; off[i] = nd.offset;
-        }
-        std::memcpy(&boxes[(size_t)i * 6], bx, 24);
-    }
+    std::vector<uint32_t> nP, off;
+    std::vector<float> boxes;
+    binaryTreeArrays(*b->bvh, nP, off, boxes);
     WideHost w;
     if (!(branching == 2 || branching == 4 || branching == 8) || !(bits == 8 || bits == 16 || bits == 32))
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "branching must be 2/4/8 and bits 8/16/32");
@@ -803,5 +808,16 @@ extern "C" int fcpwgb_gpu_scene_check_errors(fcpwgb_gpu_scene *s, uint32_t *erro
     FCPWGB_CUDA(cudaMemsetAsync(s->errorWord.ptr, 0, sizeof(err), s->stream));
     FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
     if (error_word) *error_word = err[0];
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_closest_distances_f64_device(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                   uint32_t n, double *distances, void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > (1u << 24)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "at most 2^24 queries per brute-force call");
+    if (n && (!spheres || !distances)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL array");
+    FCPWGB_CUDA(launchBruteF64(s->dim, (const unsigned char *)s->prims.ptr, s->nPrims, (const DevSphere *)spheres, n,
+                               distances, s->pick(stream)));
     return FCPWGB_OK;
 }

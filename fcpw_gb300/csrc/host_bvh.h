@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -109,4 +110,15 @@ private:
     std::vector<int> silRefs_;            // silhouette references in leaf order -> slot
 };
 
+}  // namespace fcpwgb
+
+// the object behind the C ABI's fcpwgb_cpu_bvh handle
+struct fcpwgb_cpu_bvh {
+    std::unique_ptr<fcpwgb::HostBvh> bvh;
+};
+
+namespace fcpwgb {
+// per-node primitive count, offset and box (pMin, pMax) of the flattened binary tree
+void binaryTreeArrays(const HostBvh &h, std::vector<uint32_t> &nP, std::vector<uint32_t> &off,
+                      std::vector<float> &boxes);
 }  // namespace fcpwgb

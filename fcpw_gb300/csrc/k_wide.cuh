@@ -3,6 +3,8 @@
 // branching factor in k_wide_w{2,4,8}.cu.
 #pragma once
 
+#include <type_traits>
+
 #include "kernels.h"
 #include "wide_common.cuh"
 
@@ -106,23 +108,43 @@ template<int W, int BITS> struct WideNodeRegs {
         int a = k % 3;
         return __fmaf_rn(qvalue(k, c), scale(a), origin(a));
     }
-    // the quantised integer of bound k of child c as a float: q < 2^23 placed in
-    // the mantissa of 2^23 and the bias subtracted (exact, full-rate ALU ops)
+    // the quantised integer of bound k of child c as a float: one byte permute
+    // places q (< 2^16) in the low mantissa bits of 2^23, then the bias is
+    // subtracted (exact)
     FCPWGB_D float qvalue(int k, int c) const {
-        uint32_t q = BITS == 16 ? halfAt(L::kBounds + 2 * (k * W + c)) : byteAt(L::kBounds + k * W + c);
-        return __uint_as_float(0x4b000000u | q) - 8388608.0f;
+        const int off = BITS == 16 ? L::kBounds + 2 * (k * W + c) : L::kBounds + k * W + c;
+        const uint32_t b = (uint32_t)(off & 3);
+        const uint32_t sel = BITS == 16 ? (0x7400u | ((b + 1u) << 4) | b) : (0x7440u | b);
+        return __uint_as_float(__byte_perm(w[off >> 2], 0x4b000000u, sel)) - 8388608.0f;
     }
 };
 
-// Squared min/max distances from query c to the W children of a node, on the
-// dequantised boxes fmaf(q, 2^e, origin) — the exact values the quantiser
-// checked to contain each child.
+// Squared min distances from query c to the W children of a node, and the
+// squared max distance to child k, on the dequantised boxes
+// fmaf(q, 2^e, origin) -- the exact values the quantiser checked to contain
+// each child.
+FCPWGB_D float fmax3(float a, float b, float c) {  // three-input max (sm_100+)
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
 template<int W, int BITS>
-FCPWGB_D void childDistances(const WideNodeRegs<W, BITS> &node, float3 c, float (&d2Min)[W], float (&d2Max)[W]) {
+FCPWGB_D void childD2Min(const WideNodeRegs<W, BITS> &node, float3 c, float (&d2Min)[W]) {
 #pragma unroll
-    for (int k = 0; k < W; k++)
-        boxSphereDist(make_float3(node.bound(0, k), node.bound(1, k), node.bound(2, k)),
-                      make_float3(node.bound(3, k), node.bound(4, k), node.bound(5, k)), c, d2Min[k], d2Max[k]);
+    for (int k = 0; k < W; k++) {
+        // boxSphereD2Min with the per-axis max(lo - c, c - hi, 0) in one instruction
+        float ax = fmax3(node.bound(0, k) - c.x, c.x - node.bound(3, k), 0.0f);
+        float ay = fmax3(node.bound(1, k) - c.y, c.y - node.bound(4, k), 0.0f);
+        float az = fmax3(node.bound(2, k) - c.z, c.z - node.bound(5, k), 0.0f);
+        d2Min[k] = ax * ax + ay * ay + az * az;
+    }
+}
+template<int W, int BITS>
+FCPWGB_D float childD2Max(const WideNodeRegs<W, BITS> &node, float3 c, int k) {
+    float lo, hi;
+    boxSphereDist(make_float3(node.bound(0, k), node.bound(1, k), node.bound(2, k)),
+                  make_float3(node.bound(3, k), node.bound(4, k), node.bound(5, k)), c, lo, hi);
+    return hi;
 }
 
 constexpr uint32_t kLeafBit = 0x80000000u;
@@ -150,32 +172,58 @@ template<> FCPWGB_D void sortNetwork<8>(uint32_t (&k)[8]) {
     cmpx(k[1], k[2]); cmpx(k[3], k[4]); cmpx(k[5], k[6]);
 }
 
+// Per-thread traversal stack of kWideStack entries (node reference + the
+// child's distance bound). The first kShortStack entries live in shared
+// memory, entry k of thread t at [k * 128 + t] so that a warp's accesses fall
+// in distinct banks; deeper entries go to local memory, which only deep
+// traversals touch. A whole stack in local memory (1 KB per thread) does not
+// fit the L1 of a fully occupied SM and its pushes and pops reach L2 and DRAM.
+constexpr int kShortStack = 16;
+constexpr int kWideBlock = 128;  // threads per block of the wide kernels
+struct WideStack {
+    uint32_t *sRef;  // shared, stride kWideBlock
+    float *sD;
+    uint32_t lRef[kWideStack - kShortStack];
+    float lD[kWideStack - kShortStack];
+    FCPWGB_D void push(int sp, uint32_t ref, float d) {
+        if (sp < kShortStack) {
+            sRef[sp * kWideBlock] = ref;
+            sD[sp * kWideBlock] = d;
+        } else {
+            lRef[sp - kShortStack] = ref;
+            lD[sp - kShortStack] = d;
+        }
+    }
+    FCPWGB_D float dist(int sp) const { return sp < kShortStack ? sD[sp * kWideBlock] : lD[sp - kShortStack]; }
+    FCPWGB_D uint32_t ref(int sp) const { return sp < kShortStack ? sRef[sp * kWideBlock] : lRef[sp - kShortStack]; }
+};
+
 // Closest point of one query on a wide tree (bvh.slang:395-502 semantics:
 // inclusive d2Min <= r2 pruning, r2 shrunk by child d2Max, primitives accepted
 // when d*d <= r2, the later of equal distances wins).
+// `root` is the tree's root record (always an inner record); `found`/`best`/
+// `selected`/`r2` may arrive holding a candidate already tested (a seed).
 template<int W, int BITS, class Prim>
 FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigned char *__restrict__ prims,
-                          float3 c, float r2, DevInteraction &best, uint32_t &selected, uint32_t *errorWord,
-                          uint32_t &nExpanded, uint32_t &nTests) {
-    uint32_t stRef[kWideStack];
-    float stD[kWideStack];
+                          uint32_t root, float3 c, float r2, bool found, DevInteraction &best, uint32_t &selected,
+                          WideStack &st, uint32_t *errorWord, uint32_t &nExpanded, uint32_t &nTests) {
     int sp = 0;
-    uint32_t cur = 0;  // wide node 0 (always an inner record)
-    bool found = false;
+    uint32_t cur = root;
     WideNodeRegs<W, BITS> node;
     for (;;) {
         if (!(cur & kLeafBit)) {
             node.load(nodes, cur);
             nExpanded++;
             constexpr uint32_t kSlotMask = W - 1;
-            float d2Min[W], d2Max[W];
-            childDistances<W, BITS>(node, c, d2Min, d2Max);
+            float d2Min[W];
+            childD2Min<W, BITS>(node, c, d2Min);
             // a child's far distance bounds the answer; once a primitive has been
-            // found r2 is a primitive distance and far distances rarely improve it
+            // found r2 is a primitive distance and far distances rarely improve
+            // it, so they are computed only before the first hit
             if (!found) {
 #pragma unroll
                 for (int k = 0; k < W; k++)
-                    if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, d2Max[k]);
+                    if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
             }
             // keys: distance bits with the slot in the low bits, truncating the
             // distance downwards (visits are decided on d2Min <= r2, so a smaller
@@ -210,8 +258,7 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
                         if (k == 0) {
                             firstRef = packed;
                         } else {
-                            stRef[sp] = packed;
-                            stD[sp] = __uint_as_float(key[k] & ~kSlotMask);
+                            st.push(sp, packed, __uint_as_float(key[k] & ~kSlotMask));
                             sp++;
                         }
                     }
@@ -242,8 +289,8 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
         bool next = false;
         while (sp > 0) {
             sp--;
-            if (stD[sp] <= r2) {
-                cur = stRef[sp];
+            if (st.dist(sp) <= r2) {
+                cur = st.ref(sp);
                 next = true;
                 break;
             }
@@ -253,223 +300,102 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
     return found;
 }
 
-// One thread per query; with `counter` non-NULL blocks are persistent and
-// warps fetch 32-query chunks from it; with `perm` non-NULL the queries are
-// read in sorted order and results scattered back to out[perm[i]]; with
-// `stats` non-NULL expansions and primitive tests are summed into stats[1..2].
-template<int W, int BITS, class Prim, bool PRECISE>
-__global__ void __launch_bounds__(128, 8) kWideClosestPoint(const unsigned char *__restrict__ nodes,
-                                                         const unsigned char *__restrict__ prims,
-                                                         const DevSphere *__restrict__ spheres,
-                                                         const uint32_t *__restrict__ perm,
-                                                         DevInteraction *__restrict__ out, uint32_t n,
-                                                         int recordNormal, uint32_t *counter, uint32_t *errorWord,
-                                                         unsigned long long *stats) {
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
-    uint32_t tExp = 0, tTests = 0;
-    for (;;) {
-        if (counter) {
-            uint32_t b = 0;
-            if (lane == 0) b = atomicAdd(counter, 32u);
-            base = __shfl_sync(0xffffffffu, b, 0);
+// Final record of query i: FP64 distance of the winning primitive (PRECISE),
+// its face normal (recordNormal), written to the caller's slot.
+template<class Prim, bool PRECISE>
+FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_t *__restrict__ perm,
+                          DevInteraction *__restrict__ out, uint32_t i, float3 c, bool found, uint32_t selected,
+                          int recordNormal, DevInteraction &best) {
+    if (found) {
+        Prim prim = Prim::load(prims, selected);
+        if (PRECISE) {
+            float3 p;
+            double d = prim.refine(c, p);
+            best.d = (float)d;
+            best.p = p;
         }
-        if (base >= n) break;
-        uint32_t i = base + lane;
+        if (recordNormal) best.n = prim.normal();
+    }
+    out[perm ? __ldg(perm + i) : i] = best;
+}
+
+// One thread per query. With `perm` non-NULL the queries are read in sorted
+// order and results scattered back to out[perm[i]]; with `roots` non-NULL
+// query i starts at wide record roots[i] (a forest of trees), else at 0; with
+// `stats` non-NULL expansions and primitive tests are summed into stats[1..2].
+// With `counter` non-NULL the blocks are persistent: a warp takes kWidePool
+// consecutive (sorted, so neighbouring) queries at a time from the counter and
+// walks them in rounds of 32, and a lane's previous winner -- a primitive
+// near its next query -- is tested first, so that query starts with a tight
+// radius instead of FLT_MAX. Any tested primitive is a valid candidate, so the
+// result is the same closest distance (ties may pick another primitive).
+constexpr uint32_t kWidePool = 256;
+template<int W, int BITS, class Prim, bool PRECISE, bool PERSISTENT>
+__global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigned char *__restrict__ nodes,
+                                                                const unsigned char *__restrict__ prims,
+                                                                const DevSphere *__restrict__ spheres,
+                                                                const uint32_t *__restrict__ perm,
+                                                                const uint32_t *__restrict__ roots,
+                                                                DevInteraction *__restrict__ out, uint32_t n,
+                                                                int recordNormal, uint32_t *counter,
+                                                                uint32_t *errorWord, unsigned long long *stats) {
+    __shared__ uint32_t sRef[kShortStack * kWideBlock];
+    __shared__ float sD[kShortStack * kWideBlock];
+    WideStack st;
+    st.sRef = sRef + threadIdx.x;
+    st.sD = sD + threadIdx.x;
+    uint32_t tExp = 0, tTests = 0;
+    if (!PERSISTENT) {
+        uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
         if (i < n) {
             float4 s4 = ldg4(spheres + i);
             float3 c = make_float3(s4.x, s4.y, s4.z);
             DevInteraction best = defaultInteraction();
             uint32_t selected = kUintMax;
-            bool found = wideClosest<W, BITS, Prim>(nodes, prims, c, s4.w, best, selected, errorWord, tExp, tTests);
-            if (found) {
-                Prim prim = Prim::load(prims, selected);
-                if (PRECISE) {
-                    float3 p;
-                    double d = prim.refine(c, p);
-                    best.d = (float)d;
-                    best.p = p;
-                }
-                if (recordNormal) best.n = prim.normal();
-            }
-            out[perm ? __ldg(perm + i) : i] = best;
+            uint32_t root = roots ? __ldg(roots + i) : 0u;
+            bool found = wideClosest<W, BITS, Prim>(nodes, prims, root, c, s4.w, false, best, selected, st, errorWord,
+                                                    tExp, tTests);
+            finishQuery<Prim, PRECISE>(prims, perm, out, i, c, found, selected, recordNormal, best);
         }
-        if (!counter) break;
-        __syncwarp();
-    }
-    if (stats) {
-        atomicAdd(stats + 1, (unsigned long long)tExp);
-        atomicAdd(stats + 2, (unsigned long long)tTests);
-    }
-}
-
-// Persistent variant with per-lane refill. The traversal advances in steps
-// (one node expansion or one leaf per step) in lockstep across the warp; a
-// lane whose query is finished takes the next query at once instead of idling
-// until the slowest query of its warp ends. Refills come from a warp-private
-// pool of kPool consecutive (sorted) queries, itself refilled from the global
-// work counter by one atomic per kPool queries, so lanes keep working on
-// neighbouring queries.
-template<int W, int BITS, class Prim, bool PRECISE>
-__global__ void __launch_bounds__(128, 8) kWideClosestPointRefill(const unsigned char *__restrict__ nodes,
-                                                                  const unsigned char *__restrict__ prims,
-                                                                  const DevSphere *__restrict__ spheres,
-                                                                  const uint32_t *__restrict__ perm,
-                                                                  DevInteraction *__restrict__ out, uint32_t n,
-                                                                  int recordNormal, uint32_t *counter,
-                                                                  uint32_t *errorWord, unsigned long long *stats) {
-    constexpr uint32_t kPool = 256;
-    constexpr uint32_t kNone = 0xffffffffu;
-    constexpr uint32_t kSlotMask = W - 1;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t lanesBelow = (1u << lane) - 1u;
-    uint32_t stRef[kWideStack];
-    float stD[kWideStack];
-    uint32_t poolNext = 0, poolEnd = 0;  // warp-uniform
-    bool exhausted = false;
-
-    uint32_t q = kNone, cur = 0, selected = kUintMax;
-    int sp = 0;
-    float3 c = make_float3(0.f, 0.f, 0.f);
-    float r2 = 0.0f;
-    bool found = false;
-    DevInteraction best = defaultInteraction();
-    uint32_t tExp = 0, tTests = 0;
-    WideNodeRegs<W, BITS> node;
-
-    for (;;) {
-        // ---- refill idle lanes: first from the warp's current range, then from a
-        // freshly fetched range (all control flow here is warp-uniform)
-        uint32_t idle = __ballot_sync(0xffffffffu, q == kNone);
-        for (int phase = 0; phase < 2 && idle != 0 && !exhausted; phase++) {
-            if (poolNext >= poolEnd) {
-                uint32_t b = 0;
-                if (lane == 0) b = atomicAdd(counter, kPool);
-                b = __shfl_sync(0xffffffffu, b, 0);
-                if (b >= n) {
-                    exhausted = true;
-                    break;
-                }
-                poolNext = b;
-                poolEnd = min(b + kPool, n);
-            }
-            uint32_t take = min((uint32_t)__popc(idle), poolEnd - poolNext);
-            uint32_t rank = __popc(idle & lanesBelow);
-            if (q == kNone && rank < take) {
-                q = poolNext + rank;
-                float4 s4 = ldg4(spheres + q);
-                c = make_float3(s4.x, s4.y, s4.z);
-                r2 = s4.w;
-                cur = 0;
-                sp = 0;
-                found = false;
-                selected = kUintMax;
-                best = defaultInteraction();
-            }
-            poolNext += take;
-            idle = __ballot_sync(0xffffffffu, q == kNone);
-        }
-        if (__ballot_sync(0xffffffffu, q != kNone) == 0) break;
-
-        if (q != kNone) {
-            bool pop = true;
-            if (!(cur & kLeafBit)) {
-                node.load(nodes, cur);
-                tExp++;
-                float d2Min[W], d2Max[W];
-                childDistances<W, BITS>(node, c, d2Min, d2Max);
-                if (!found) {
-#pragma unroll
-                    for (int k = 0; k < W; k++)
-                        if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, d2Max[k]);
-                }
-                uint32_t key[W];
-                int nh = 0;
-#pragma unroll
-                for (int k = 0; k < W; k++) {
-                    bool hit = node.cnt(k) != kWideEmpty && d2Min[k] <= r2;
-                    key[k] = hit ? ((__float_as_uint(d2Min[k]) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
-                    nh += hit ? 1 : 0;
-                }
-                sortNetwork<W>(key);
-                if (nh > 0) {
-                    if (sp + nh - 1 > kWideStack) {
-                        atomicOr(errorWord, kErrStackOverflow);
-                        nh = 0;
-                        sp = 0;
-                    }
-                }
-                if (nh > 0) {
-                    uint32_t firstRef = 0;
-#pragma unroll
-                    for (int k = W - 1; k >= 0; k--) {
-                        if (k < nh) {
-                            uint32_t slot = key[k] & kSlotMask, ref = 0, cntv = 0;
-#pragma unroll
-                            for (int s = 0; s < W; s++) {
-                                if (slot == (uint32_t)s) {
-                                    ref = node.ref(s);
-                                    cntv = node.cnt(s);
-                                }
-                            }
-                            uint32_t packed = cntv == 0 ? ref : packLeaf(ref, cntv);
-                            if (k == 0) {
-                                firstRef = packed;
-                            } else {
-                                stRef[sp] = packed;
-                                stD[sp] = __uint_as_float(key[k] & ~kSlotMask);
-                                sp++;
-                            }
-                        }
-                    }
-                    cur = firstRef;
-                    pop = false;
-                }
-            } else {
-                uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
-                tTests += cnt;
-                for (uint32_t p = 0; p < cnt; p++) {
-                    Prim prim = Prim::load(prims, off + p);
+    } else {
+        const uint32_t lane = threadIdx.x & 31u;
+        for (;;) {
+            __syncwarp();
+            uint32_t b = 0;
+            if (lane == 0) b = atomicAdd(counter, kWidePool);
+            b = __shfl_sync(0xffffffffu, b, 0);
+            if (b >= n) break;
+            const uint32_t e = min(b + kWidePool, n);
+            uint32_t seed = kUintMax, seedRoot = kUintMax;
+            for (uint32_t i = b + lane; i < e; i += 32) {
+                float4 s4 = ldg4(spheres + i);
+                float3 c = make_float3(s4.x, s4.y, s4.z);
+                float r2 = s4.w;
+                DevInteraction best = defaultInteraction();
+                uint32_t selected = kUintMax;
+                uint32_t root = roots ? __ldg(roots + i) : 0u;
+                bool found = false;
+                if (seed != kUintMax && seedRoot == root) {
+                    Prim prim = Prim::load(prims, seed);
                     float3 pt;
                     float2 uv;
                     float d = prim.closestPoint(c, pt, uv);
+                    tTests++;
                     if (d * d <= r2) {
-                        r2 = fminf(r2, d * d);
+                        r2 = d * d;
                         best.p = pt;
-                        best.n = make_float3(0.f, 0.f, 0.f);
                         best.uv = uv;
                         best.d = d;
                         best.index = prim.index;
-                        selected = off + p;
+                        selected = seed;
                         found = true;
                     }
                 }
-            }
-            if (pop) {
-                bool next = false;
-                while (sp > 0) {
-                    sp--;
-                    if (stD[sp] <= r2) {
-                        cur = stRef[sp];
-                        next = true;
-                        break;
-                    }
-                }
-                if (!next) {
-                    // query finished: final record, then the lane becomes idle
-                    if (found) {
-                        Prim prim = Prim::load(prims, selected);
-                        if (PRECISE) {
-                            float3 p;
-                            double d = prim.refine(c, p);
-                            best.d = (float)d;
-                            best.p = p;
-                        }
-                        if (recordNormal) best.n = prim.normal();
-                    }
-                    out[perm ? __ldg(perm + q) : q] = best;
-                    q = kNone;
-                }
+                found = wideClosest<W, BITS, Prim>(nodes, prims, root, c, r2, found, best, selected, st, errorWord,
+                                                   tExp, tTests);
+                seed = found ? selected : kUintMax;
+                seedRoot = root;
+                finishQuery<Prim, PRECISE>(prims, perm, out, i, c, found, selected, recordNormal, best);
             }
         }
     }
@@ -517,19 +443,23 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
         dim3 g(l.grid), b(128);                                                                                    \
         _Pragma("nv_diag_suppress 177")                                                                            \
         auto go = [&](auto kern) {                                                                                 \
-            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.out, l.n, l.recordNormal, l.counter,       \
-                                 l.errorWord, l.stats);                                                            \
+            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal,         \
+                                 l.counter, l.errorWord, l.stats);                                                 \
         };                                                                                                         \
-        const bool rf = l.counter != nullptr;                                                                      \
-        if (dim == 3) {                                                                                            \
-            if (bits == 8) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 8, Tri48Prim, true>); else go(kWideClosestPoint<W, 8, Tri48Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 8, Tri48Prim, false>); else go(kWideClosestPoint<W, 8, Tri48Prim, false>); } } \
-            else if (bits == 16) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 16, Tri48Prim, true>); else go(kWideClosestPoint<W, 16, Tri48Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 16, Tri48Prim, false>); else go(kWideClosestPoint<W, 16, Tri48Prim, false>); } } \
-            else { if (precise) { if (rf) go(kWideClosestPointRefill<W, 32, Tri48Prim, true>); else go(kWideClosestPoint<W, 32, Tri48Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 32, Tri48Prim, false>); else go(kWideClosestPoint<W, 32, Tri48Prim, false>); } } \
-        } else {                                                                                                   \
-            if (bits == 8) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 8, Seg24Prim, true>); else go(kWideClosestPoint<W, 8, Seg24Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 8, Seg24Prim, false>); else go(kWideClosestPoint<W, 8, Seg24Prim, false>); } } \
-            else if (bits == 16) { if (precise) { if (rf) go(kWideClosestPointRefill<W, 16, Seg24Prim, true>); else go(kWideClosestPoint<W, 16, Seg24Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 16, Seg24Prim, false>); else go(kWideClosestPoint<W, 16, Seg24Prim, false>); } } \
-            else { if (precise) { if (rf) go(kWideClosestPointRefill<W, 32, Seg24Prim, true>); else go(kWideClosestPoint<W, 32, Seg24Prim, true>); } else { if (rf) go(kWideClosestPointRefill<W, 32, Seg24Prim, false>); else go(kWideClosestPoint<W, 32, Seg24Prim, false>); } } \
-        }                                                                                                          \
+        auto pick = [&](auto bitsConst) {                                                                          \
+            constexpr int B = decltype(bitsConst)::value;                                                          \
+            const bool p = l.counter != nullptr;                                                                   \
+            if (dim == 3) {                                                                                        \
+                if (precise) { if (p) go(kWideClosestPoint<W, B, Tri48Prim, true, true>); else go(kWideClosestPoint<W, B, Tri48Prim, true, false>); } \
+                else { if (p) go(kWideClosestPoint<W, B, Tri48Prim, false, true>); else go(kWideClosestPoint<W, B, Tri48Prim, false, false>); } \
+            } else {                                                                                               \
+                if (precise) { if (p) go(kWideClosestPoint<W, B, Seg24Prim, true, true>); else go(kWideClosestPoint<W, B, Seg24Prim, true, false>); } \
+                else { if (p) go(kWideClosestPoint<W, B, Seg24Prim, false, true>); else go(kWideClosestPoint<W, B, Seg24Prim, false, false>); } \
+            }                                                                                                      \
+        };                                                                                                         \
+        if (bits == 8) pick(std::integral_constant<int, 8>());                                                     \
+        else if (bits == 16) pick(std::integral_constant<int, 16>());                                              \
+        else pick(std::integral_constant<int, 32>());                                                              \
         return cudaGetLastError();                                                                                 \
     }                                                                                                              \
     template<> cudaError_t launchRequantizeT<W>(int bits, unsigned char *wideNodes, const int32_t *childBinary,    \

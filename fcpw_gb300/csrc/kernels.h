@@ -34,12 +34,17 @@ cudaError_t launchSilhouetteBinary(const SceneView &v, const DevSphere *spheres,
                                    cudaStream_t s);
 cudaError_t launchFillDefault(DevInteraction *out, uint32_t n, cudaStream_t s);
 
+// FP64 brute-force closest distance of every query over all primitives (k_check.cu)
+cudaError_t launchBruteF64(int dim, const unsigned char *prims, uint32_t nPrims, const DevSphere *spheres,
+                           uint32_t n, double *out, cudaStream_t s);
+
 // wide / quantised closest point (k_wide.cuh, k_wide_w{2,4,8}.cu)
 struct WideLaunch {
     const unsigned char *nodes = nullptr;  // wide node records
     const unsigned char *prims = nullptr;  // 48 B triangles (3D) or 24 B segments (2D)
     const DevSphere *spheres = nullptr;    // queries (sorted when perm is set)
     const uint32_t *perm = nullptr;        // sorted position -> caller query index, or NULL
+    const uint32_t *roots = nullptr;       // root record of every (sorted) query in a forest, or NULL (root 0)
     DevInteraction *out = nullptr;
     uint32_t n = 0;
     int recordNormal = 0;
@@ -49,16 +54,36 @@ struct WideLaunch {
     uint32_t grid = 0;
 };
 template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
+// dispatch over W = 2, 4, 8
+cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
 template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes, const int32_t *childBinary,
                                               const unsigned char *binNodes, int binStride, uint32_t nWide,
                                               uint32_t *errorWord, cudaStream_t s);
 
 // query reordering and record packing (k_sort.cu)
 constexpr uint32_t kSortCellBits = 18;  // 2^18 cells: 64^3 in 3D, 512^2 in 2D
-struct SortGrid { float3 lo; float3 invCell; int dim; };
-cudaError_t launchSortQueries(const SortGrid &g, const DevSphere *spheres, uint32_t n, uint32_t *cells,
-                              DevSphere *sorted, uint32_t *perm, cudaStream_t s);
+constexpr uint32_t kSortCells = 1u << kSortCellBits;
+// the sort grid spans the query bounds clipped to [lo, hi]
+struct SortLimits { float3 lo; float3 hi; int dim; };
+// cells: scratch of kSortScratchWords words (counters, query bounds, scan tile sums)
+constexpr uint32_t kSortScratchWords = kSortCells + 8 + kSortCells / 4096;
+cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, uint32_t n, uint32_t *cells,
+                              DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s);
 cudaError_t launchPackTri48(const DevTriangle *tris, uint32_t n, float4 *out, cudaStream_t s);
+
+// batches of scenes: per-scene sort grid (cells cellBase .. cellBase + 2^(dim*bits))
+struct BatchSceneGrid {
+    float3 lo, inv;     // grid origin and cells per unit length (2^bits / extent)
+    uint32_t cellBase;  // first cell of the scene in the concatenated cell array
+    uint32_t bits;      // cells per axis = 2^bits (<= 6 in 3D, <= 9 in 2D)
+    uint32_t root;      // wide record of the scene's root in the forest
+    uint32_t pad;
+};
+uint32_t batchScanTiles(uint32_t nCells);  // entries of the tileSums scratch
+cudaError_t launchSortBatchQueries(int dim, const BatchSceneGrid *grids, const uint32_t *offsets, uint32_t nScenes,
+                                   const DevSphere *spheres, uint32_t n, uint32_t *cells, uint32_t nCells,
+                                   uint32_t *tileSums, DevSphere *sorted, uint32_t *perm, uint32_t *roots,
+                                   cudaStream_t s);
 
 // backward of the differentiable queries (k_grad.cu)
 struct GradView {

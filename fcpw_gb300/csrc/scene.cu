@@ -7,7 +7,6 @@
 
 namespace fcpwgb {
 
-namespace {
 cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s) {
     switch (W) {
         case 2: return launchWideClosestT<2>(bits, dim, precise, l, s);
@@ -15,6 +14,8 @@ cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch 
         default: return launchWideClosestT<8>(bits, dim, precise, l, s);
     }
 }
+
+namespace {
 cudaError_t launchRequant(int W, int bits, unsigned char *wn, const int32_t *cb, const unsigned char *bn, int stride,
                           uint32_t n, uint32_t *err, cudaStream_t s) {
     switch (W) {
@@ -76,23 +77,19 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
     l.stats = stats;
     cudaError_t e;
     if (c.sortQueries && n >= 4096) {
-        if ((rc = sortCells.ensure(sizeof(uint32_t) << kSortCellBits))) return rc;
+        if ((rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;
         if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
         if ((rc = sortSpheres.ensure((size_t)n * sizeof(DevSphere)))) return rc;
-        // grid over the scene box grown by its extent on every side
-        SortGrid g;
-        float lo[3], ext[3];
-        for (int a = 0; a < 3; a++) {
-            float e0 = std::max(rootBox[3 + a] - rootBox[a], 1e-6f);
-            lo[a] = rootBox[a] - e0;
-            ext[a] = 3.0f * e0;
-        }
-        float cells = dim == 3 ? 64.0f : 512.0f;
-        g.lo = make_float3(lo[0], lo[1], lo[2]);
-        g.invCell = make_float3(cells / ext[0], cells / ext[1], cells / ext[2]);
+        // the grid covers the queries, but no more than the scene box grown by
+        // twice its largest extent on every side
+        float ext = 1e-6f;
+        for (int a = 0; a < dim; a++) ext = std::max(ext, rootBox[3 + a] - rootBox[a]);
+        SortLimits g;
+        g.lo = make_float3(rootBox[0] - 2.0f * ext, rootBox[1] - 2.0f * ext, rootBox[2] - 2.0f * ext);
+        g.hi = make_float3(rootBox[3] + 2.0f * ext, rootBox[4] + 2.0f * ext, rootBox[5] + 2.0f * ext);
         g.dim = dim;
         if ((e = launchSortQueries(g, spheres, n, (uint32_t *)sortCells.ptr, (DevSphere *)sortSpheres.ptr,
-                                   (uint32_t *)sortPerm.ptr, st)) != cudaSuccess)
+                                   (uint32_t *)sortPerm.ptr, numSMs, st)) != cudaSuccess)
             return cudaFail(e, "sort queries");
         l.spheres = (const DevSphere *)sortSpheres.ptr;
         l.perm = (const uint32_t *)sortPerm.ptr;
@@ -102,7 +99,7 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
         if ((rc = workCounter.ensure(16))) return rc;
         if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)workCounter.ptr;
-        blocks = std::min<uint32_t>(blocks, (uint32_t)numSMs * 16u);
+        blocks = std::min<uint32_t>(blocks, (uint32_t)numSMs * 8u);  // one resident wave
     }
     l.grid = blocks;
     if (!stats && (rc = timeStart(st))) return rc;

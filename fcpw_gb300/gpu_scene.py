@@ -400,6 +400,16 @@ class _GPUScene:
                                                  int(bool(check_for_occlusion)), self._stream(rays)))
         return _split_records(raw)
 
+    def closest_distances_f64_tensor(self, spheres):
+        """FP64 brute-force closest distances of the (N, 4) query tensor's centres over
+        all primitives (an accuracy probe, O(N x primitives)). Returns a float64 tensor."""
+        import torch
+        self._check_tensor(spheres, 4)
+        out = torch.empty(spheres.shape[0], dtype=torch.float64, device=spheres.device)
+        check(lib().fcpwgb_closest_distances_f64_device(self._h, spheres.data_ptr(), spheres.shape[0],
+                                                        out.data_ptr(), self._stream(spheres)))
+        return out
+
     def export_nodes(self) -> np.ndarray:
         """The device tree (after any refit) in the interop node layout."""
         nodes = np.zeros(self._n_nodes, R.SNCH_NODE if self._snch else R.BVH_NODE)

@@ -13,8 +13,15 @@ No dataset is involved; every mesh and query set is generated from
 * ``star_polylines``: closed stars, radius 1 + 0.3 sin(k theta + phi),
   k ~ U{3..12}, phi ~ U[0, 2pi), scaled by ``scale`` and centred on a square
   grid covering [-extent, extent]^2.
+* ``batched_meshes``: the uneven-batch workload, n meshes with triangle counts
+  log-uniform in [1e3, 2e5] realised as the nearest perturbed geodesic sphere
+  (20 freq^2) or torus (2 nu nv) count, kinds 50/50, and query counts
+  log-uniform in [1e3, 1e6], queries uniform in each mesh's bounding cube
+  grown by a quarter of its side on every side.
 """
 from __future__ import annotations
+
+import functools
 
 import numpy as np
 
@@ -35,8 +42,21 @@ def _icosahedron():
     return v / np.linalg.norm(v, axis=1, keepdims=True), f
 
 
+@functools.lru_cache(maxsize=None)
+def _geodesic_sphere_cached(freq: int):
+    v, f = _geodesic_sphere(freq)
+    v.setflags(write=False)
+    f.setflags(write=False)
+    return v, f
+
+
 def geodesic_sphere(freq: int):
     """Unit geodesic sphere with 20*freq^2 triangles (shared vertices)."""
+    v, f = _geodesic_sphere_cached(freq)
+    return v.copy(), f.copy()
+
+
+def _geodesic_sphere(freq: int):
     v0, f0 = _icosahedron()
     pts, tris = [], []
     base = 0
@@ -71,18 +91,27 @@ def geodesic_sphere(freq: int):
 
 
 def _vertex_neighbours(n_vertices: int, tris: np.ndarray):
-    e = np.concatenate([tris[:, [0, 1]], tris[:, [1, 2]], tris[:, [2, 0]]])
-    e = np.concatenate([e, e[:, ::-1]])
-    e = np.unique(e, axis=0)
-    return e[:, 0], e[:, 1]
+    """Both directions of every mesh edge, each once, ordered by (src, dst)."""
+    e = np.concatenate([tris[:, [0, 1]], tris[:, [1, 2]], tris[:, [2, 0]]]).astype(np.int64)
+    key = np.unique(np.concatenate([e[:, 0] * n_vertices + e[:, 1], e[:, 1] * n_vertices + e[:, 0]]))
+    return key // n_vertices, key % n_vertices
+
+
+@functools.lru_cache(maxsize=None)
+def _sphere_neighbours(freq: int):
+    verts, tris = _geodesic_sphere_cached(freq)
+    src, dst = _vertex_neighbours(len(verts), tris)
+    deg = np.bincount(src, minlength=len(verts)).astype(np.float64)
+    for a in (src, dst, deg):
+        a.setflags(write=False)
+    return src, dst, deg
 
 
 def perturbed_sphere(freq: int, seed: int, sigma: float = 0.1, smooth_passes: int = 2):
     verts, tris = geodesic_sphere(freq)
     g = rng(seed)
     r = 1.0 + sigma * g.standard_normal(len(verts))
-    src, dst = _vertex_neighbours(len(verts), tris)
-    deg = np.bincount(src, minlength=len(verts)).astype(np.float64)
+    src, dst, deg = _sphere_neighbours(freq)
     for _ in range(smooth_passes):
         mean = np.bincount(src, weights=r[dst], minlength=len(verts)) / deg
         r = 0.5 * (r + mean)
@@ -140,3 +169,37 @@ def uniform_points(n: int, dim: int, lo: float, hi: float, seed: int) -> np.ndar
 def uniform_directions(n: int, dim: int, seed: int) -> np.ndarray:
     d = rng(seed).standard_normal((n, dim))
     return (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+
+
+def batched_meshes(n_meshes: int = 512, seed: int = SEED_BASE + 5, tri_range=(1e3, 2e5), query_range=(1e3, 1e6)):
+    """Returns (meshes, query_counts, query_boxes): meshes[k] = (vertices, triangles),
+    query_boxes[k] = (lo, hi) of the cube the queries of mesh k are drawn from."""
+    g = rng(seed)
+    tris = np.exp(g.uniform(np.log(tri_range[0]), np.log(tri_range[1]), n_meshes))
+    counts = np.exp(g.uniform(np.log(query_range[0]), np.log(query_range[1]), n_meshes)).astype(np.int64)
+    kinds = g.integers(0, 2, n_meshes)
+    meshes, boxes = [], []
+    for k in range(n_meshes):
+        if kinds[k] == 0:
+            freq = max(2, int(round(np.sqrt(tris[k] / 20.0))))
+            v, f = perturbed_sphere(freq, seed + 1000 + k)
+        else:
+            nu = max(4, int(round(np.sqrt(tris[k]))))
+            nv = max(3, int(round(tris[k] / (2.0 * nu))))
+            v, f = torus(nu, nv, seed + 1000 + k)
+        lo, hi = v.min(0), v.max(0)
+        c, side = (lo + hi) / 2, float((hi - lo).max()) * 1.5
+        meshes.append((v, f))
+        boxes.append((c - side / 2, c + side / 2))
+    return meshes, counts, boxes
+
+
+def batched_queries(counts, boxes, seed: int) -> np.ndarray:
+    """Queries of all meshes, grouped by mesh: uniform in each mesh's cube."""
+    g = rng(seed)
+    out = np.empty((int(np.sum(counts)), 3), np.float32)
+    o = 0
+    for nq, (lo, hi) in zip(counts, boxes):
+        out[o:o + nq] = g.uniform(lo, hi, size=(int(nq), 3))
+        o += int(nq)
+    return out

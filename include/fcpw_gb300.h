@@ -300,6 +300,54 @@ int fcpwgb_gpu_scene_export_nodes(fcpwgb_gpu_scene *scene, void *nodes);
  * step budget exhausted in a traversal). Synchronises the scene stream. */
 int fcpwgb_gpu_scene_check_errors(fcpwgb_gpu_scene *scene, uint32_t *error_word);
 
+/* No counterpart in the reference: the FP64 closest distance of every query
+ * (its centre; r2 is ignored) over ALL primitives of the scene, by brute
+ * force, for measuring the distance error of any traversal variant. Device
+ * arrays, asynchronous on stream; O(n x primitives), n <= 2^24. */
+int fcpwgb_closest_distances_f64_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                        uint32_t n, double *distances, void *stream);
+
+/* ------------------------------------------------- batches of scenes ----- */
+/* No counterpart in the reference (its GPUScene holds one object). A batch
+ * holds many scenes of uneven size; the closest points of all their query
+ * sets are found by one persistent launch over a forest of wide trees,
+ * replayed from a captured CUDA graph. Queries arrive grouped by scene: those
+ * of scene s are spheres[query_offsets[s] .. query_offsets[s+1]) and their
+ * interaction indices are primitive indices of scene s. Not thread-safe. */
+typedef struct fcpwgb_gpu_batch fcpwgb_gpu_batch;
+int fcpwgb_gpu_batch_create(int dim, int device, fcpwgb_gpu_batch **out);
+void fcpwgb_gpu_batch_destroy(fcpwgb_gpu_batch *batch);
+/* Copies the trees and primitives of n_scenes host-built BVHs (the handles
+ * may be destroyed afterwards). */
+int fcpwgb_gpu_batch_set_scenes(fcpwgb_gpu_batch *batch, const fcpwgb_cpu_bvh *const *bvhs, uint32_t n_scenes);
+/* branching 2/4/8 and bits 8/16/32 (default 8 and 8), persistent, precise;
+ * queries are always sorted. The forest is rebuilt on the next query when
+ * branching or bits change. */
+int fcpwgb_gpu_batch_set_traversal(fcpwgb_gpu_batch *batch, const fcpwgb_traversal_config *config);
+int fcpwgb_gpu_batch_get_traversal(const fcpwgb_gpu_batch *batch, fcpwgb_traversal_config *config);
+/* Graph replay on (default) or off: with it on, the first call with a given
+ * set of arrays, query layout and traversal captures the call's work in a
+ * CUDA graph and later identical calls launch that graph. */
+int fcpwgb_gpu_batch_use_graph(fcpwgb_gpu_batch *batch, int on);
+/* query_offsets: host array of n_offsets = n_scenes + 1 non-decreasing
+ * entries, query_offsets[0] = 0. Device arrays, asynchronous on stream. */
+int fcpwgb_gpu_batch_find_closest_points_device(fcpwgb_gpu_batch *batch, const fcpwgb_bounding_sphere *spheres,
+                                                const uint32_t *query_offsets, uint32_t n_offsets,
+                                                fcpwgb_interaction *interactions, int record_normals,
+                                                void *stream);
+/* Host arrays, synchronous. */
+int fcpwgb_gpu_batch_find_closest_points(fcpwgb_gpu_batch *batch, const fcpwgb_bounding_sphere *spheres,
+                                         const uint32_t *query_offsets, uint32_t n_offsets,
+                                         fcpwgb_interaction *interactions, int record_normals);
+/* Device arrays, synchronous: stats = {queries, 0, wide records expanded,
+ * primitive tests}. */
+int fcpwgb_gpu_batch_traversal_stats(fcpwgb_gpu_batch *batch, const fcpwgb_bounding_sphere *spheres,
+                                     const uint32_t *query_offsets, uint32_t n_offsets,
+                                     fcpwgb_interaction *interactions, uint64_t stats[4]);
+int fcpwgb_gpu_batch_info(const fcpwgb_gpu_batch *batch, uint32_t *n_scenes, uint32_t *n_wide_nodes,
+                          uint32_t *n_primitives, uint32_t *n_sort_cells);
+int fcpwgb_gpu_batch_check_errors(fcpwgb_gpu_batch *batch, uint32_t *error_word);
+
 #ifdef __cplusplus
 }
 #endif

@@ -292,3 +292,19 @@ def test_queries_before_transfer_raise():
     g = F.GPUScene3D()
     with pytest.raises(F.FcpwError):
         g.find_closest_points(np.zeros((4, 3), np.float32), np.ones(4, np.float32), F.GPUInteractionList())
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_fp64_brute_force_probe_matches_oracle(sphere20k, stars2d, dim):
+    """fcpwgb_closest_distances_f64_device (the accuracy probe) against the C
+    oracle's FP64 brute force: the same FP64 formulas, so agreement to 1e-12."""
+    import torch
+    s, g = sphere20k if dim == 3 else stars2d
+    _, prims, _ = s.cpu_bvh.export()
+    lo, hi = (-1.5, 1.5) if dim == 3 else (-3.0, 3.0)
+    pts = W.uniform_points(700, dim, lo, hi, 33)
+    sph = R.make_spheres(pts, R.FLT_MAX)
+    d_ref, _ = O.closest_points_brute_f64(dim, prims, sph)
+    t = torch.from_numpy(sph.view(np.float32).reshape(-1, 4).copy()).cuda()
+    d_gpu = g.closest_distances_f64_tensor(t).cpu().numpy()
+    assert np.allclose(d_gpu, d_ref, rtol=1e-12, atol=1e-14)
