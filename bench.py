@@ -220,6 +220,10 @@ def distance_loss_bench(device_index: int, steps: int = 20, warmup: int = 5):
             "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "ratio": fb_ms / fwd_ms, "target_ratio_max": 2.5}
 
 
+def _schedule(c) -> str:
+    return "packet" if c.get("packet") else ("persistent" if c.get("persistent") else "thread")
+
+
 def batched_scenes_bench(device_index: int, reps: int = 5):
     """Batched uneven scenes: 512 seeded meshes (perturbed geodesic spheres and
     tori, triangle counts log-uniform in [1e3, 2e5], queries per mesh
@@ -255,7 +259,7 @@ def batched_scenes_bench(device_index: int, reps: int = 5):
     t0 = time.perf_counter()
     batch.set_scenes(scenes)
     set_s = time.perf_counter() - t0
-    space = {"branching": [2, 4, 8], "bits": [8, 16, 32], "persistent": [False]}
+    space = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "packet"]}
     best, table = autotune_batch(batch, spheres, offsets, space=space, reps=2)
 
     def timed(fn):
@@ -292,7 +296,8 @@ def batched_scenes_bench(device_index: int, reps: int = 5):
         g.set_traversal(0)
     plain_ms = timed(per_scene)
     for g in gpus:
-        g.set_traversal(best["branching"], best["bits"], sort_queries=True, persistent=False, precise=True)
+        g.set_traversal(best["branching"], best["bits"], sort_queries=True, persistent=False, precise=True,
+                        packet=best.get("packet", False))
     wide_ms = timed(per_scene)
 
     # FP64 error of the batched results on 256 queries of each of 8 scenes
@@ -309,7 +314,7 @@ def batched_scenes_bench(device_index: int, reps: int = 5):
                         "r2 = FLT_MAX; one graph launch per batch (sort + persistent-capable wide traversal)",
             "meshes": len(scenes), "triangles": info["primitives"], "queries": n,
             "queries_per_s": n / (ms / 1e3), "ms": ms, "variant": best,
-            "autotune_ms": [[c["branching"], c["bits"], round(t, 3)] for c, t in table],
+            "autotune_ms": [[c["branching"], c["bits"], _schedule(c), round(t, 3)] for c, t in table],
             "per_query": {"wide_records_expanded": stats["expanded"] / n, "prim_tests": stats["prim_tests"] / n},
             "per_scene_plain": {"variant": "one GPUScene and one launch per mesh, binary tree, reference order",
                                 "queries_per_s": n / (plain_ms / 1e3), "ms": plain_ms},
@@ -402,9 +407,10 @@ def run_ours(args):
     sample = spheres[: min(n, 1 << 20)]
     if args.variant == "auto":
         best, table = autotune_closest_points(gpu, sample)
-    else:  # fixed "branching,bits,persistent", e.g. for profiling one kernel
+    else:  # fixed "branching,bits,schedule" (0 thread, 1 persistent, 2 packet), e.g. for profiling one kernel
         b, q, p = (int(x) for x in args.variant.split(","))
-        best = {"branching": b, "bits": q, "persistent": bool(p), "sort_queries": True, "precise": True}
+        best = {"branching": b, "bits": q, "persistent": p == 1, "packet": p == 2, "sort_queries": True,
+                "precise": True}
         gpu.set_traversal(**best)
         table = []
     from fcpw_gb300.wide_format import layout
@@ -449,7 +455,8 @@ def run_ours(args):
 
         peak, peak_kind = peaks()
         achieved = fast_stats["bytes"] / (kms / 1e3) / 1e9
-        variant = f"wide{best['branching']}_q{best['bits']}" + ("_persistent" if best["persistent"] else "")
+        variant = f"wide{best['branching']}_q{best['bits']}" + {"thread": "", "persistent": "_persistent",
+                                                                  "packet": "_packet"}[_schedule(best)]
         traffic = profiled_traffic(variant)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -465,7 +472,7 @@ def run_ours(args):
                                  "kernel_ms": plain_kms, "per_query": plain_stats["per_query"],
                                  "achieved_gbs": plain_stats["bytes"] / (plain_kms / 1e3) / 1e9},
                        "speedup_vs_plain": plain_ms / ms,
-                       "autotune_ms": [[c["branching"], c["bits"], int(c["persistent"]), round(t, 4)]
+                       "autotune_ms": [[c["branching"], c["bits"], _schedule(c), round(t, 4)]
                                        for c, t in table]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 40},
             "gpu_launches": args.steps * 4,

@@ -1,17 +1,23 @@
 """Autotuner of the closest point traversal: times candidate variants
-(branching factor, child box precision, persistent scheduling) on a sample of
-the caller's queries and keeps the fastest."""
+(branching factor, child box precision, and the schedule: a thread per query,
+persistent blocks, or warp packets) on a sample of the caller's queries and
+keeps the fastest."""
 from __future__ import annotations
 
 import itertools
 
-DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32], "persistent": [True, False]}
+# schedule: "thread" = one thread per query, "persistent" = persistent blocks
+# with neighbour seeding, "packet" = the queries of a warp traverse together
+DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "persistent", "packet"]}
 
 
 def candidates(space=None, sort_queries=True, precise=True):
-    space = space or DEFAULT_SPACE
-    for b, q, p in itertools.product(space["branching"], space["bits"], space["persistent"]):
-        yield {"branching": b, "bits": q, "persistent": p, "sort_queries": sort_queries, "precise": precise}
+    space = dict(space or DEFAULT_SPACE)
+    if "schedule" not in space:  # older spelling: a list of persistent flags
+        space["schedule"] = ["persistent" if p else "thread" for p in space.get("persistent", [False])]
+    for b, q, sch in itertools.product(space["branching"], space["bits"], space["schedule"]):
+        yield {"branching": b, "bits": q, "persistent": sch == "persistent", "packet": sch == "packet",
+               "sort_queries": sort_queries, "precise": precise}
 
 
 def autotune_closest_points(gpu, spheres, space=None, reps: int = 3, precise: bool = True, out=None):

@@ -56,9 +56,10 @@ class _GPUSceneBatch:
         self._n_scenes = len(bvhs)
 
     def set_traversal(self, branching: int = 8, bits: int = 8, persistent: bool = False,
-                      precise: bool = True) -> None:
+                      precise: bool = True, packet: bool = False) -> None:
         from ._lib import TraversalConfig
-        cfg = TraversalConfig(int(branching), int(bits), 128, 1, int(bool(persistent)), int(bool(precise)))
+        cfg = TraversalConfig(int(branching), int(bits), 128, 1, int(bool(persistent)), int(bool(precise)),
+                              int(bool(packet)))
         check(lib().fcpwgb_gpu_batch_set_traversal(self._h, C.byref(cfg)))
 
     def get_traversal(self) -> dict:
@@ -146,7 +147,7 @@ def autotune_batch(batch: _GPUSceneBatch, spheres, query_offsets, space=None, re
     table = []
     for cfg in candidates(space, precise=precise):
         try:
-            batch.set_traversal(cfg["branching"], cfg["bits"], cfg["persistent"], precise)
+            batch.set_traversal(cfg["branching"], cfg["bits"], cfg["persistent"], precise, cfg.get("packet", False))
             batch.find_closest_points_tensor(spheres, query_offsets, out=out)  # forest build + graph capture
         except Exception:
             continue
@@ -158,5 +159,5 @@ def autotune_batch(batch: _GPUSceneBatch, spheres, query_offsets, space=None, re
         end.synchronize()
         table.append((cfg, start.elapsed_time(end) / reps))
     best = min(table, key=lambda t: t[1])[0]
-    batch.set_traversal(best["branching"], best["bits"], best["persistent"], precise)
+    batch.set_traversal(best["branching"], best["bits"], best["persistent"], precise, best.get("packet", False))
     return best, table

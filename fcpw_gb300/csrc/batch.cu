@@ -32,7 +32,7 @@ struct BatchScene {
 
 struct GraphKey {
     const void *spheres, *out, *nodes, *prims, *cells, *perm, *sorted, *roots, *grids, *offsets;
-    uint32_t n, recordNormal, branching, bits, persistent, precise, sort;
+    uint32_t n, recordNormal, branching, bits, persistent, precise, sort, packet;
     bool operator==(const GraphKey &o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
 
@@ -228,7 +228,8 @@ int enqueue(fcpwgb_gpu_batch *b, const DevSphere *spheres, DevInteraction *out, 
     l.perm = (const uint32_t *)b->perm.ptr;
     l.roots = (const uint32_t *)b->rootBuf.ptr;
     uint32_t blocks = (n + 127) / 128;
-    if (b->cfg.persistent) {
+    l.packet = b->cfg.packet;
+    if (b->cfg.persistent && !b->cfg.packet) {
         if ((e = cudaMemsetAsync(b->counter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)b->counter.ptr;
         blocks = std::min<uint32_t>(blocks, (uint32_t)b->numSMs * 8u);
@@ -262,6 +263,7 @@ int runDevice(fcpwgb_gpu_batch *b, const DevSphere *spheres, const uint32_t *off
     k.branching = (uint32_t)b->cfg.branching; k.bits = (uint32_t)b->cfg.bits;
     k.persistent = (uint32_t)b->cfg.persistent; k.precise = (uint32_t)b->cfg.precise;
     k.sort = (uint32_t)b->cfg.sortQueries;
+    k.packet = (uint32_t)b->cfg.packet;
     cudaError_t e;
     if (!b->exec || !(k == b->key)) {
         b->dropGraph();
@@ -389,6 +391,7 @@ extern "C" int fcpwgb_gpu_batch_set_traversal(fcpwgb_gpu_batch *b, const fcpwgb_
     b->cfg.sortQueries = 1;  // the per-query roots come from the sort
     b->cfg.persistent = c->persistent != 0;
     b->cfg.precise = c->precise != 0;
+    b->cfg.packet = c->packet != 0;
     return FCPWGB_OK;
 }
 
@@ -400,6 +403,7 @@ extern "C" int fcpwgb_gpu_batch_get_traversal(const fcpwgb_gpu_batch *b, fcpwgb_
     c->sort_queries = 1;
     c->persistent = b->cfg.persistent;
     c->precise = b->cfg.precise;
+    c->packet = b->cfg.packet;
     return FCPWGB_OK;
 }
 

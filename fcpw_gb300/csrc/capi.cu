@@ -689,6 +689,7 @@ extern "C" int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *s, const fcpwgb_
     w.sortQueries = c->sort_queries != 0;
     w.persistent = c->persistent != 0;
     w.precise = c->precise != 0;
+    w.packet = c->packet != 0;
     s->wideConfig = w;
     return FCPWGB_OK;
 }
@@ -701,6 +702,7 @@ extern "C" int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *s, fcpwgb_
     c->sort_queries = s->wideConfig.sortQueries;
     c->persistent = s->wideConfig.persistent;
     c->precise = s->wideConfig.precise;
+    c->packet = s->wideConfig.packet;
     return FCPWGB_OK;
 }
 

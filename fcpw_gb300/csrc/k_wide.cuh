@@ -405,6 +405,180 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
     }
 }
 
+// Packet traversal: the 32 (sorted, neighbouring) queries of a warp walk the
+// tree together. Each visited record is loaded once for the warp (all lanes
+// read the same address) and every lane tests its own query against it; a
+// lane takes part in a record only while the record's box is within its own
+// search radius, so each query still prunes exactly as alone. A child is
+// visited when any lane needs it (a ballot), in the order of one lane's
+// distances; per-lane child distances stay on a warp stack (shared memory,
+// one column per lane) and are re-checked against each lane's radius when the
+// entry is popped. Queries of a warp that start at different roots (a forest
+// whose scene boundary falls inside the warp) are walked one root at a time.
+constexpr int kPacketShort = 32;  // warp-stack entries held in shared memory
+template<int W, int BITS, class Prim, bool PRECISE>
+__global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const unsigned char *__restrict__ nodes,
+                                                                      const unsigned char *__restrict__ prims,
+                                                                      const DevSphere *__restrict__ spheres,
+                                                                      const uint32_t *__restrict__ perm,
+                                                                      const uint32_t *__restrict__ roots,
+                                                                      DevInteraction *__restrict__ out, uint32_t n,
+                                                                      int recordNormal, uint32_t *errorWord,
+                                                                      unsigned long long *stats) {
+    constexpr uint32_t kSlotMask = W - 1;
+    constexpr int kWarps = kWideBlock / 32;
+    __shared__ uint32_t sRef[kWarps][kPacketShort];
+    __shared__ float sDist[kWarps][kPacketShort][32];
+    uint32_t lRef[kWideStack - kPacketShort];  // deeper entries: every lane keeps the (uniform) refs
+    float lDist[kWideStack - kPacketShort];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
+    const bool valid = i < n;
+    float3 c = make_float3(0.f, 0.f, 0.f);
+    float r2 = -1.0f;  // a lane without a query needs nothing
+    uint32_t root = 0;
+    if (valid) {
+        float4 s4 = ldg4(spheres + i);
+        c = make_float3(s4.x, s4.y, s4.z);
+        r2 = s4.w;
+        root = roots ? __ldg(roots + i) : 0u;
+    }
+    DevInteraction best = defaultInteraction();
+    uint32_t selected = kUintMax;
+    bool found = false;
+    uint32_t tExp = 0, tTests = 0, tVisits = 0;
+    WideNodeRegs<W, BITS> node;
+
+    uint32_t pending = __ballot_sync(0xffffffffu, valid);
+    while (pending) {
+        const uint32_t rootNow = __shfl_sync(0xffffffffu, root, __ffs(pending) - 1);
+        const bool mine = valid && root == rootNow && ((pending >> lane) & 1u);
+        pending &= ~__ballot_sync(0xffffffffu, mine);
+        bool act = mine;  // this lane needs the current record
+        uint32_t cur = rootNow;
+        int sp = 0;       // warp-uniform
+        for (;;) {
+            bool descend = false;
+            if (!(cur & kLeafBit)) {
+                node.load(nodes, cur);
+                tVisits++;
+                float d2Min[W];
+                childD2Min<W, BITS>(node, c, d2Min);
+                if (act) {
+                    tExp++;
+                    if (!found) {
+#pragma unroll
+                        for (int k = 0; k < W; k++)
+                            if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
+                    }
+                }
+                // children needed by any lane, ordered by the first active lane's distances
+                const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
+                uint32_t key[W];
+                int nh = 0;
+#pragma unroll
+                for (int k = 0; k < W; k++) {
+                    bool need = act && node.cnt(k) != kWideEmpty && d2Min[k] <= r2;
+                    bool any = __ballot_sync(0xffffffffu, need) != 0;
+                    float lead = __shfl_sync(0xffffffffu, d2Min[k], leader);
+                    key[k] = any ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
+                    nh += any ? 1 : 0;
+                }
+                sortNetwork<W>(key);
+                if (nh > 0) {
+                    if (sp + nh - 1 > kWideStack) {
+                        if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
+                        break;
+                    }
+#pragma unroll
+                    for (int k = W - 1; k >= 0; k--) {
+                        if (k < nh) {
+                            uint32_t slot = key[k] & kSlotMask, ref = 0, cntv = 0;
+                            float mine2 = 0.0f;
+#pragma unroll
+                            for (int s = 0; s < W; s++) {
+                                if (slot == (uint32_t)s) {
+                                    ref = node.ref(s);
+                                    cntv = node.cnt(s);
+                                    mine2 = d2Min[s];
+                                }
+                            }
+                            uint32_t packed = cntv == 0 ? ref : packLeaf(ref, cntv);
+                            // a lane out of this record is out of its children too
+                            float dl = act ? mine2 : __int_as_float(0x7fc00000);  // NaN: never <= r2
+                            if (k == 0) {
+                                cur = packed;
+                                act = dl <= r2;
+                            } else {
+                                if (sp < kPacketShort) {
+                                    if (lane == 0) sRef[warp][sp] = packed;
+                                    sDist[warp][sp][lane] = dl;
+                                } else {
+                                    lRef[sp - kPacketShort] = packed;
+                                    lDist[sp - kPacketShort] = dl;
+                                }
+                                sp++;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    descend = true;
+                }
+            } else {
+                uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+                if (act) tTests += cnt;
+                for (uint32_t p = 0; p < cnt; p++) {
+                    Prim prim = Prim::load(prims, off + p);
+                    if (act) {
+                        float3 pt;
+                        float2 uv;
+                        float d = prim.closestPoint(c, pt, uv);
+                        if (d * d <= r2) {
+                            r2 = fminf(r2, d * d);
+                            best.p = pt;
+                            best.n = make_float3(0.f, 0.f, 0.f);
+                            best.uv = uv;
+                            best.d = d;
+                            best.index = prim.index;
+                            selected = off + p;
+                            found = true;
+                        }
+                    }
+                }
+            }
+            if (descend) continue;
+            // pop until some lane needs the entry
+            bool next = false;
+            while (sp > 0) {
+                sp--;
+                uint32_t ref;
+                float dl;
+                if (sp < kPacketShort) {
+                    ref = sRef[warp][sp];
+                    dl = sDist[warp][sp][lane];
+                } else {
+                    ref = lRef[sp - kPacketShort];
+                    dl = lDist[sp - kPacketShort];
+                }
+                act = dl <= r2;
+                if (__ballot_sync(0xffffffffu, act)) {
+                    cur = ref;
+                    next = true;
+                    break;
+                }
+            }
+            __syncwarp();
+            if (!next) break;
+        }
+    }
+    if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, i, c, found, selected, recordNormal, best);
+    if (stats) {
+        if (lane == 0) atomicAdd(stats + 0, (unsigned long long)tVisits);
+        atomicAdd(stats + 1, (unsigned long long)tExp);
+        atomicAdd(stats + 2, (unsigned long long)tTests);
+    }
+}
+
 // Re-quantises every wide node from the (refit) binary boxes behind its slots.
 template<int W, int BITS>
 __global__ void kRequantize(unsigned char *wideNodes, const int32_t *childBinary, const unsigned char *binNodes,
@@ -446,9 +620,23 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
             kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal,         \
                                  l.counter, l.errorWord, l.stats);                                                 \
         };                                                                                                         \
+        auto goPacket = [&](auto kern) {                                                                           \
+            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal,         \
+                                 l.errorWord, l.stats);                                                            \
+        };                                                                                                         \
         auto pick = [&](auto bitsConst) {                                                                          \
             constexpr int B = decltype(bitsConst)::value;                                                          \
             const bool p = l.counter != nullptr;                                                                   \
+            if (l.packet) {                                                                                        \
+                if (dim == 3) {                                                                                    \
+                    if (precise) goPacket(kWidePacketClosestPoint<W, B, Tri48Prim, true>);                         \
+                    else goPacket(kWidePacketClosestPoint<W, B, Tri48Prim, false>);                                \
+                } else {                                                                                           \
+                    if (precise) goPacket(kWidePacketClosestPoint<W, B, Seg24Prim, true>);                         \
+                    else goPacket(kWidePacketClosestPoint<W, B, Seg24Prim, false>);                                \
+                }                                                                                                  \
+                return;                                                                                            \
+            }                                                                                                      \
             if (dim == 3) {                                                                                        \
                 if (precise) { if (p) go(kWideClosestPoint<W, B, Tri48Prim, true, true>); else go(kWideClosestPoint<W, B, Tri48Prim, true, false>); } \
                 else { if (p) go(kWideClosestPoint<W, B, Tri48Prim, false, true>); else go(kWideClosestPoint<W, B, Tri48Prim, false, false>); } \

@@ -49,6 +49,7 @@ struct WideLaunch {
     uint32_t n = 0;
     int recordNormal = 0;
     uint32_t *counter = nullptr;           // work counter (zero on entry) for persistent blocks, or NULL
+    int packet = 0;                        // 1: warp packets (kWidePacketClosestPoint), counter unused
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;   // traversal statistics, or NULL
     uint32_t grid = 0;

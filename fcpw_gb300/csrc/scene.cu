@@ -95,7 +95,8 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
         l.perm = (const uint32_t *)sortPerm.ptr;
     }
     uint32_t blocks = (n + 127) / 128;
-    if (c.persistent) {
+    l.packet = c.packet;
+    if (c.persistent && !c.packet) {
         if ((rc = workCounter.ensure(16))) return rc;
         if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)workCounter.ptr;

@@ -27,6 +27,7 @@ struct WideConfig {
     int sortQueries = 1; // reorder queries by spatial cell before traversal
     int persistent = 1;  // persistent blocks fetching query chunks from a work counter
     int precise = 1;     // recompute the winning primitive's distance in FP64
+    int packet = 0;      // traverse the 32 queries of a warp as one packet
 };
 
 constexpr int wideHeaderBytes(int bits) { return bits == 32 ? 0 : 16; }

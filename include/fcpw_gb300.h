@@ -210,9 +210,12 @@ int fcpwgb_gpu_scene_update_vertices_device_static(fcpwgb_gpu_scene *scene, cons
  * are stored in 32-bit floats or conservatively quantised to 16 or 8 bits;
  * sort_queries reorders each batch spatially before traversal, persistent
  * runs one resident block set that fetches query chunks from a counter, and
- * precise recomputes the winning primitive's distance and point in FP64.
- * Defaults: {0, 32, 128, 1, 1, 1}. Results differ from the binary order only
- * on equidistant ties (and, with precise, by the FP32 rounding removed). */
+ * precise recomputes the winning primitive's distance and point in FP64;
+ * packet traverses the 32 (sorted) queries of a warp together, one record
+ * load per warp and step, each query pruning with its own radius (persistent
+ * is then ignored). Defaults: {0, 32, 128, 1, 1, 1, 0}. Results differ from
+ * the binary order only on equidistant ties (and, with precise, by the FP32
+ * rounding removed). */
 typedef struct {
     int branching;     /* 0, 2, 4 or 8 */
     int bits;          /* 32, 16 or 8 */
@@ -220,6 +223,7 @@ typedef struct {
     int sort_queries;  /* 0 or 1 */
     int persistent;    /* 0 or 1 */
     int precise;       /* 0 or 1 */
+    int packet;        /* 0 or 1 */
 } fcpwgb_traversal_config;
 int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *scene, const fcpwgb_traversal_config *config);
 int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *scene, fcpwgb_traversal_config *config);

@@ -68,12 +68,14 @@ def _tensor_run(b, pts, offsets, **kw):
 
 @pytest.mark.parametrize("branching", [2, 4, 8])
 @pytest.mark.parametrize("bits", [32, 16, 8])
-@pytest.mark.parametrize("persistent", [False, True])
-def test_batch_matches_per_scene_oracle(batch3, branching, bits, persistent):
+@pytest.mark.parametrize("schedule", ["thread", "persistent", "packet"])
+def test_batch_matches_per_scene_oracle(batch3, branching, bits, schedule):
+    """Warps straddling scene boundaries (137 and 1 queries) exercise the
+    per-root passes of the packet kernel and the root change of the seeds."""
     b, scenes, pts, refs, prims, offsets = batch3
-    b.set_traversal(branching, bits, persistent=persistent, precise=True)
+    b.set_traversal(branching, bits, persistent=schedule == "persistent", precise=True, packet=schedule == "packet")
     got, _ = _tensor_run(b, pts, offsets)
-    _check(b, pts, refs, prims, offsets, got, f"batch {branching}/{bits}/{int(persistent)}")
+    _check(b, pts, refs, prims, offsets, got, f"batch {branching}/{bits}/{schedule}")
     assert b.check_errors() == 0
 
 
@@ -126,7 +128,8 @@ def test_batch_2d_segments():
     offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32)
     b = F.GPUSceneBatch2D()
     b.set_scenes(scenes)
-    for cfg in [(4, 8, False), (8, 16, True), (2, 32, False)]:
+    for cfg in [(4, 8, False, True, False), (8, 16, True, True, False), (2, 32, False, True, False),
+                (4, 8, False, True, True)]:
         b.set_traversal(*cfg)
         out = F.GPUInteractionList()
         b.find_closest_points(np.concatenate(pts), np.full(int(offsets[-1]), R.FLT_MAX, np.float32), offsets, out)

@@ -49,6 +49,32 @@ def test_wide_scheduling_options_agree(torus, sort_queries, persistent):
     compare_closest(3, prims, pts, got, ref, "wide scheduling")
 
 
+@pytest.mark.parametrize("branching", [2, 4, 8])
+@pytest.mark.parametrize("bits", [32, 16, 8])
+def test_packet_traversal_matches_oracle(torus, branching, bits):
+    """Warp packets: each query still prunes with its own radius."""
+    s, g, pts, ref, prims = torus
+    g.set_traversal(branching, bits, sort_queries=True, precise=False, packet=True)
+    got = _run(g, pts)
+    compare_closest(3, prims, pts, got, ref, f"packet {branching}/{bits}")
+    assert g.check_errors() == 0
+
+
+def test_packet_unsorted_finite_radius_and_normals(torus):
+    """Packets of unsorted queries with finite, different radii per lane."""
+    s, g, pts, ref, prims = torus
+    r2 = (0.05 * W.rng(43).uniform(0, 1, len(pts))).astype(np.float32)
+    nodes, _, _ = s.cpu_bvh.export()
+    ref2 = O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts, r2), record_normals=True)
+    g.set_traversal(4, 8, sort_queries=False, precise=False, packet=True)
+    out = F.GPUInteractionList()
+    g.find_closest_points(pts, r2, out, True)
+    got = out.array()
+    compare_closest(3, prims, pts, got, ref2, "packet finite radius")
+    same = (got["index"] == ref2["index"]) & (ref2["index"] != R.UINT_MAX)
+    assert np.allclose(got["n"][same], ref2["n"][same], atol=1e-6)
+
+
 def test_precise_mode_within_1e6_of_fp64(torus):
     s, g, pts, ref, prims = torus
     g.set_traversal(4, 8, precise=True)
