@@ -362,17 +362,21 @@ def run_ours(args):
     def step():
         check(L.fcpwgb_find_closest_points_device(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, 0, sptr))
 
-    def traversal_stats(node_bytes, prim_bytes, in_bytes):
-        stats = (C.c_uint64 * 4)()
+    def traversal_stats(node_bytes, prim_bytes, in_bytes, packet=False):
+        stats = (C.c_uint64 * 8)()
         check(L.fcpwgb_closest_points_traversal_stats(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, stats))
-        n_q, n_pop, n_inner, n_prim = [int(x) for x in stats]
+        n_q, n_pop, n_inner, n_prim, w_rec, w_prim = [int(x) for x in stats[:6]]
         if node_bytes == 32:  # binary: every expansion loads two 32 B child records, plus the root
-            nb = 32 * (n_q + 2 * n_inner)
-        else:  # wide: every expansion loads one node record holding all child boxes
-            nb = node_bytes * n_inner
-        return {"bytes": n_q * (in_bytes + 40) + nb + prim_bytes * n_prim,
-                "per_query": {"nodes_popped": n_pop / n_q if node_bytes == 32 else n_inner / n_q,
-                              "inner_expanded": n_inner / n_q, "prim_tests": n_prim / n_q}}
+            nb, pb = 32 * (n_q + 2 * n_inner), prim_bytes * n_prim
+        elif packet:  # warp packets: one record / triangle load serves the 32 queries of a warp
+            nb, pb = node_bytes * w_rec, prim_bytes * w_prim
+        else:  # wide, a thread per query: every expansion loads one record holding all child boxes
+            nb, pb = node_bytes * n_inner, prim_bytes * n_prim
+        per_query = {"nodes_popped": n_pop / n_q if node_bytes == 32 else n_inner / n_q,
+                     "inner_expanded": n_inner / n_q, "prim_tests": n_prim / n_q}
+        if packet:
+            per_query.update({"warp_record_loads": w_rec / n_q, "warp_prim_loads": w_prim / n_q})
+        return {"bytes": n_q * (in_bytes + 40) + nb + pb, "per_query": per_query}
 
     def timed(steps, warmup):
         for _ in range(warmup):
@@ -419,7 +423,7 @@ def run_ours(args):
     sampler.start()
     time.sleep(0.3)
     ms, kms = timed(args.steps, args.warmup)
-    fast_stats = traversal_stats(node_bytes, 48, 20)  # sorted sphere + permutation index per query
+    fast_stats = traversal_stats(node_bytes, 48, 20, packet=bool(best.get("packet")))  # sorted query + permutation
     ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
     if world > 1:
         dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
@@ -478,7 +482,8 @@ def run_ours(args):
             "gpu_launches": args.steps * 4,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"hbm_gbs ({peak_kind})",
-                         "kernel": "kWideClosestPoint", "kernel_ms": kms,
+                         "kernel": "kWidePacketClosestPoint" if best.get("packet") else "kWideClosestPoint",
+                         "kernel_ms": kms,
                          "algorithmic_bytes_per_launch": fast_stats["bytes"], "per_query": fast_stats["per_query"]},
             "clocks": clocks, "accuracy": accuracy,
         }

@@ -111,10 +111,11 @@ class _GPUSceneBatch:
         off = _offsets(query_offsets, self._n_scenes)
         n = spheres.shape[0]
         raw = out if out is not None else torch.empty((n, 10), dtype=torch.float32, device=spheres.device)
-        st = (C.c_uint64 * 4)()
+        st = (C.c_uint64 * 8)()
         check(lib().fcpwgb_gpu_batch_traversal_stats(self._h, spheres.data_ptr(), ptr(off), len(off),
                                                      raw.data_ptr(), st))
-        return {"queries": int(st[0]), "expanded": int(st[2]), "prim_tests": int(st[3])}
+        return {"queries": int(st[0]), "expanded": int(st[2]), "prim_tests": int(st[3]),
+                "warp_record_loads": int(st[4]), "warp_prim_loads": int(st[5])}
 
     def info(self) -> dict:
         v = [C.c_uint32(0) for _ in range(4)]

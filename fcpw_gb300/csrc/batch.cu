@@ -455,26 +455,25 @@ extern "C" int fcpwgb_gpu_batch_find_closest_points(fcpwgb_gpu_batch *b, const f
 
 extern "C" int fcpwgb_gpu_batch_traversal_stats(fcpwgb_gpu_batch *b, const fcpwgb_bounding_sphere *spheres,
                                                 const uint32_t *query_offsets, uint32_t n_offsets,
-                                                fcpwgb_interaction *interactions, uint64_t stats[4]) {
+                                                fcpwgb_interaction *interactions, uint64_t stats[8]) {
     if (!b || !stats) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
     int rc = prepare(b, query_offsets, n_offsets);
     if (rc) return rc;
     const uint32_t n = b->hostOffsets.back();
     DeviceBuffer counters;
-    if ((rc = counters.ensure(4 * sizeof(unsigned long long)))) return rc;
-    cudaError_t e = cudaMemsetAsync(counters.ptr, 0, 4 * sizeof(unsigned long long), b->stream);
+    if ((rc = counters.ensure(8 * sizeof(unsigned long long)))) return rc;
+    cudaError_t e = cudaMemsetAsync(counters.ptr, 0, 8 * sizeof(unsigned long long), b->stream);
     if (e != cudaSuccess) return cudaFail(e, "cudaMemsetAsync");
     if (n > 0 && (rc = enqueue(b, (const DevSphere *)spheres, (DevInteraction *)interactions, n, 0,
                                (unsigned long long *)counters.ptr, b->stream)))
         return rc;
-    unsigned long long h[4];
+    unsigned long long h[8];
     if ((e = cudaMemcpyAsync(h, counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, b->stream)) != cudaSuccess)
         return cudaFail(e, "cudaMemcpyAsync");
     if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return cudaFail(e, "cudaStreamSynchronize");
     stats[0] = n;
-    stats[1] = 0;
-    stats[2] = h[1];
-    stats[3] = h[2];
+    for (int k = 0; k < 5; k++) stats[k + 1] = h[k];
+    stats[6] = stats[7] = 0;
     return FCPWGB_OK;
 }
 

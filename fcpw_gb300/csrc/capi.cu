@@ -660,18 +660,17 @@ extern "C" int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *s, const 
     if (!stats) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL stats");
     if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
     DeviceBuffer counters;
-    if ((rc = counters.ensure(4 * sizeof(unsigned long long)))) return rc;
-    FCPWGB_CUDA(cudaMemsetAsync(counters.ptr, 0, 4 * sizeof(unsigned long long), s->stream));
+    if ((rc = counters.ensure(8 * sizeof(unsigned long long)))) return rc;
+    FCPWGB_CUDA(cudaMemsetAsync(counters.ptr, 0, 8 * sizeof(unsigned long long), s->stream));
     if ((rc = s->closestPointsStats((const DevSphere *)spheres, (DevInteraction *)out, n,
                                     (unsigned long long *)counters.ptr, s->stream)))
         return rc;
-    unsigned long long h[4] = {0, 0, 0, 0};
+    unsigned long long h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     FCPWGB_CUDA(cudaMemcpyAsync(h, counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
     FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
     stats[0] = n;
-    stats[1] = h[0];
-    stats[2] = h[1];
-    stats[3] = h[2];
+    for (int k = 0; k < 5; k++) stats[k + 1] = h[k];
+    stats[6] = stats[7] = 0;
     return FCPWGB_OK;
 }
 

@@ -150,6 +150,31 @@ FCPWGB_D float childD2Max(const WideNodeRegs<W, BITS> &node, float3 c, int k) {
 constexpr uint32_t kLeafBit = 0x80000000u;
 FCPWGB_D uint32_t packLeaf(uint32_t off, uint32_t cnt) { return kLeafBit | (cnt << 27) | off; }
 
+// a[slot] for a register array and a runtime slot < W: a binary tree of
+// selects on the slot's bits (W - 1 selects) instead of W compare-and-selects
+template<int W, class T> FCPWGB_D T selectBySlot(const T (&a)[W], uint32_t slot) {
+    if constexpr (W == 2) {
+        return (slot & 1u) ? a[1] : a[0];
+    } else if constexpr (W == 4) {
+        T lo = (slot & 1u) ? a[1] : a[0], hi = (slot & 1u) ? a[3] : a[2];
+        return (slot & 2u) ? hi : lo;
+    } else {
+        T q0 = (slot & 1u) ? a[1] : a[0], q1 = (slot & 1u) ? a[3] : a[2];
+        T q2 = (slot & 1u) ? a[5] : a[4], q3 = (slot & 1u) ? a[7] : a[6];
+        T h0 = (slot & 2u) ? q1 : q0, h1 = (slot & 2u) ? q3 : q2;
+        return (slot & 4u) ? h1 : h0;
+    }
+}
+
+// the stack reference of every child slot: inner record index, or a packed leaf
+template<int W, int BITS> FCPWGB_D void childRefs(const WideNodeRegs<W, BITS> &node, uint32_t (&packed)[W]) {
+#pragma unroll
+    for (int s = 0; s < W; s++) {
+        uint32_t n = node.cnt(s);
+        packed[s] = n == 0 ? node.ref(s) : packLeaf(node.ref(s), n);
+    }
+}
+
 // Sorting networks over packed keys (non-negative float bits with the child
 // slot in the low bits): integer min/max compare-exchanges. Optimal networks
 // for 2, 4 (5 comparators) and 8 (19 comparators) inputs.
@@ -242,19 +267,12 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
                     atomicOr(errorWord, kErrStackOverflow);
                     return found;
                 }
-                uint32_t firstRef = 0;
+                uint32_t firstRef = 0, refs[W];
+                childRefs<W, BITS>(node, refs);
 #pragma unroll
                 for (int k = W - 1; k >= 0; k--) {
                     if (k < nh) {
-                        uint32_t slot = key[k] & kSlotMask, ref = 0, n = 0;
-#pragma unroll
-                        for (int s = 0; s < W; s++) {
-                            if (slot == (uint32_t)s) {
-                                ref = node.ref(s);
-                                n = node.cnt(s);
-                            }
-                        }
-                        uint32_t packed = n == 0 ? ref : packLeaf(ref, n);
+                        uint32_t packed = selectBySlot<W>(refs, key[k] & kSlotMask);
                         if (k == 0) {
                             firstRef = packed;
                         } else {
@@ -446,7 +464,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
     DevInteraction best = defaultInteraction();
     uint32_t selected = kUintMax;
     bool found = false;
-    uint32_t tExp = 0, tTests = 0, tVisits = 0;
+    uint32_t tExp = 0, tTests = 0, tVisits = 0, tPrimLoads = 0;
     WideNodeRegs<W, BITS> node;
 
     uint32_t pending = __ballot_sync(0xffffffffu, valid);
@@ -490,22 +508,18 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                         if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
                         break;
                     }
+                    uint32_t refs[W];
+                    childRefs<W, BITS>(node, refs);
+                    // a lane out of this record is out of its children too (NaN is never <= r2)
+                    float mine[W];
+#pragma unroll
+                    for (int s = 0; s < W; s++) mine[s] = act ? d2Min[s] : __int_as_float(0x7fc00000);
 #pragma unroll
                     for (int k = W - 1; k >= 0; k--) {
                         if (k < nh) {
-                            uint32_t slot = key[k] & kSlotMask, ref = 0, cntv = 0;
-                            float mine2 = 0.0f;
-#pragma unroll
-                            for (int s = 0; s < W; s++) {
-                                if (slot == (uint32_t)s) {
-                                    ref = node.ref(s);
-                                    cntv = node.cnt(s);
-                                    mine2 = d2Min[s];
-                                }
-                            }
-                            uint32_t packed = cntv == 0 ? ref : packLeaf(ref, cntv);
-                            // a lane out of this record is out of its children too
-                            float dl = act ? mine2 : __int_as_float(0x7fc00000);  // NaN: never <= r2
+                            const uint32_t slot = key[k] & kSlotMask;
+                            uint32_t packed = selectBySlot<W>(refs, slot);
+                            float dl = selectBySlot<W>(mine, slot);
                             if (k == 0) {
                                 cur = packed;
                                 act = dl <= r2;
@@ -526,6 +540,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                 }
             } else {
                 uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+                tPrimLoads += cnt;
                 if (act) tTests += cnt;
                 for (uint32_t p = 0; p < cnt; p++) {
                     Prim prim = Prim::load(prims, off + p);
@@ -573,7 +588,10 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
     }
     if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, i, c, found, selected, recordNormal, best);
     if (stats) {
-        if (lane == 0) atomicAdd(stats + 0, (unsigned long long)tVisits);
+        if (lane == 0) {
+            atomicAdd(stats + 3, (unsigned long long)tVisits);
+            atomicAdd(stats + 4, (unsigned long long)tPrimLoads);
+        }
         atomicAdd(stats + 1, (unsigned long long)tExp);
         atomicAdd(stats + 2, (unsigned long long)tTests);
     }

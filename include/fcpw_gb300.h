@@ -265,12 +265,15 @@ int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *scene,
                                                  void *stream);
 
 /* Runs the closest point query of the scene's current variant over device
- * spheres in counting mode and returns, synchronously, stats[0] = queries,
- * stats[1] = popped (loaded) nodes, stats[2] = expanded inner nodes,
- * stats[3] = primitive tests, summed over all queries. Used to compute the
- * algorithmic bytes of a launch; results are written to interactions. */
+ * spheres in counting mode and returns, synchronously, eight counters:
+ * stats[0] = queries, stats[1] = popped (loaded) binary nodes, stats[2] =
+ * expanded inner records, stats[3] = primitive tests (the last three summed
+ * over all queries), stats[4] = record loads and stats[5] = primitive loads
+ * of the warp-packet kernel (one per warp and step), stats[6..7] = 0. Used
+ * to compute the algorithmic bytes of a launch; results are written to
+ * interactions. */
 int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
-                                          fcpwgb_interaction *interactions, uint32_t n, uint64_t *stats);
+                                          fcpwgb_interaction *interactions, uint32_t n, uint64_t stats[8]);
 
 /* ----- differentiation (no counterpart in the reference; needs a tree
  * transferred with prim_vertices). Device arrays, asynchronous on stream. ----- */
@@ -343,11 +346,11 @@ int fcpwgb_gpu_batch_find_closest_points_device(fcpwgb_gpu_batch *batch, const f
 int fcpwgb_gpu_batch_find_closest_points(fcpwgb_gpu_batch *batch, const fcpwgb_bounding_sphere *spheres,
                                          const uint32_t *query_offsets, uint32_t n_offsets,
                                          fcpwgb_interaction *interactions, int record_normals);
-/* Device arrays, synchronous: stats = {queries, 0, wide records expanded,
- * primitive tests}. */
+/* Device arrays, synchronous: the eight counters of
+ * fcpwgb_closest_points_traversal_stats for one batched launch. */
 int fcpwgb_gpu_batch_traversal_stats(fcpwgb_gpu_batch *batch, const fcpwgb_bounding_sphere *spheres,
                                      const uint32_t *query_offsets, uint32_t n_offsets,
-                                     fcpwgb_interaction *interactions, uint64_t stats[4]);
+                                     fcpwgb_interaction *interactions, uint64_t stats[8]);
 int fcpwgb_gpu_batch_info(const fcpwgb_gpu_batch *batch, uint32_t *n_scenes, uint32_t *n_wide_nodes,
                           uint32_t *n_primitives, uint32_t *n_sort_cells);
 int fcpwgb_gpu_batch_check_errors(fcpwgb_gpu_batch *batch, uint32_t *error_word);
