@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-loss", action="store_true", help="skip the fwd/fwd+bwd distance loss measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven scenes measurement")
+    ap.add_argument("--suite", action="store_true",
+                    help="instead of the headline line, one line per other configuration of the scope")
     return ap.parse_args()
 
 
@@ -218,6 +220,196 @@ def distance_loss_bench(device_index: int, steps: int = 20, warmup: int = 5):
     return {"workload": "loss = mean unsigned distance^2, perturbed sphere 200,000 triangles (geodesic frequency 100), "
                         "2^20 queries uniform in [-1.5,1.5]^3, GPU refit every forward, backward to queries and vertices",
             "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "ratio": fb_ms / fwd_ms, "target_ratio_max": 2.5}
+
+
+def run_suite(args):
+    """One JSON line per configuration of the scope (1M-query icosphere, rays on
+    the 1M-triangle torus, 2D segments and silhouettes, 3D silhouettes on the
+    torus): GPU kernels timed with CUDA events on device-resident inputs (L2
+    flushed before each timed call), next to the reference CPU algorithm (the
+    oracle port, all host threads) on a bounded sample of the same inputs."""
+    import torch
+    import fcpw_gb300 as F
+    from fcpw_gb300 import records as R
+    from fcpw_gb300 import workloads as W
+    from fcpw_gb300._lib import check, lib
+    from fcpw_gb300.autotune import autotune_closest_points
+    from oracle import oracle as O
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    L = lib()
+    threads = os.cpu_count() or 1
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            tot += a.elapsed_time(b)
+        return tot / reps
+
+    def cpu_rate(fn, n_all, budget_s=6.0):
+        n0 = min(n_all, 8192)
+        t = time.perf_counter()
+        fn(n0)
+        rate = n0 / max(time.perf_counter() - t, 1e-9)
+        n = int(min(n_all, max(n0, rate * budget_s)))
+        t = time.perf_counter()
+        fn(n)
+        dt = time.perf_counter() - t
+        return {"value": n / dt, "unit": UNIT, "cores": threads, "kind": "port", "sample": f"first {n} of {n_all}"}
+
+    def sph_tensor(pts, r2=R.FLT_MAX):
+        t = torch.empty((len(pts), 4), dtype=torch.float32, device=dev)
+        t[:, : pts.shape[1]] = torch.from_numpy(pts).to(dev)
+        if pts.shape[1] == 2:
+            t[:, 2] = 0.0
+        t[:, 3] = float(r2)
+        return t
+
+    def closest_point_config(name, dim, v, idx, pts, silhouettes=False):
+        s = F.Scene3D() if dim == 3 else F.Scene2D()
+        s.set_object_count(1)
+        s.set_object_vertices(v, 0)
+        if dim == 3:
+            s.set_object_triangles(idx, 0)
+        else:
+            s.set_object_line_segments(idx, 0)
+        if silhouettes:
+            s.compute_silhouettes()
+        s.build(F.AggregateType.Bvh_SurfaceArea, False)
+        g = (F.GPUScene3D if dim == 3 else F.GPUScene2D)("", False, device=0)
+        g.transfer_to_gpu(s)
+        n = len(pts)
+        sph = sph_tensor(pts)
+        out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+
+        def run():
+            check(L.fcpwgb_find_closest_points_device(g.handle, sph.data_ptr(), out.data_ptr(), n, 0, sp))
+
+        g.set_traversal(0)
+        plain_ms = timed(run)
+        best, _ = autotune_closest_points(g, sph[: min(n, 1 << 20)])
+        fast_ms = timed(run)
+        k = 1024
+        d64 = g.closest_distances_f64_tensor(sph[:k].contiguous()).cpu().numpy()
+        rel = np.abs(out[:k, 8].cpu().numpy().astype(np.float64) - d64) / d64
+        nodes, prims, sils = s.cpu_bvh.export()
+        cpu = cpu_rate(lambda m: O.closest_points_bvh(dim, nodes, prims, R.make_spheres(pts[:m], R.FLT_MAX),
+                                                      nthreads=threads), n)
+        return s, g, {"config": name, "queries": n, "primitives": int(len(idx)),
+                      "plain": {"queries_per_s": n / (plain_ms / 1e3), "ms": plain_ms},
+                      "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms, "variant": best},
+                      "speedup_vs_plain": plain_ms / fast_ms,
+                      "accuracy": {"samples": k, "max_rel_err_vs_fp64": float(rel.max()),
+                                   "mean_rel_err_vs_fp64": float(rel.mean())},
+                      "cpu_baseline": cpu}
+
+    lines = []
+    # C1: 20,480-triangle perturbed icosphere, 1,048,576 queries in [-1.5, 1.5]^3
+    v, f = W.perturbed_sphere(32, W.SEED_BASE + 1)
+    _, _, line = closest_point_config("icosphere 20,480 triangles, 1,048,576 closest-point queries", 3, v, f,
+                                      W.uniform_points(1 << 20, 3, -1.5, 1.5, W.SEED_BASE + 1001))
+    lines.append(line)
+
+    # C2 rays: 4,194,304 rays on the 1M-triangle torus, origins in [-2, 2]^3, directions uniform on S^2
+    v, f, _ = make_workload(0, 1)
+    s, _ = build_scene(v, f)
+    g = F.GPUScene3D("", False, device=0)
+    g.transfer_to_gpu(s)
+    n = N_QUERIES
+    o = W.uniform_points(n, 3, -2.0, 2.0, W.SEED_BASE + 2002)
+    d = W.uniform_directions(n, 3, W.SEED_BASE + 2003)
+    rays_np = R.make_rays(o, d, R.FLT_MAX)
+    rays = torch.from_numpy(rays_np.view(np.float32).reshape(n, 10).copy()).to(dev)
+    out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+    def ray_run():
+        check(L.fcpwgb_intersect_rays_device(g.handle, rays.data_ptr(), out.data_ptr(), n, 0, sp))
+
+    g.set_traversal(0)
+    ray_ms = timed(ray_run)
+    hits = float((out[:, 9].view(torch.int32) != -1).float().mean())
+    table = []
+    for wb in [(2, 32, True), (4, 8, True), (4, 16, True), (4, 32, True), (4, 32, False), (8, 8, True),
+               (8, 16, True), (8, 32, True)]:
+        g.set_traversal(*wb[:2], sort_queries=wb[2])
+        table.append((wb, timed(ray_run, reps=3)))
+    (wb_best, _) = min(table, key=lambda t: t[1])
+    g.set_traversal(*wb_best[:2], sort_queries=wb_best[2])
+    fast_ms = timed(ray_run)
+    nodes, prims, _ = s.cpu_bvh.export()
+    cpu = cpu_rate(lambda m: O.intersect_rays_bvh(3, nodes, prims, rays_np[:m], nthreads=threads), n)
+    lines.append({"config": "rays, torus 1,048,576 triangles, 4,194,304 rays (first hit)", "queries": n,
+                  "plain": {"queries_per_s": n / (ray_ms / 1e3), "ms": ray_ms},
+                  "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms,
+                           "variant": {"branching": wb_best[0], "bits": wb_best[1], "sort_queries": wb_best[2]}},
+                  "speedup_vs_plain": ray_ms / fast_ms, "hit_fraction": hits,
+                  "autotune_ms": [[w, b, int(o), round(t, 3)] for (w, b, o), t in table], "cpu_baseline": cpu})
+    del g, s
+
+    # C3: 256 star polylines x 512 segments, 8,388,608 queries in [-3, 3]^2: closest point and silhouettes
+    v, sg = W.star_polylines(256, 512, W.SEED_BASE + 3, extent=3.0, scale=0.14)
+    pts2 = W.uniform_points(8 << 20, 2, -3.0, 3.0, W.SEED_BASE + 3003)
+    s2, g2, line = closest_point_config("2D stars 131,072 segments, 8,388,608 closest-point queries", 2, v, sg,
+                                        pts2, silhouettes=True)
+    lines.append(line)
+    n = len(pts2)
+    sph = sph_tensor(pts2)
+    flip = torch.zeros(n, dtype=torch.int32, device=dev)
+    out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+    def sil_run(gs, sph, flip, out, n):
+        return lambda: check(L.fcpwgb_find_closest_silhouette_points_device(
+            gs.handle, sph.data_ptr(), flip.data_ptr(), out.data_ptr(), n, 0.0, 1e-3, sp))
+
+    def sil_times(gs, sph, flip, out, n):
+        gs.set_traversal(0)
+        plain = timed(sil_run(gs, sph, flip, out, n))
+        gs.set_traversal(4, 8, sort_queries=True)  # queries sorted spatially, same traversal
+        fast = timed(sil_run(gs, sph, flip, out, n))
+        return {"plain": {"queries_per_s": n / (plain / 1e3), "ms": plain},
+                "fast": {"queries_per_s": n / (fast / 1e3), "ms": fast, "variant": "queries sorted spatially"},
+                "speedup_vs_plain": plain / fast}
+
+    times = sil_times(g2, sph, flip, out, n)
+    nodes, _, sils = s2.cpu_bvh.export()
+    zf = np.zeros(n, np.uint32)
+    cpu = cpu_rate(lambda m: O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts2[:m], R.FLT_MAX), zf[:m],
+                                               nthreads=threads), n)
+    lines.append({"config": "2D stars 131,072 segments, 8,388,608 closest-silhouette queries (flip 0)",
+                  "queries": n, **times, "cpu_baseline": cpu})
+    del g2, s2
+
+    # 3D silhouettes on the 1M-triangle torus (SNCH), 4,194,304 queries in [-2, 2]^3
+    v, f, pts = make_workload(0, N_QUERIES)
+    s = F.Scene3D()
+    s.set_object_count(1)
+    s.set_object_vertices(v, 0)
+    s.set_object_triangles(f, 0)
+    s.compute_silhouettes()
+    s.build(F.AggregateType.Bvh_SurfaceArea, False)
+    g = F.GPUScene3D("", False, device=0)
+    g.transfer_to_gpu(s)
+    n = len(pts)
+    sph = sph_tensor(pts)
+    flip = torch.zeros(n, dtype=torch.int32, device=dev)
+    out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+    times = sil_times(g, sph, flip, out, n)
+    nodes, _, sils = s.cpu_bvh.export()
+    zf = np.zeros(n, np.uint32)
+    cpu = cpu_rate(lambda m: O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pts[:m], R.FLT_MAX), zf[:m],
+                                               nthreads=threads), n)
+    lines.append({"config": "3D silhouettes, torus 1,048,576 triangles (SNCH), 4,194,304 queries (flip 0)",
+                  "queries": n, **times, "cpu_baseline": cpu})
+    for line in lines:
+        print(json.dumps(line), flush=True)
 
 
 def _schedule(c) -> str:
@@ -540,5 +732,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.suite:
+        run_suite(a)
     else:
         run_ours(a)

@@ -566,8 +566,20 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
         FCPWGB_CUDA(launchFillDefault((DevInteraction *)out, n, st));
         return FCPWGB_OK;
     }
-    FCPWGB_CUDA(launchSilhouetteBinary(s->view(), (const DevSphere *)spheres, flip, (DevInteraction *)out, n,
-                                       sq_min_r, precision, st));
+    const DevSphere *q = (const DevSphere *)spheres;
+    const uint32_t *perm = nullptr;
+    if (s->useWide() && s->wideConfig.sortQueries && n >= 4096) {
+        // with a fast-path configuration the queries are sorted spatially first;
+        // each query's traversal, and so its result, is unchanged
+        if ((rc = s->sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;
+        if ((rc = s->sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
+        if ((rc = s->sortSpheres.ensure((size_t)n * sizeof(DevSphere)))) return rc;
+        FCPWGB_CUDA(launchSortQueries(s->sortLimits(), q, n, (uint32_t *)s->sortCells.ptr,
+                                      (DevSphere *)s->sortSpheres.ptr, (uint32_t *)s->sortPerm.ptr, s->smCount(), st));
+        q = (const DevSphere *)s->sortSpheres.ptr;
+        perm = (const uint32_t *)s->sortPerm.ptr;
+    }
+    FCPWGB_CUDA(launchSilhouetteBinary(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st));
     return FCPWGB_OK;
 }
 

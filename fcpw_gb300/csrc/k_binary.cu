@@ -281,14 +281,16 @@ __global__ void __launch_bounds__(256) kSilhouetteBinary(const unsigned char *__
                                                          const unsigned char *__restrict__ sils,
                                                          const DevSphere *__restrict__ spheres,
                                                          const uint32_t *__restrict__ flip,
+                                                         const uint32_t *__restrict__ perm,
                                                          DevInteraction *__restrict__ out, uint32_t n,
                                                          float sqMinR, float precision, uint32_t *errorWord) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
+    const uint32_t src = perm ? __ldg(perm + q) : q;  // sorted queries: the caller's slot
     float4 s4 = ldg4(spheres + q);
     float3 c = make_float3(s4.x, s4.y, s4.z);
     float r2 = s4.w;
-    bool flipNormal = flip[q] != 0;
+    bool flipNormal = __ldg(flip + src) != 0;
     DevInteraction best = defaultInteraction();
 
     if (!(sqMinR >= r2)) {
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(256) kSilhouetteBinary(const unsigned char *__
             }
         }
     }
-    out[q] = best;
+    out[src] = best;
 }
 
 // ------------------------------------------------------------ launchers
@@ -410,12 +412,12 @@ cudaError_t launchSphereSampleBinary(const SceneView &v, const DevSphere *sphere
 }
 
 cudaError_t launchSilhouetteBinary(const SceneView &v, const DevSphere *spheres, const uint32_t *flip,
-                                   DevInteraction *out, uint32_t n, float sqMinR, float precision,
-                                   cudaStream_t s) {
+                                   const uint32_t *perm, DevInteraction *out, uint32_t n, float sqMinR,
+                                   float precision, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     dim3 g(blocksFor(n, 256)), b(256);
-    if (v.dim == 3) kSilhouetteBinary<EdgeSil, 3><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, out, n, sqMinR, precision, v.errorWord);
-    else kSilhouetteBinary<VertexSil, 2><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, out, n, sqMinR, precision, v.errorWord);
+    if (v.dim == 3) kSilhouetteBinary<EdgeSil, 3><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR, precision, v.errorWord);
+    else kSilhouetteBinary<VertexSil, 2><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR, precision, v.errorWord);
     return cudaGetLastError();
 }
 

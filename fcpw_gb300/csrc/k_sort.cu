@@ -1,6 +1,6 @@
 // Spatial reordering of query batches and record packing for the wide kernels.
 //
-// Queries are bucketed by a Morton-ordered cell of a 2^18-cell grid (64^3 in
+// Queries (sphere centres, ray origins) are bucketed by a Morton-ordered cell of a 2^18-cell grid (64^3 in
 // 3D, 512^2 in 2D) and counting-sorted (histogram, exclusive scan, scatter).
 // The grid spans the bounding box of the batch's own query centres, clipped
 // to limits around the scene, so that cells are neither empty nor crowded
@@ -77,12 +77,32 @@ FCPWGB_D uint32_t cellOf(int dim, const CellGrid &g, float3 c) {
     return spread2(ix) | (spread2(iy) << 1);
 }
 
-// min/max of the finite query centres: a warp reduction, then one atomic per
-// warp and axis into qb (initialised to +3.4e38 / -3.4e38 by a byte memset)
-__global__ void kQueryBounds(const DevSphere *__restrict__ q, uint32_t n, int *qb) {
+// the position a record is sorted by: a sphere's centre, a ray's origin
+FCPWGB_D float3 recordPosition(const DevSphere *q, uint32_t i) {
+    float4 s = ldg4(q + i);
+    return make_float3(s.x, s.y, s.z);
+}
+FCPWGB_D float3 recordPosition(const DevRay *q, uint32_t i) {  // 40 B records: 8 B aligned
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(q + i);
+    float2 a = ldg2(p), b = ldg2(p + 8);
+    return make_float3(a.x, a.y, b.x);
+}
+FCPWGB_D void copyRecord(const DevSphere *q, uint32_t i, DevSphere *dst, uint32_t j) {
+    reinterpret_cast<float4 *>(dst)[j] = ldg4(q + i);
+}
+FCPWGB_D void copyRecord(const DevRay *q, uint32_t i, DevRay *dst, uint32_t j) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(q + i);
+    float2 *d = reinterpret_cast<float2 *>(dst + j);
+#pragma unroll
+    for (int k = 0; k < 5; k++) d[k] = ldg2(p + 8 * k);
+}
+
+// min/max of the finite record positions: a warp reduction, then one atomic
+// per warp and axis into qb (initialised to +3.4e38 / -3.4e38 by a byte memset)
+template<class Rec> __global__ void kQueryBounds(const Rec *__restrict__ q, uint32_t n, int *qb) {
     float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 s = ldg4(q + i);
+        float3 s = recordPosition(q, i);
         float v[3] = {s.x, s.y, s.z};
 #pragma unroll
         for (int a = 0; a < 3; a++) {
@@ -108,30 +128,31 @@ __global__ void kQueryBounds(const DevSphere *__restrict__ q, uint32_t n, int *q
     }
 }
 
-__global__ void kCellHistogram(SortLimits lim, const int *qb, const DevSphere *__restrict__ q, uint32_t n,
+template<class Rec>
+__global__ void kCellHistogram(SortLimits lim, const int *qb, const Rec *__restrict__ q, uint32_t n,
                                uint32_t *cells) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     CellGrid g = cellGrid(lim, qb);
-    float4 s = ldg4(q + i);
-    atomicAdd(cells + cellOf(lim.dim, g, make_float3(s.x, s.y, s.z)), 1u);
+    atomicAdd(cells + cellOf(lim.dim, g, recordPosition(q, i)), 1u);
 }
 
-__global__ void kScatterQueries(SortLimits lim, const int *qb, const DevSphere *__restrict__ q, uint32_t n,
-                                uint32_t *cells, DevSphere *sorted, uint32_t *perm) {
+template<class Rec>
+__global__ void kScatterQueries(SortLimits lim, const int *qb, const Rec *__restrict__ q, uint32_t n,
+                                uint32_t *cells, Rec *sorted, uint32_t *perm) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     CellGrid g = cellGrid(lim, qb);
-    float4 s = ldg4(q + i);
-    uint32_t pos = atomicAdd(cells + cellOf(lim.dim, g, make_float3(s.x, s.y, s.z)), 1u);
-    reinterpret_cast<float4 *>(sorted)[pos] = s;
+    uint32_t pos = atomicAdd(cells + cellOf(lim.dim, g, recordPosition(q, i)), 1u);
+    copyRecord(q, i, sorted, pos);
     perm[pos] = i;
 }
 
 cudaError_t scanCounts(uint32_t *cells, uint32_t nCells, uint32_t *tileSums, cudaStream_t s);
 
-cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, uint32_t n, uint32_t *cells,
-                              DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s) {
+template<class Rec>
+cudaError_t sortRecords(const SortLimits &lim, const Rec *recs, uint32_t n, uint32_t *cells, Rec *sorted,
+                        uint32_t *perm, int numSMs, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     int *qb = reinterpret_cast<int *>(cells + kSortCells);
     cudaError_t e = cudaMemsetAsync(cells, 0, sizeof(uint32_t) * kSortCells, s);
@@ -139,11 +160,21 @@ cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, u
     if (e == cudaSuccess) e = cudaMemsetAsync(qb + 3, 0x80, 3 * sizeof(int), s);
     if (e != cudaSuccess) return e;
     uint32_t blocks = (n + 255) / 256;
-    kQueryBounds<<<std::min<uint32_t>(blocks, (uint32_t)std::max(numSMs, 1) * 8u), 256, 0, s>>>(spheres, n, qb);
-    kCellHistogram<<<blocks, 256, 0, s>>>(lim, qb, spheres, n, cells);
+    kQueryBounds<Rec><<<std::min<uint32_t>(blocks, (uint32_t)std::max(numSMs, 1) * 8u), 256, 0, s>>>(recs, n, qb);
+    kCellHistogram<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells);
     if ((e = scanCounts(cells, kSortCells, cells + kSortCells + 8, s)) != cudaSuccess) return e;
-    kScatterQueries<<<blocks, 256, 0, s>>>(lim, qb, spheres, n, cells, sorted, perm);
+    kScatterQueries<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, sorted, perm);
     return cudaGetLastError();
+}
+
+cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, uint32_t n, uint32_t *cells,
+                              DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s) {
+    return sortRecords(lim, spheres, n, cells, sorted, perm, numSMs, s);
+}
+
+cudaError_t launchSortRays(const SortLimits &lim, const DevRay *rays, uint32_t n, uint32_t *cells, DevRay *sorted,
+                           uint32_t *perm, int numSMs, cudaStream_t s) {
+    return sortRecords(lim, rays, n, cells, sorted, perm, numSMs, s);
 }
 
 // ---------------------------------------------------------------- batches

@@ -28,8 +28,12 @@ struct Tri48Prim {
         return closestPointTriangle(pa, pb, pc, x, p, uv);
     }
     FCPWGB_D float3 normal() const { return normalize3(cross3(pb - pa, pc - pa)); }
+    FCPWGB_D bool intersect(const DevRay &r, bool occl, DevInteraction &i) const {
+        return intersectTriangle(pa, pb, pc, r, occl, i);
+    }
     // FP64 distance and closest point, vertices taken relative to the query
-    FCPWGB_D double refine(float3 x, float3 &pOut) const {
+    // (not inlined: its FP64 registers stay out of the traversal loop)
+    __device__ __noinline__ double refine(float3 x, float3 &pOut) const {
         double ax = (double)pa.x - x.x, ay = (double)pa.y - x.y, az = (double)pa.z - x.z;
         double bx = (double)pb.x - x.x, by = (double)pb.y - x.y, bz = (double)pb.z - x.z;
         double cx = (double)pc.x - x.x, cy = (double)pc.y - x.y, cz = (double)pc.z - x.z;
@@ -71,7 +75,7 @@ struct Seg24Prim : SegPrim {
         s.pa = b.pa; s.pb = b.pb; s.index = b.index;
         return s;
     }
-    FCPWGB_D double refine(float3 x, float3 &pOut) const {
+    __device__ __noinline__ double refine(float3 x, float3 &pOut) const {
         double ax = (double)pa.x - x.x, ay = (double)pa.y - x.y;
         double ux = (double)pb.x - pa.x, uy = (double)pb.y - pa.y;
         double c1 = -(ux * ax + uy * ay), c2 = ux * ux + uy * uy, px, py;
@@ -223,22 +227,76 @@ struct WideStack {
     FCPWGB_D uint32_t ref(int sp) const { return sp < kShortStack ? sRef[sp * kWideBlock] : lRef[sp - kShortStack]; }
 };
 
+// Traversal statistics (expansions, tests, warp loads): compiled in only for
+// the counting launches, so the timed kernels carry no counter registers.
+template<bool ON> struct Count {
+    FCPWGB_D void add(uint32_t) {}
+    FCPWGB_D unsigned long long get() const { return 0; }
+};
+template<> struct Count<true> {
+    uint32_t v = 0;
+    FCPWGB_D void add(uint32_t x) { v += x; }
+    FCPWGB_D unsigned long long get() const { return v; }
+};
+
+// Near ties of the precise mode. The FP32 traversal picks its winner with the
+// reference's rounding, but a primitive whose FP32 distance lies within the
+// rounding band of the winner's may be the closer one in exact arithmetic.
+// So the precise mode prunes boxes against the winner's distance plus that
+// band, keeps the best primitive within the band other than the winner (the
+// runner-up), and refines both in FP64 at the end. The band, 8 units of
+// 2^-24 times (|c|_inf + d), bounds the FP32 error of a point-primitive
+// distance with coordinates of magnitude |c| + d. Without it, near-tied
+// segments of a polyline gave 7.5e-7 relative error on 1024 2D samples.
+constexpr float kBandEps = 8.0f * 5.9604645e-8f;
+template<bool TRACK> struct NearTie {  // off: no state
+    FCPWGB_D float prune(float r2, float3) const { return r2; }
+    FCPWGB_D float pruneHit(float d, float3) const { return d * d; }
+    FCPWGB_D void replaced(float, uint32_t) {}
+    FCPWGB_D void offer(float, uint32_t) {}
+};
+FCPWGB_D float tieBand(float3 c, float d) { return kBandEps * (fmax3(fabsf(c.x), fabsf(c.y), fabsf(c.z)) + d); }
+template<> struct NearTie<true> {  // two registers; the band is recomputed from the query when needed
+    float d2nd = kFltMax;
+    uint32_t sel2nd = kUintMax;
+    FCPWGB_D float pruneHit(float d, float3 c) const {
+        float t = d + tieBand(c, d);
+        return t * t;
+    }
+    FCPWGB_D float prune(float r2, float3 c) const { return pruneHit(sqrtf(r2), c); }
+    // the previous winner becomes the runner-up when a primitive beats it
+    FCPWGB_D void replaced(float d, uint32_t sel) {
+        d2nd = d;
+        sel2nd = sel;
+    }
+    // a primitive that did not beat the winner (the caller's radius is checked at the end)
+    FCPWGB_D void offer(float d, uint32_t sel) {
+        if (d < d2nd) {
+            d2nd = d;
+            sel2nd = sel;
+        }
+    }
+};
+
 // Closest point of one query on a wide tree (bvh.slang:395-502 semantics:
 // inclusive d2Min <= r2 pruning, r2 shrunk by child d2Max, primitives accepted
 // when d*d <= r2, the later of equal distances wins).
 // `root` is the tree's root record (always an inner record); `found`/`best`/
 // `selected`/`r2` may arrive holding a candidate already tested (a seed).
-template<int W, int BITS, class Prim>
+// Boxes are pruned against rp2: r2, or with TRACK r2 widened by the band.
+template<int W, int BITS, class Prim, bool TRACK, bool STATS>
 FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigned char *__restrict__ prims,
                           uint32_t root, float3 c, float r2, bool found, DevInteraction &best, uint32_t &selected,
-                          WideStack &st, uint32_t *errorWord, uint32_t &nExpanded, uint32_t &nTests) {
+                          NearTie<TRACK> &tie, WideStack &st, uint32_t *errorWord, Count<STATS> &nExpanded,
+                          Count<STATS> &nTests) {
     int sp = 0;
     uint32_t cur = root;
     WideNodeRegs<W, BITS> node;
+    float rp2 = found ? tie.pruneHit(best.d, c) : tie.prune(r2, c);
     for (;;) {
         if (!(cur & kLeafBit)) {
             node.load(nodes, cur);
-            nExpanded++;
+            nExpanded.add(1);
             constexpr uint32_t kSlotMask = W - 1;
             float d2Min[W];
             childD2Min<W, BITS>(node, c, d2Min);
@@ -249,15 +307,16 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
 #pragma unroll
                 for (int k = 0; k < W; k++)
                     if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
+                rp2 = tie.prune(r2, c);
             }
             // keys: distance bits with the slot in the low bits, truncating the
-            // distance downwards (visits are decided on d2Min <= r2, so a smaller
+            // distance downwards (visits are decided on d2Min <= rp2, so a smaller
             // stored distance can only add visits, never skip one)
             uint32_t key[W];
             int nh = 0;
 #pragma unroll
             for (int k = 0; k < W; k++) {
-                bool hit = node.cnt(k) != kWideEmpty && d2Min[k] <= r2;
+                bool hit = node.cnt(k) != kWideEmpty && d2Min[k] <= rp2;
                 key[k] = hit ? ((__float_as_uint(d2Min[k]) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
                 nh += hit ? 1 : 0;
             }
@@ -286,14 +345,16 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
             }
         } else {
             uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
-            nTests += cnt;
+            nTests.add(cnt);
             for (uint32_t p = 0; p < cnt; p++) {
                 Prim prim = Prim::load(prims, off + p);
                 float3 pt;
                 float2 uv;
                 float d = prim.closestPoint(c, pt, uv);
                 if (d * d <= r2) {
+                    if (found) tie.replaced(best.d, selected);
                     r2 = fminf(r2, d * d);
+                    rp2 = tie.pruneHit(d, c);
                     best.p = pt;
                     best.n = make_float3(0.f, 0.f, 0.f);
                     best.uv = uv;
@@ -301,13 +362,15 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
                     best.index = prim.index;
                     selected = off + p;
                     found = true;
+                } else {
+                    tie.offer(d, off + p);
                 }
             }
         }
         bool next = false;
         while (sp > 0) {
             sp--;
-            if (st.dist(sp) <= r2) {
+            if (st.dist(sp) <= rp2) {
                 cur = st.ref(sp);
                 next = true;
                 break;
@@ -318,17 +381,34 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
     return found;
 }
 
-// Final record of query i: FP64 distance of the winning primitive (PRECISE),
+// Final record of query i: FP64 distance of the winning primitive (PRECISE;
+// with a runner-up within the rounding band, the closer of the two in FP64),
 // its face normal (recordNormal), written to the caller's slot.
 template<class Prim, bool PRECISE>
 FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_t *__restrict__ perm,
-                          DevInteraction *__restrict__ out, uint32_t i, float3 c, bool found, uint32_t selected,
-                          int recordNormal, DevInteraction &best) {
+                          DevInteraction *__restrict__ out, uint32_t i, float3 c, float r2User, bool found,
+                          uint32_t selected, int recordNormal, DevInteraction &best, const NearTie<PRECISE> &tie) {
     if (found) {
         Prim prim = Prim::load(prims, selected);
-        if (PRECISE) {
+        if constexpr (PRECISE) {
             float3 p;
             double d = prim.refine(c, p);
+            if (tie.sel2nd != kUintMax && tie.d2nd <= best.d + tieBand(c, best.d) &&
+                tie.d2nd * tie.d2nd <= r2User) {
+                Prim q = Prim::load(prims, tie.sel2nd);
+                float3 p2;
+                double d2 = q.refine(c, p2);
+                if (d2 < d) {
+                    float3 pt;
+                    float2 uv;
+                    q.closestPoint(c, pt, uv);
+                    d = d2;
+                    p = p2;
+                    best.uv = uv;
+                    best.index = q.index;
+                    prim = q;
+                }
+            }
             best.d = (float)d;
             best.p = p;
         }
@@ -348,7 +428,7 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
 // radius instead of FLT_MAX. Any tested primitive is a valid candidate, so the
 // result is the same closest distance (ties may pick another primitive).
 constexpr uint32_t kWidePool = 256;
-template<int W, int BITS, class Prim, bool PRECISE, bool PERSISTENT>
+template<int W, int BITS, class Prim, bool PRECISE, bool PERSISTENT, bool STATS>
 __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigned char *__restrict__ nodes,
                                                                 const unsigned char *__restrict__ prims,
                                                                 const DevSphere *__restrict__ spheres,
@@ -362,7 +442,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
     WideStack st;
     st.sRef = sRef + threadIdx.x;
     st.sD = sD + threadIdx.x;
-    uint32_t tExp = 0, tTests = 0;
+    Count<STATS> tExp, tTests;
     if (!PERSISTENT) {
         uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
         if (i < n) {
@@ -371,9 +451,10 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
             DevInteraction best = defaultInteraction();
             uint32_t selected = kUintMax;
             uint32_t root = roots ? __ldg(roots + i) : 0u;
-            bool found = wideClosest<W, BITS, Prim>(nodes, prims, root, c, s4.w, false, best, selected, st, errorWord,
-                                                    tExp, tTests);
-            finishQuery<Prim, PRECISE>(prims, perm, out, i, c, found, selected, recordNormal, best);
+            NearTie<PRECISE> tie;
+            bool found = wideClosest<W, BITS, Prim, PRECISE, STATS>(nodes, prims, root, c, s4.w, false, best, selected, tie,
+                                                             st, errorWord, tExp, tTests);
+            finishQuery<Prim, PRECISE>(prims, perm, out, i, c, s4.w, found, selected, recordNormal, best, tie);
         }
     } else {
         const uint32_t lane = threadIdx.x & 31u;
@@ -393,12 +474,13 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                 uint32_t selected = kUintMax;
                 uint32_t root = roots ? __ldg(roots + i) : 0u;
                 bool found = false;
+                NearTie<PRECISE> tie;
                 if (seed != kUintMax && seedRoot == root) {
                     Prim prim = Prim::load(prims, seed);
                     float3 pt;
                     float2 uv;
                     float d = prim.closestPoint(c, pt, uv);
-                    tTests++;
+                    tTests.add(1);
                     if (d * d <= r2) {
                         r2 = d * d;
                         best.p = pt;
@@ -409,17 +491,17 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                         found = true;
                     }
                 }
-                found = wideClosest<W, BITS, Prim>(nodes, prims, root, c, r2, found, best, selected, st, errorWord,
-                                                   tExp, tTests);
+                found = wideClosest<W, BITS, Prim, PRECISE, STATS>(nodes, prims, root, c, r2, found, best, selected, tie,
+                                                            st, errorWord, tExp, tTests);
                 seed = found ? selected : kUintMax;
                 seedRoot = root;
-                finishQuery<Prim, PRECISE>(prims, perm, out, i, c, found, selected, recordNormal, best);
+                finishQuery<Prim, PRECISE>(prims, perm, out, i, c, s4.w, found, selected, recordNormal, best, tie);
             }
         }
     }
-    if (stats) {
-        atomicAdd(stats + 1, (unsigned long long)tExp);
-        atomicAdd(stats + 2, (unsigned long long)tTests);
+    if (STATS && stats) {
+        atomicAdd(stats + 1, tExp.get());
+        atomicAdd(stats + 2, tTests.get());
     }
 }
 
@@ -434,7 +516,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
 // entry is popped. Queries of a warp that start at different roots (a forest
 // whose scene boundary falls inside the warp) are walked one root at a time.
 constexpr int kPacketShort = 32;  // warp-stack entries held in shared memory
-template<int W, int BITS, class Prim, bool PRECISE>
+template<int W, int BITS, class Prim, bool PRECISE, bool STATS>
 __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const unsigned char *__restrict__ nodes,
                                                                       const unsigned char *__restrict__ prims,
                                                                       const DevSphere *__restrict__ spheres,
@@ -464,7 +546,10 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
     DevInteraction best = defaultInteraction();
     uint32_t selected = kUintMax;
     bool found = false;
-    uint32_t tExp = 0, tTests = 0, tVisits = 0, tPrimLoads = 0;
+    NearTie<PRECISE> tie;
+    const float r2User = r2;
+    float rp2 = tie.prune(r2, c);  // pruning radius^2 (NaN for a lane without a query)
+    Count<STATS> tExp, tTests, tVisits, tPrimLoads;
     WideNodeRegs<W, BITS> node;
 
     uint32_t pending = __ballot_sync(0xffffffffu, valid);
@@ -479,15 +564,16 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
             bool descend = false;
             if (!(cur & kLeafBit)) {
                 node.load(nodes, cur);
-                tVisits++;
+                tVisits.add(1);
                 float d2Min[W];
                 childD2Min<W, BITS>(node, c, d2Min);
                 if (act) {
-                    tExp++;
+                    tExp.add(1);
                     if (!found) {
 #pragma unroll
                         for (int k = 0; k < W; k++)
                             if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
+                        rp2 = tie.prune(r2, c);
                     }
                 }
                 // children needed by any lane, ordered by the first active lane's distances
@@ -496,7 +582,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                 int nh = 0;
 #pragma unroll
                 for (int k = 0; k < W; k++) {
-                    bool need = act && node.cnt(k) != kWideEmpty && d2Min[k] <= r2;
+                    bool need = act && node.cnt(k) != kWideEmpty && d2Min[k] <= rp2;
                     bool any = __ballot_sync(0xffffffffu, need) != 0;
                     float lead = __shfl_sync(0xffffffffu, d2Min[k], leader);
                     key[k] = any ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
@@ -510,7 +596,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                     }
                     uint32_t refs[W];
                     childRefs<W, BITS>(node, refs);
-                    // a lane out of this record is out of its children too (NaN is never <= r2)
+                    // a lane out of this record is out of its children too (NaN is never <= rp2)
                     float mine[W];
 #pragma unroll
                     for (int s = 0; s < W; s++) mine[s] = act ? d2Min[s] : __int_as_float(0x7fc00000);
@@ -522,7 +608,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                             float dl = selectBySlot<W>(mine, slot);
                             if (k == 0) {
                                 cur = packed;
-                                act = dl <= r2;
+                                act = dl <= rp2;
                             } else {
                                 if (sp < kPacketShort) {
                                     if (lane == 0) sRef[warp][sp] = packed;
@@ -540,8 +626,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                 }
             } else {
                 uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
-                tPrimLoads += cnt;
-                if (act) tTests += cnt;
+                tPrimLoads.add(cnt);
+                if (act) tTests.add(cnt);
                 for (uint32_t p = 0; p < cnt; p++) {
                     Prim prim = Prim::load(prims, off + p);
                     if (act) {
@@ -549,7 +635,9 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                         float2 uv;
                         float d = prim.closestPoint(c, pt, uv);
                         if (d * d <= r2) {
+                            if (found) tie.replaced(best.d, selected);
                             r2 = fminf(r2, d * d);
+                            rp2 = tie.pruneHit(d, c);
                             best.p = pt;
                             best.n = make_float3(0.f, 0.f, 0.f);
                             best.uv = uv;
@@ -557,6 +645,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                             best.index = prim.index;
                             selected = off + p;
                             found = true;
+                        } else {
+                            tie.offer(d, off + p);
                         }
                     }
                 }
@@ -575,7 +665,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                     ref = lRef[sp - kPacketShort];
                     dl = lDist[sp - kPacketShort];
                 }
-                act = dl <= r2;
+                act = dl <= rp2;
                 if (__ballot_sync(0xffffffffu, act)) {
                     cur = ref;
                     next = true;
@@ -586,12 +676,118 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
             if (!next) break;
         }
     }
-    if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, i, c, found, selected, recordNormal, best);
-    if (stats) {
+    if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, i, c, r2User, found, selected, recordNormal, best, tie);
+    if (STATS && stats) {
         if (lane == 0) {
-            atomicAdd(stats + 3, (unsigned long long)tVisits);
-            atomicAdd(stats + 4, (unsigned long long)tPrimLoads);
+            atomicAdd(stats + 3, tVisits.get());
+            atomicAdd(stats + 4, tPrimLoads.get());
         }
+        atomicAdd(stats + 1, tExp.get());
+        atomicAdd(stats + 2, tTests.get());
+    }
+}
+
+// Ray first hit / occlusion on a wide tree, one thread per ray, with the
+// semantics of bvh.slang:144-254: a child is entered when the slab test with
+// the parallel-slab guard passes against the current tMax, nearest entry
+// first; a stacked child is skipped when its entry distance exceeds tMax;
+// hits are accepted when 0 <= t <= tMax (a later equal t wins), and an
+// occlusion query stops at its first hit.
+template<int W, int BITS, class Prim>
+__global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *__restrict__ nodes,
+                                                       const unsigned char *__restrict__ prims,
+                                                       const DevRay *__restrict__ rays,
+                                                       const uint32_t *__restrict__ perm,
+                                                       DevInteraction *__restrict__ out, uint32_t n, int occl,
+                                                       uint32_t *errorWord, unsigned long long *stats) {
+    constexpr uint32_t kSlotMask = W - 1;
+    __shared__ uint32_t sRef[kShortStack * kWideBlock];
+    __shared__ float sD[kShortStack * kWideBlock];
+    WideStack st;
+    st.sRef = sRef + threadIdx.x;
+    st.sD = sD + threadIdx.x;
+    const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
+    if (i >= n) return;
+    const unsigned char *rp = reinterpret_cast<const unsigned char *>(rays + i);
+    float2 a = ldg2(rp), b = ldg2(rp + 8), cc = ldg2(rp + 16), d = ldg2(rp + 24), e = ldg2(rp + 32);
+    DevRay r;
+    r.o = make_float3(a.x, a.y, b.x);
+    r.d = make_float3(b.y, cc.x, cc.y);
+    r.dInv = make_float3(d.x, d.y, e.x);
+    r.tMax = e.y;
+    DevInteraction best = defaultInteraction();
+    uint32_t tExp = 0, tTests = 0;
+    WideNodeRegs<W, BITS> node;
+    uint32_t cur = 0;
+    int sp = 0;
+    bool done = false;
+    while (!done) {
+        if (!(cur & kLeafBit)) {
+            node.load(nodes, cur);
+            tExp++;
+            uint32_t key[W];
+            int nh = 0;
+#pragma unroll
+            for (int k = 0; k < W; k++) {
+                float t0, t1;
+                bool hit = node.cnt(k) != kWideEmpty &&
+                           boxRayIntersect(make_float3(node.bound(0, k), node.bound(1, k), node.bound(2, k)),
+                                           make_float3(node.bound(3, k), node.bound(4, k), node.bound(5, k)), r, t0,
+                                           t1);
+                // entry distances are >= 0 (+ 0 turns a -0 into +0), so their bits sort as integers
+                key[k] = hit ? ((__float_as_uint(t0 + 0.0f) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
+                nh += hit ? 1 : 0;
+            }
+            sortNetwork<W>(key);
+            if (nh > 0) {
+                if (sp + nh - 1 > kWideStack) {
+                    atomicOr(errorWord, kErrStackOverflow);
+                    break;
+                }
+                uint32_t refs[W];
+                childRefs<W, BITS>(node, refs);
+#pragma unroll
+                for (int k = W - 1; k >= 1; k--) {
+                    if (k < nh) {
+                        st.push(sp, selectBySlot<W>(refs, key[k] & kSlotMask), __uint_as_float(key[k] & ~kSlotMask));
+                        sp++;
+                    }
+                }
+                cur = selectBySlot<W>(refs, key[0] & kSlotMask);
+                continue;
+            }
+        } else {
+            uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+            tTests += cnt;
+            for (uint32_t p = 0; p < cnt; p++) {
+                Prim prim = Prim::load(prims, off + p);
+                DevInteraction c = defaultInteraction();
+                if (prim.intersect(r, occl != 0, c)) {
+                    c.index = prim.index;
+                    if (occl) {
+                        best.index = c.index;
+                        done = true;
+                        break;
+                    }
+                    r.tMax = fminf(r.tMax, c.d);
+                    best = c;
+                }
+            }
+            if (done) break;
+        }
+        bool next = false;
+        while (sp > 0) {
+            sp--;
+            if (st.dist(sp) <= r.tMax) {
+                cur = st.ref(sp);
+                next = true;
+                break;
+            }
+        }
+        if (!next) break;
+    }
+    out[perm ? __ldg(perm + i) : i] = best;
+    if (stats) {
         atomicAdd(stats + 1, (unsigned long long)tExp);
         atomicAdd(stats + 2, (unsigned long long)tTests);
     }
@@ -624,48 +820,60 @@ __global__ void kRequantize(unsigned char *wideNodes, const int32_t *childBinary
     for (int k = 0; k < WideLayout<W, BITS>::kSize; k++) dst[k] = rec[k];
 }
 
-template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
+template<int W, int B, class Prim, bool PRECISE, bool STATS>
+cudaError_t launchWideClosestKernel(const WideLaunch &l, cudaStream_t s) {
+    dim3 g(l.grid), b(kWideBlock);
+    if (l.packet)
+        kWidePacketClosestPoint<W, B, Prim, PRECISE, STATS><<<g, b, 0, s>>>(
+            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.errorWord, l.stats);
+    else if (l.counter)
+        kWideClosestPoint<W, B, Prim, PRECISE, true, STATS><<<g, b, 0, s>>>(
+            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats);
+    else
+        kWideClosestPoint<W, B, Prim, PRECISE, false, STATS><<<g, b, 0, s>>>(
+            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats);
+    return cudaGetLastError();
+}
+template<int W, int B, class Prim>
+cudaError_t launchWideClosestPrim(bool precise, const WideLaunch &l, cudaStream_t s) {
+    if (precise)
+        return l.stats ? launchWideClosestKernel<W, B, Prim, true, true>(l, s)
+                       : launchWideClosestKernel<W, B, Prim, true, false>(l, s);
+    return l.stats ? launchWideClosestKernel<W, B, Prim, false, true>(l, s)
+                   : launchWideClosestKernel<W, B, Prim, false, false>(l, s);
+}
+template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s) {
+    if (dim == 3) {
+        if (bits == 8) return launchWideClosestPrim<W, 8, Tri48Prim>(precise, l, s);
+        if (bits == 16) return launchWideClosestPrim<W, 16, Tri48Prim>(precise, l, s);
+        return launchWideClosestPrim<W, 32, Tri48Prim>(precise, l, s);
+    }
+    if (bits == 8) return launchWideClosestPrim<W, 8, Seg24Prim>(precise, l, s);
+    if (bits == 16) return launchWideClosestPrim<W, 16, Seg24Prim>(precise, l, s);
+    return launchWideClosestPrim<W, 32, Seg24Prim>(precise, l, s);
+}
 template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes, const int32_t *childBinary,
                                               const unsigned char *binNodes, int binStride, uint32_t nWide,
                                               uint32_t *errorWord, cudaStream_t s);
 
 #define FCPWGB_WIDE_INSTANTIATE(W)                                                                                \
-    template<> cudaError_t launchWideClosestT<W>(int bits, int dim, bool precise, const WideLaunch &l,             \
-                                                 cudaStream_t s) {                                                 \
-        dim3 g(l.grid), b(128);                                                                                    \
-        _Pragma("nv_diag_suppress 177")                                                                            \
+    template cudaError_t launchWideClosestT<W>(int bits, int dim, bool precise, const WideLaunch &l,              \
+                                               cudaStream_t s);                                                   \
+    template<> cudaError_t launchWideRayT<W>(int bits, int dim, const WideRayLaunch &l, cudaStream_t s) {         \
+        if (l.n == 0) return cudaSuccess;                                                                          \
+        dim3 g((l.n + 127) / 128), b(128);                                                                         \
         auto go = [&](auto kern) {                                                                                 \
-            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal,         \
-                                 l.counter, l.errorWord, l.stats);                                                 \
+            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.errorWord, l.stats);     \
         };                                                                                                         \
-        auto goPacket = [&](auto kern) {                                                                           \
-            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal,         \
-                                 l.errorWord, l.stats);                                                            \
-        };                                                                                                         \
-        auto pick = [&](auto bitsConst) {                                                                          \
-            constexpr int B = decltype(bitsConst)::value;                                                          \
-            const bool p = l.counter != nullptr;                                                                   \
-            if (l.packet) {                                                                                        \
-                if (dim == 3) {                                                                                    \
-                    if (precise) goPacket(kWidePacketClosestPoint<W, B, Tri48Prim, true>);                         \
-                    else goPacket(kWidePacketClosestPoint<W, B, Tri48Prim, false>);                                \
-                } else {                                                                                           \
-                    if (precise) goPacket(kWidePacketClosestPoint<W, B, Seg24Prim, true>);                         \
-                    else goPacket(kWidePacketClosestPoint<W, B, Seg24Prim, false>);                                \
-                }                                                                                                  \
-                return;                                                                                            \
-            }                                                                                                      \
-            if (dim == 3) {                                                                                        \
-                if (precise) { if (p) go(kWideClosestPoint<W, B, Tri48Prim, true, true>); else go(kWideClosestPoint<W, B, Tri48Prim, true, false>); } \
-                else { if (p) go(kWideClosestPoint<W, B, Tri48Prim, false, true>); else go(kWideClosestPoint<W, B, Tri48Prim, false, false>); } \
-            } else {                                                                                               \
-                if (precise) { if (p) go(kWideClosestPoint<W, B, Seg24Prim, true, true>); else go(kWideClosestPoint<W, B, Seg24Prim, true, false>); } \
-                else { if (p) go(kWideClosestPoint<W, B, Seg24Prim, false, true>); else go(kWideClosestPoint<W, B, Seg24Prim, false, false>); } \
-            }                                                                                                      \
-        };                                                                                                         \
-        if (bits == 8) pick(std::integral_constant<int, 8>());                                                     \
-        else if (bits == 16) pick(std::integral_constant<int, 16>());                                              \
-        else pick(std::integral_constant<int, 32>());                                                              \
+        if (dim == 3) {                                                                                            \
+            if (bits == 8) go(kWideRay<W, 8, Tri48Prim>);                                                          \
+            else if (bits == 16) go(kWideRay<W, 16, Tri48Prim>);                                                   \
+            else go(kWideRay<W, 32, Tri48Prim>);                                                                   \
+        } else {                                                                                                   \
+            if (bits == 8) go(kWideRay<W, 8, Seg24Prim>);                                                          \
+            else if (bits == 16) go(kWideRay<W, 16, Seg24Prim>);                                                   \
+            else go(kWideRay<W, 32, Seg24Prim>);                                                                   \
+        }                                                                                                          \
         return cudaGetLastError();                                                                                 \
     }                                                                                                              \
     template<> cudaError_t launchRequantizeT<W>(int bits, unsigned char *wideNodes, const int32_t *childBinary,    \

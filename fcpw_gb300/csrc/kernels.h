@@ -29,9 +29,10 @@ cudaError_t launchRayBinary(const SceneView &v, const DevRay *rays, DevInteracti
                             cudaStream_t s);
 cudaError_t launchSphereSampleBinary(const SceneView &v, const DevSphere *spheres, const float3 *randNums,
                                      DevInteraction *out, uint32_t n, cudaStream_t s);
+// perm: sorted position -> caller query (spheres sorted, flip and out in caller order), or NULL
 cudaError_t launchSilhouetteBinary(const SceneView &v, const DevSphere *spheres, const uint32_t *flip,
-                                   DevInteraction *out, uint32_t n, float sqMinR, float precision,
-                                   cudaStream_t s);
+                                   const uint32_t *perm, DevInteraction *out, uint32_t n, float sqMinR,
+                                   float precision, cudaStream_t s);
 cudaError_t launchFillDefault(DevInteraction *out, uint32_t n, cudaStream_t s);
 
 // FP64 brute-force closest distance of every query over all primitives (k_check.cu)
@@ -57,6 +58,20 @@ struct WideLaunch {
 template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
 // dispatch over W = 2, 4, 8
 cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
+// rays on the wide trees (one thread per ray)
+struct WideRayLaunch {
+    const unsigned char *nodes = nullptr;
+    const unsigned char *prims = nullptr;
+    const DevRay *rays = nullptr;           // (sorted when perm is set)
+    const uint32_t *perm = nullptr;
+    DevInteraction *out = nullptr;
+    uint32_t n = 0;
+    int occl = 0;
+    uint32_t *errorWord = nullptr;
+    unsigned long long *stats = nullptr;
+};
+template<int W> cudaError_t launchWideRayT(int bits, int dim, const WideRayLaunch &l, cudaStream_t s);
+cudaError_t launchWideRays(int W, int bits, int dim, const WideRayLaunch &l, cudaStream_t s);
 template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes, const int32_t *childBinary,
                                               const unsigned char *binNodes, int binStride, uint32_t nWide,
                                               uint32_t *errorWord, cudaStream_t s);
@@ -70,6 +85,9 @@ struct SortLimits { float3 lo; float3 hi; int dim; };
 constexpr uint32_t kSortScratchWords = kSortCells + 8 + kSortCells / 4096;
 cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, uint32_t n, uint32_t *cells,
                               DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s);
+// the same for rays, by origin
+cudaError_t launchSortRays(const SortLimits &lim, const DevRay *rays, uint32_t n, uint32_t *cells, DevRay *sorted,
+                           uint32_t *perm, int numSMs, cudaStream_t s);
 cudaError_t launchPackTri48(const DevTriangle *tris, uint32_t n, float4 *out, cudaStream_t s);
 
 // batches of scenes: per-scene sort grid (cells cellBase .. cellBase + 2^(dim*bits))

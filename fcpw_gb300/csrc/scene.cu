@@ -15,6 +15,14 @@ cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch 
     }
 }
 
+cudaError_t launchWideRays(int W, int bits, int dim, const WideRayLaunch &l, cudaStream_t s) {
+    switch (W) {
+        case 2: return launchWideRayT<2>(bits, dim, l, s);
+        case 4: return launchWideRayT<4>(bits, dim, l, s);
+        default: return launchWideRayT<8>(bits, dim, l, s);
+    }
+}
+
 namespace {
 cudaError_t launchRequant(int W, int bits, unsigned char *wn, const int32_t *cb, const unsigned char *bn, int stride,
                           uint32_t n, uint32_t *err, cudaStream_t s) {
@@ -53,11 +61,16 @@ int GpuScene::ensureWide(cudaStream_t st) {
     wide.nNodes = h.nNodes;
     wide.depth = h.depth;
     wide.builtFromVersion = treeVersion;
+    smCount();
+    return 0;
+}
+
+int GpuScene::smCount() {
     if (numSMs == 0) {
         cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device);
         if (numSMs <= 0) numSMs = 1;
     }
-    return 0;
+    return numSMs;
 }
 
 int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal,
@@ -80,15 +93,7 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
         if ((rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;
         if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
         if ((rc = sortSpheres.ensure((size_t)n * sizeof(DevSphere)))) return rc;
-        // the grid covers the queries, but no more than the scene box grown by
-        // twice its largest extent on every side
-        float ext = 1e-6f;
-        for (int a = 0; a < dim; a++) ext = std::max(ext, rootBox[3 + a] - rootBox[a]);
-        SortLimits g;
-        g.lo = make_float3(rootBox[0] - 2.0f * ext, rootBox[1] - 2.0f * ext, rootBox[2] - 2.0f * ext);
-        g.hi = make_float3(rootBox[3] + 2.0f * ext, rootBox[4] + 2.0f * ext, rootBox[5] + 2.0f * ext);
-        g.dim = dim;
-        if ((e = launchSortQueries(g, spheres, n, (uint32_t *)sortCells.ptr, (DevSphere *)sortSpheres.ptr,
+        if ((e = launchSortQueries(sortLimits(), spheres, n, (uint32_t *)sortCells.ptr, (DevSphere *)sortSpheres.ptr,
                                    (uint32_t *)sortPerm.ptr, numSMs, st)) != cudaSuccess)
             return cudaFail(e, "sort queries");
         l.spheres = (const DevSphere *)sortSpheres.ptr;
@@ -107,6 +112,47 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
     if ((e = launchWide(c.branching, c.bits, dim, c.precise != 0, l, st)) != cudaSuccess)
         return cudaFail(e, "wide closest point launch");
     return stats ? 0 : timeEnd(st);
+}
+
+// the sort grid covers the queries, but no more than the scene box grown by
+// twice its largest extent on every side
+SortLimits GpuScene::sortLimits() const {
+    float ext = 1e-6f;
+    for (int a = 0; a < dim; a++) ext = std::max(ext, rootBox[3 + a] - rootBox[a]);
+    SortLimits g;
+    g.lo = make_float3(rootBox[0] - 2.0f * ext, rootBox[1] - 2.0f * ext, rootBox[2] - 2.0f * ext);
+    g.hi = make_float3(rootBox[3] + 2.0f * ext, rootBox[4] + 2.0f * ext, rootBox[5] + 2.0f * ext);
+    g.dim = dim;
+    return g;
+}
+
+int GpuScene::wideRays(const DevRay *r, DevInteraction *out, uint32_t n, int occl, cudaStream_t st) {
+    int rc = ensureWide(st);
+    if (rc) return rc;
+    if (n == 0) return 0;
+    WideRayLaunch l;
+    l.nodes = (const unsigned char *)wideNodes.ptr;
+    l.prims = dim == 3 ? (const unsigned char *)widePrims.ptr : (const unsigned char *)prims.ptr;
+    l.rays = r;
+    l.out = out;
+    l.n = n;
+    l.occl = occl;
+    l.errorWord = (uint32_t *)errorWord.ptr;
+    cudaError_t e;
+    if (wideConfig.sortQueries && n >= 4096) {
+        if ((rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;
+        if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
+        if ((rc = sortRays.ensure((size_t)n * sizeof(DevRay)))) return rc;
+        if ((e = launchSortRays(sortLimits(), r, n, (uint32_t *)sortCells.ptr, (DevRay *)sortRays.ptr,
+                                (uint32_t *)sortPerm.ptr, numSMs, st)) != cudaSuccess)
+            return cudaFail(e, "sort rays");
+        l.rays = (const DevRay *)sortRays.ptr;
+        l.perm = (const uint32_t *)sortPerm.ptr;
+    }
+    if ((rc = timeStart(st))) return rc;
+    if ((e = launchWideRays(wideConfig.branching, wideConfig.bits, dim, l, st)) != cudaSuccess)
+        return cudaFail(e, "wide ray launch");
+    return timeEnd(st);
 }
 
 int GpuScene::timeStart(cudaStream_t st) {
@@ -149,6 +195,7 @@ int GpuScene::closestPointsStats(const DevSphere *spheres, DevInteraction *out, 
 }
 
 int GpuScene::rays(const DevRay *r, DevInteraction *out, uint32_t n, int occl, cudaStream_t st) {
+    if (useWide()) return wideRays(r, out, n, occl, st);
     cudaError_t e = launchRayBinary(view(), r, out, n, occl, st);
     return e == cudaSuccess ? 0 : cudaFail(e, "ray launch");
 }

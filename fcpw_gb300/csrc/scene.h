@@ -74,7 +74,7 @@ struct GpuScene {
     WideTree wide;
     DeviceBuffer wideNodes, wideChildBinary, widePrims;
     // scratch of the fast path: query sort cells / permutation / sorted copy, work counter
-    DeviceBuffer sortCells, sortPerm, sortSpheres, workCounter;
+    DeviceBuffer sortCells, sortPerm, sortSpheres, sortRays, workCounter;
     int numSMs = 0;
 
     // optional event timing of traversal launches
@@ -114,6 +114,9 @@ struct GpuScene {
     // builds (or rebuilds) the wide tree the current config asks for
     int ensureWide(cudaStream_t st);
     bool useWide() const { return wideConfig.branching > 0; }
+    int wideRays(const DevRay *rays, DevInteraction *out, uint32_t n, int occl, cudaStream_t st);
+    SortLimits sortLimits() const;
+    int smCount();  // multiprocessors of the scene's device (queried once)
     int wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal,
                     unsigned long long *stats, cudaStream_t st);
 };

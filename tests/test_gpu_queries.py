@@ -308,3 +308,22 @@ def test_fp64_brute_force_probe_matches_oracle(sphere20k, stars2d, dim):
     t = torch.from_numpy(sph.view(np.float32).reshape(-1, 4).copy()).cuda()
     d_gpu = g.closest_distances_f64_tensor(t).cpu().numpy()
     assert np.allclose(d_gpu, d_ref, rtol=1e-12, atol=1e-14)
+
+
+def test_sorted_silhouette_queries_give_identical_results(stars2d):
+    """With a fast-path configuration silhouette queries are sorted spatially
+    before the traversal; each query's traversal is unchanged, so the results
+    are bit-identical to the unsorted ones, in the caller's order."""
+    s, g = stars2d
+    n = 50000
+    pts = W.uniform_points(n, 2, -3, 3, 61)
+    flip = (W.rng(62).uniform(0, 1, n) < 0.5).astype(np.uint32)
+    r2 = np.full(n, R.FLT_MAX, np.float32)
+    g.set_traversal(0)
+    a = F.GPUInteractionList()
+    g.find_closest_silhouette_points(pts, r2, flip, a, 0.0, 1e-3)
+    g.set_traversal(4, 8, sort_queries=True)
+    b = F.GPUInteractionList()
+    g.find_closest_silhouette_points(pts, r2, flip, b, 0.0, 1e-3)
+    g.set_traversal(0)
+    assert a.array().tobytes() == b.array().tobytes()

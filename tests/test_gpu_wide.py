@@ -131,3 +131,72 @@ def test_wide_2d_segments():
     for b, q in [(4, 8), (8, 16), (2, 32)]:
         g.set_traversal(b, q, precise=False)
         compare_closest(2, prims, pts, _run(g, pts), ref, f"2D wide {b}/{q}")
+
+
+def _ray_check(got, ref_out, ref_hit, occl=False):
+    g_hit = got["index"] != R.UINT_MAX
+    mism = g_hit != ref_hit
+    # grazing rays through shared edges/vertices may flip between FP32 evaluations
+    assert mism.sum() <= max(2, int(1e-4 * len(got))), f"{mism.sum()} hit/miss disagreements"
+    both = g_hit & ref_hit
+    if not occl:
+        tol = 1e-5 * np.maximum(ref_out["d"][both], 1.0)
+        assert np.all(np.abs(got["d"][both] - ref_out["d"][both]) <= tol)
+        assert (got["index"][both] == ref_out["index"][both]).mean() > 0.999
+
+
+@pytest.mark.parametrize("branching", [2, 4, 8])
+@pytest.mark.parametrize("bits", [32, 16, 8])
+def test_wide_rays_match_oracle(torus, branching, bits):
+    """Rays on the wide trees (sorted by origin) against the reference CPU order."""
+    s, g, pts, ref, prims = torus
+    n = 60000
+    o = W.uniform_points(n, 3, -2, 2, 51)
+    d = W.uniform_directions(n, 3, 52)
+    tmax = np.full(n, R.FLT_MAX, np.float32)
+    nodes, _, _ = s.cpu_bvh.export()
+    ref_out, ref_hit = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax))
+    g.set_traversal(branching, bits, sort_queries=True)
+    out = F.GPUInteractionList()
+    g.intersect(o, d, tmax, out)
+    _ray_check(out.array(), ref_out, ref_hit)
+    out2 = F.GPUInteractionList()
+    g.intersect(o, d, tmax, out2, True)
+    ref2, hit2 = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax), occlusion=True)
+    _ray_check(out2.array(), ref2, hit2, occl=True)
+    assert g.check_errors() == 0
+
+
+def test_wide_rays_finite_tmax_unsorted_and_2d():
+    v, sg = W.star_polylines(16, 64, W.SEED_BASE + 53)
+    s = build_scene(2, v, sg)
+    g = F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    n = 30000
+    o = W.uniform_points(n, 2, -3, 3, 54)
+    d = W.uniform_directions(n, 2, 55)
+    tmax = W.rng(56).uniform(0.1, 3.0, n).astype(np.float32)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref_out, ref_hit = O.intersect_rays_bvh(2, nodes, prims, R.make_rays(o, d, tmax))
+    for cfg in [(4, 8, True), (8, 16, False), (2, 32, True)]:
+        g.set_traversal(cfg[0], cfg[1], sort_queries=cfg[2])
+        out = F.GPUInteractionList()
+        g.intersect(o, d, tmax, out)
+        _ray_check(out.array(), ref_out, ref_hit)
+
+
+@pytest.mark.parametrize("packet", [False, True])
+def test_precise_mode_near_ties_2d_within_1e6(packet):
+    """2D polylines: adjacent segments tie within FP32 rounding near shared
+    vertices; the precise mode refines the winner and the runner-up in FP64."""
+    v, sg = W.star_polylines(64, 256, W.SEED_BASE + 57)
+    s = build_scene(2, v, sg)
+    g = F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    pts = W.uniform_points(30000, 2, -3, 3, 58)
+    g.set_traversal(4, 32, sort_queries=True, precise=True, packet=packet)
+    got = _run(g, pts)
+    _, prims, _ = s.cpu_bvh.export()
+    d64, _ = O.closest_points_brute_f64(2, prims, R.make_spheres(pts, R.FLT_MAX))
+    rel = relative_error(got["d"], d64)
+    assert rel.max() <= 1e-6, f"max relative error {rel.max():.3e}"
