@@ -59,8 +59,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The maximum of x over all ranks (the slowest rank's time); x itself on one rank.
+    device: where the reduction tensor lives (the rank's GPU for NCCL, None for gloo)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # --------------------------------------------------------------- workload
 def make_workload(rank: int, n_queries: int):
+    """Weak scaling: every rank holds the whole scene and its own query set of
+    n_queries (a different seed per rank); no data is exchanged."""
     from fcpw_gb300 import workloads as W
     v, f = W.torus(*TORUS, seed=W.SEED_BASE + 2)
     pts = W.uniform_points(n_queries, 3, -2.0, 2.0, W.SEED_BASE + 2 + 1000 * (rank + 1))
@@ -616,10 +630,7 @@ def run_ours(args):
     time.sleep(0.3)
     ms, kms = timed(args.steps, args.warmup)
     fast_stats = traversal_stats(node_bytes, 48, 20, packet=bool(best.get("packet")))  # sorted query + permutation
-    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    ms_max = max_over_ranks(ms, world, dev)
     value = world * n / (ms_max / 1e3)
 
     # end to end through the host-array C ABI call (pinned host buffers, copies inside)
@@ -635,10 +646,7 @@ def run_ours(args):
         e2e_t.append(time.perf_counter() - t)
     clocks = sampler.stop()
     e2e_s = statistics.median(e2e_t)
-    e2e_t_t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(e2e_t_t, op=dist.ReduceOp.MAX)
-    e2e_value = world * n / float(e2e_t_t.item())
+    e2e_value = world * n / max_over_ranks(e2e_s, world, dev)
 
     result = None
     if rank == 0:
@@ -671,7 +679,9 @@ def run_ours(args):
                        "autotune_ms": [[c["branching"], c["bits"], _schedule(c), round(t, 4)]
                                        for c, t in table]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 40},
-            "gpu_launches": args.steps * 4,
+            # per timed step: the query-bound reduction, histogram, three scan kernels and the scatter of
+            # the spatial sort (when on), then the traversal kernel
+            "gpu_launches": args.steps * (7 if best.get("sort_queries", True) else 1),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"hbm_gbs ({peak_kind})",
                          "kernel": "kWidePacketClosestPoint" if best.get("packet") else "kWideClosestPoint",
