@@ -427,7 +427,12 @@ def run_suite(args):
 
 
 def _schedule(c) -> str:
-    return "packet" if c.get("packet") else ("persistent" if c.get("persistent") else "thread")
+    s = "packet" if c.get("packet") else ("persistent" if c.get("persistent") else "thread")
+    if c.get("leaf_size"):
+        s += f"+leaf{c['leaf_size']}"
+    if not c.get("packet") and c.get("short_stack", 16) != 16:
+        s += f"+stack{c['short_stack']}"
+    return s
 
 
 def batched_scenes_bench(device_index: int, reps: int = 5):
@@ -465,7 +470,8 @@ def batched_scenes_bench(device_index: int, reps: int = 5):
     t0 = time.perf_counter()
     batch.set_scenes(scenes)
     set_s = time.perf_counter() - t0
-    space = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "packet"]}
+    space = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "packet"], "leaf_size": [8],
+             "short_stack": [8, 32]}
     best, table = autotune_batch(batch, spheres, offsets, space=space, reps=2)
 
     def timed(fn):
@@ -503,7 +509,8 @@ def batched_scenes_bench(device_index: int, reps: int = 5):
     plain_ms = timed(per_scene)
     for g in gpus:
         g.set_traversal(best["branching"], best["bits"], sort_queries=True, persistent=False, precise=True,
-                        packet=best.get("packet", False))
+                        packet=best.get("packet", False), leaf_size=best.get("leaf_size", 0),
+                        short_stack=best.get("short_stack", 16))
     wide_ms = timed(per_scene)
 
     # FP64 error of the batched results on 256 queries of each of 8 scenes
@@ -659,8 +666,7 @@ def run_ours(args):
 
         peak, peak_kind = peaks()
         achieved = fast_stats["bytes"] / (kms / 1e3) / 1e9
-        variant = f"wide{best['branching']}_q{best['bits']}" + {"thread": "", "persistent": "_persistent",
-                                                                  "packet": "_packet"}[_schedule(best)]
+        variant = f"wide{best['branching']}_q{best['bits']}_" + _schedule(best)
         traffic = profiled_traffic(variant)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -26,7 +26,8 @@ SIGNATURES = {
     "fcpwgb_cpu_bvh_export": (c_int, [P, P, P, P]),
     "fcpwgb_cpu_bvh_export_topology": (c_int, [P, P, P, P, P]),
     "fcpwgb_cpu_bvh_update_positions": (c_int, [P, P]),
-    "fcpwgb_cpu_bvh_export_wide": (c_int, [P, c_int, c_int, P, P, C.POINTER(c_uint32), C.POINTER(c_uint32)]),
+    "fcpwgb_cpu_bvh_export_wide": (c_int, [P, c_int, c_int, c_int, P, P, C.POINTER(c_uint32),
+                                           C.POINTER(c_uint32)]),
     "fcpwgb_gpu_scene_create": (c_int, [c_int, c_int, C.POINTER(c_void_p)]),
     "fcpwgb_gpu_scene_destroy": (None, [P]),
     "fcpwgb_gpu_scene_transfer": (c_int, [P, c_int, P, c_uint32, P, c_uint32, P, c_uint32, P, c_uint32]),
@@ -75,7 +76,8 @@ class BvhInfo(C.Structure):
 
 class TraversalConfig(C.Structure):
     _fields_ = [("branching", c_int), ("bits", c_int), ("block_size", c_int), ("sort_queries", c_int),
-                ("persistent", c_int), ("precise", c_int), ("packet", c_int)]
+                ("persistent", c_int), ("precise", c_int), ("packet", c_int), ("leaf_size", c_int),
+                ("short_stack", c_int)]
 
 
 class FcpwError(RuntimeError):

@@ -1,23 +1,54 @@
-"""Autotuner of the closest point traversal: times candidate variants
-(branching factor, child box precision, and the schedule: a thread per query,
-persistent blocks, or warp packets) on a sample of the caller's queries and
-keeps the fastest."""
+"""Autotuner of the closest point traversal: times candidate variants on a
+sample of the caller's queries and keeps the fastest. Stage 1 covers the
+branching factor (2/4/8), the child box precision (8/16/32 bits) and the
+schedule (a thread per query, persistent blocks, or warp packets); stage 2
+tries merged leaves (subtrees of up to 6, 8 or 12 primitives as one leaf) on
+the stage-1 winner; stage 3, for the one-thread-per-query schedules, the
+number of stack entries per thread kept in shared memory (0, 8, 32; 16 is
+the default)."""
 from __future__ import annotations
 
 import itertools
 
 # schedule: "thread" = one thread per query, "persistent" = persistent blocks
 # with neighbour seeding, "packet" = the queries of a warp traverse together
-DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "persistent", "packet"]}
+DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "persistent", "packet"],
+                 "leaf_size": [6, 8, 12], "short_stack": [0, 8, 32]}
 
 
 def candidates(space=None, sort_queries=True, precise=True):
-    space = dict(space or DEFAULT_SPACE)
-    if "schedule" not in space:  # older spelling: a list of persistent flags
-        space["schedule"] = ["persistent" if p else "thread" for p in space.get("persistent", [False])]
+    """The stage-1 grid (leaf_size 0, short_stack 16)."""
+    space = dict(DEFAULT_SPACE, **(space or {}))
+    if "persistent" in (space or {}) and "schedule" not in (space or {}):  # older spelling
+        space["schedule"] = ["persistent" if p else "thread" for p in space["persistent"]]
     for b, q, sch in itertools.product(space["branching"], space["bits"], space["schedule"]):
         yield {"branching": b, "bits": q, "persistent": sch == "persistent", "packet": sch == "packet",
-               "sort_queries": sort_queries, "precise": precise}
+               "sort_queries": sort_queries, "precise": precise, "leaf_size": 0, "short_stack": 16}
+
+
+def staged_search(measure, space=None, sort_queries=True, precise=True):
+    """measure(cfg) -> ms per call (raises if the layout cannot be encoded).
+    Returns (best config, [(config, ms)])."""
+    space = dict(DEFAULT_SPACE, **(space or {}))
+    table = []
+
+    def run(cfg):
+        try:
+            table.append((cfg, measure(cfg)))
+        except Exception:  # a layout this tree cannot be encoded in is skipped
+            pass
+
+    for cfg in candidates(space, sort_queries, precise):
+        run(cfg)
+    best = min(table, key=lambda t: t[1])[0]
+    for leaf in space["leaf_size"]:
+        run(dict(best, leaf_size=leaf))
+    best = min(table, key=lambda t: t[1])[0]
+    if not best["packet"]:
+        for short in space["short_stack"]:
+            run(dict(best, short_stack=short))
+    best = min(table, key=lambda t: t[1])[0]
+    return best, table
 
 
 def autotune_closest_points(gpu, spheres, space=None, reps: int = 3, precise: bool = True, out=None):
@@ -27,13 +58,10 @@ def autotune_closest_points(gpu, spheres, space=None, reps: int = 3, precise: bo
     stream = torch.cuda.current_stream(spheres.device)
     out = out if out is not None else torch.empty((spheres.shape[0], 10), dtype=torch.float32,
                                                   device=spheres.device)
-    table = []
-    for cfg in candidates(space, precise=precise):
-        try:
-            gpu.set_traversal(**cfg)
-            gpu.find_closest_points_tensor(spheres, out=out)  # builds the wide tree, warms caches
-        except Exception:  # a layout this tree cannot be encoded in is skipped
-            continue
+
+    def measure(cfg):
+        gpu.set_traversal(**cfg)
+        gpu.find_closest_points_tensor(spheres, out=out)  # builds the wide tree, warms caches
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
         start.record(stream)
@@ -41,7 +69,8 @@ def autotune_closest_points(gpu, spheres, space=None, reps: int = 3, precise: bo
             gpu.find_closest_points_tensor(spheres, out=out)
         end.record(stream)
         end.synchronize()
-        table.append((cfg, start.elapsed_time(end) / reps))
-    best = min(table, key=lambda t: t[1])[0]
+        return start.elapsed_time(end) / reps
+
+    best, table = staged_search(measure, space, precise=precise)
     gpu.set_traversal(**best)
     return best, table

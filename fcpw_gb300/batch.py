@@ -56,10 +56,10 @@ class _GPUSceneBatch:
         self._n_scenes = len(bvhs)
 
     def set_traversal(self, branching: int = 8, bits: int = 8, persistent: bool = False,
-                      precise: bool = True, packet: bool = False) -> None:
+                      precise: bool = True, packet: bool = False, leaf_size: int = 0, short_stack: int = 16) -> None:
         from ._lib import TraversalConfig
         cfg = TraversalConfig(int(branching), int(bits), 128, 1, int(bool(persistent)), int(bool(precise)),
-                              int(bool(packet)))
+                              int(bool(packet)), int(leaf_size), int(short_stack))
         check(lib().fcpwgb_gpu_batch_set_traversal(self._h, C.byref(cfg)))
 
     def get_traversal(self) -> dict:
@@ -138,27 +138,29 @@ class GPUSceneBatch2D(_GPUSceneBatch):
 
 def autotune_batch(batch: _GPUSceneBatch, spheres, query_offsets, space=None, reps: int = 3,
                    precise: bool = True):
-    """Times the batched closest point launch (graph replay) for every
-    (branching, bits, persistent) candidate on the caller's queries and keeps the
+    """Times the batched closest point launch (graph replay) for the candidates
+    of fcpw_gb300.autotune.staged_search on the caller's queries and keeps the
     fastest. Returns (best config, [(config, ms per call)])."""
     import torch
-    from .autotune import candidates
+    from .autotune import staged_search
     out = torch.empty((spheres.shape[0], 10), dtype=torch.float32, device=spheres.device)
     stream = torch.cuda.current_stream(spheres.device)
-    table = []
-    for cfg in candidates(space, precise=precise):
-        try:
-            batch.set_traversal(cfg["branching"], cfg["bits"], cfg["persistent"], precise, cfg.get("packet", False))
-            batch.find_closest_points_tensor(spheres, query_offsets, out=out)  # forest build + graph capture
-        except Exception:
-            continue
+
+    def set_cfg(cfg):
+        batch.set_traversal(cfg["branching"], cfg["bits"], cfg["persistent"], precise, cfg["packet"],
+                            cfg["leaf_size"], cfg["short_stack"])
+
+    def measure(cfg):
+        set_cfg(cfg)
+        batch.find_closest_points_tensor(spheres, query_offsets, out=out)  # forest build + graph capture
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         start.record(stream)
         for _ in range(reps):
             batch.find_closest_points_tensor(spheres, query_offsets, out=out)
         end.record(stream)
         end.synchronize()
-        table.append((cfg, start.elapsed_time(end) / reps))
-    best = min(table, key=lambda t: t[1])[0]
-    batch.set_traversal(best["branching"], best["bits"], best["persistent"], precise, best.get("packet", False))
+        return start.elapsed_time(end) / reps
+
+    best, table = staged_search(measure, space, precise=precise)
+    set_cfg(best)
     return best, table

@@ -32,7 +32,7 @@ struct BatchScene {
 
 struct GraphKey {
     const void *spheres, *out, *nodes, *prims, *cells, *perm, *sorted, *roots, *grids, *offsets;
-    uint32_t n, recordNormal, branching, bits, persistent, precise, sort, packet;
+    uint32_t n, recordNormal, branching, bits, persistent, precise, sort, packet, leaf, shortStack;
     bool operator==(const GraphKey &o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
 
@@ -49,7 +49,7 @@ struct fcpwgb_gpu_batch {
 
     // forest of the current (branching, bits)
     bool forestValid = false;
-    int forestW = 0, forestBits = 0;
+    int forestW = 0, forestBits = 0, forestLeaf = 0;
     uint32_t nNodes = 0, nPrims = 0;
     std::vector<uint32_t> roots;
     DeviceBuffer nodes, prims;
@@ -84,8 +84,8 @@ int activate(const fcpwgb_gpu_batch *b) {
 // collapse every scene to (W, bits) on the host (scenes in parallel), rebase
 // and concatenate; upload the forest
 int ensureForest(fcpwgb_gpu_batch *b) {
-    const int W = b->cfg.branching, bits = b->cfg.bits;
-    if (b->forestValid && b->forestW == W && b->forestBits == bits) return FCPWGB_OK;
+    const int W = b->cfg.branching, bits = b->cfg.bits, leaf = b->cfg.leafSize;
+    if (b->forestValid && b->forestW == W && b->forestBits == bits && b->forestLeaf == leaf) return FCPWGB_OK;
     if (b->scenes.empty()) return setError(FCPWGB_ERR_NOT_TRANSFERRED, "the batch holds no scenes");
     const size_t nS = b->scenes.size();
     std::vector<WideHost> wide(nS);
@@ -96,7 +96,7 @@ int ensureForest(fcpwgb_gpu_batch *b) {
     for (unsigned t = 0; t < nThreads; t++)
         pool.emplace_back([&, t]() {
             for (size_t s = t; s < nS; s += nThreads)
-                ok[s] = buildWideTree(W, bits, b->scenes[s].nP, b->scenes[s].off, b->scenes[s].boxes, wide[s]);
+                ok[s] = buildWideTree(W, bits, b->scenes[s].nP, b->scenes[s].off, b->scenes[s].boxes, wide[s], leaf);
         });
     for (auto &th : pool) th.join();
     for (size_t s = 0; s < nS; s++)
@@ -144,6 +144,7 @@ int ensureForest(fcpwgb_gpu_batch *b) {
     b->forestValid = true;
     b->forestW = W;
     b->forestBits = bits;
+    b->forestLeaf = leaf;
     b->nNodes = (uint32_t)totalNodes;
     b->nPrims = (uint32_t)totalPrims;
     for (size_t s = 0; s < b->grids.size() && s < nS; s++) b->grids[s].root = b->roots[s];
@@ -229,6 +230,7 @@ int enqueue(fcpwgb_gpu_batch *b, const DevSphere *spheres, DevInteraction *out, 
     l.roots = (const uint32_t *)b->rootBuf.ptr;
     uint32_t blocks = (n + 127) / 128;
     l.packet = b->cfg.packet;
+    l.shortStack = b->cfg.shortStack;
     if (b->cfg.persistent && !b->cfg.packet) {
         if ((e = cudaMemsetAsync(b->counter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)b->counter.ptr;
@@ -264,6 +266,8 @@ int runDevice(fcpwgb_gpu_batch *b, const DevSphere *spheres, const uint32_t *off
     k.persistent = (uint32_t)b->cfg.persistent; k.precise = (uint32_t)b->cfg.precise;
     k.sort = (uint32_t)b->cfg.sortQueries;
     k.packet = (uint32_t)b->cfg.packet;
+    k.leaf = (uint32_t)b->cfg.leafSize;
+    k.shortStack = (uint32_t)b->cfg.shortStack;
     cudaError_t e;
     if (!b->exec || !(k == b->key)) {
         b->dropGraph();
@@ -385,6 +389,9 @@ extern "C" int fcpwgb_gpu_batch_set_traversal(fcpwgb_gpu_batch *b, const fcpwgb_
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "bits must be 8, 16 or 32");
     if (c->block_size != 0 && c->block_size != 128)
         return setError(FCPWGB_ERR_UNSUPPORTED, "block_size must be 128 (or 0 for the default)");
+    if (c->leaf_size < 0 || c->leaf_size > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf_size must be 0..15");
+    if (c->short_stack < 0 || c->short_stack > 32)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0..32");
     b->dropGraph();
     b->cfg.branching = c->branching;
     b->cfg.bits = c->bits;
@@ -392,6 +399,8 @@ extern "C" int fcpwgb_gpu_batch_set_traversal(fcpwgb_gpu_batch *b, const fcpwgb_
     b->cfg.persistent = c->persistent != 0;
     b->cfg.precise = c->precise != 0;
     b->cfg.packet = c->packet != 0;
+    b->cfg.leafSize = c->leaf_size;
+    b->cfg.shortStack = c->short_stack;
     return FCPWGB_OK;
 }
 
@@ -404,6 +413,8 @@ extern "C" int fcpwgb_gpu_batch_get_traversal(const fcpwgb_gpu_batch *b, fcpwgb_
     c->persistent = b->cfg.persistent;
     c->precise = b->cfg.precise;
     c->packet = b->cfg.packet;
+    c->leaf_size = b->cfg.leafSize;
+    c->short_stack = b->cfg.shortStack;
     return FCPWGB_OK;
 }
 

@@ -134,8 +134,9 @@ extern "C" int fcpwgb_cpu_bvh_export_topology(const fcpwgb_cpu_bvh *b, int32_t *
     return FCPWGB_OK;
 }
 
-extern "C" int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *b, int branching, int bits, void *nodes,
-                                          int32_t *child_binary, uint32_t *n_nodes, uint32_t *node_bytes) {
+extern "C" int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *b, int branching, int bits, int leaf_size,
+                                          void *nodes, int32_t *child_binary, uint32_t *n_nodes,
+                                          uint32_t *node_bytes) {
     if (!b || !n_nodes || !node_bytes) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL argument");
     std::vector<uint32_t> nP, off;
     std::vector<float> boxes;
@@ -143,7 +144,8 @@ extern "C" int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *b, int branching
     WideHost w;
     if (!(branching == 2 || branching == 4 || branching == 8) || !(bits == 8 || bits == 16 || bits == 32))
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "branching must be 2/4/8 and bits 8/16/32");
-    if (!buildWideTree(branching, bits, nP, off, boxes, w))
+    if (leaf_size < 0 || leaf_size > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf_size must be 0..15");
+    if (!buildWideTree(branching, bits, nP, off, boxes, w, leaf_size))
         return setError(FCPWGB_ERR_UNSUPPORTED, "this tree cannot be collapsed into the requested wide layout");
     *n_nodes = w.nNodes;
     *node_bytes = (uint32_t)wideNodeBytes(branching, bits);
@@ -693,6 +695,9 @@ extern "C" int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *s, const fcpwgb_
     if (!(c->bits == 8 || c->bits == 16 || c->bits == 32))
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "bits must be 8, 16 or 32");
     if (c->block_size != 128) return setError(FCPWGB_ERR_UNSUPPORTED, "the wide kernels run 128-thread blocks");
+    if (c->leaf_size < 0 || c->leaf_size > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf_size must be 0..15");
+    if (c->short_stack < 0 || c->short_stack > 32)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0..32");
     WideConfig w;
     w.branching = c->branching;
     w.bits = c->bits;
@@ -701,6 +706,8 @@ extern "C" int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *s, const fcpwgb_
     w.persistent = c->persistent != 0;
     w.precise = c->precise != 0;
     w.packet = c->packet != 0;
+    w.leafSize = c->leaf_size;
+    w.shortStack = c->short_stack;
     s->wideConfig = w;
     return FCPWGB_OK;
 }
@@ -714,6 +721,8 @@ extern "C" int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *s, fcpwgb_
     c->persistent = s->wideConfig.persistent;
     c->precise = s->wideConfig.precise;
     c->packet = s->wideConfig.packet;
+    c->leaf_size = s->wideConfig.leafSize;
+    c->short_stack = s->wideConfig.shortStack;
     return FCPWGB_OK;
 }
 

@@ -202,30 +202,39 @@ template<> FCPWGB_D void sortNetwork<8>(uint32_t (&k)[8]) {
 }
 
 // Per-thread traversal stack of kWideStack entries (node reference + the
-// child's distance bound). The first kShortStack entries live in shared
-// memory, entry k of thread t at [k * 128 + t] so that a warp's accesses fall
-// in distinct banks; deeper entries go to local memory, which only deep
-// traversals touch. A whole stack in local memory (1 KB per thread) does not
-// fit the L1 of a fully occupied SM and its pushes and pops reach L2 and DRAM.
-constexpr int kShortStack = 16;
+// child's distance bound). The first `shortN` entries (a launch parameter,
+// 0..kMaxShortStack) live in dynamic shared memory, entry k of thread t at
+// [k * 128 + t] so that a warp's accesses fall in distinct banks; deeper
+// entries go to local memory, which only deep traversals touch. A whole stack
+// in local memory (1 KB per thread) does not fit the L1 of a fully occupied
+// SM and its pushes and pops reach L2 and DRAM.
+constexpr int kMaxShortStack = 32;
 constexpr int kWideBlock = 128;  // threads per block of the wide kernels
 struct WideStack {
     uint32_t *sRef;  // shared, stride kWideBlock
     float *sD;
-    uint32_t lRef[kWideStack - kShortStack];
-    float lD[kWideStack - kShortStack];
+    int shortN;
+    uint32_t lRef[kWideStack];
+    float lD[kWideStack];
+    // dynamic shared memory: shortN * 128 references, then shortN * 128 distances
+    FCPWGB_D void bind(unsigned char *smem, int n) {
+        shortN = n;
+        sRef = reinterpret_cast<uint32_t *>(smem) + threadIdx.x;
+        sD = reinterpret_cast<float *>(smem) + (size_t)n * kWideBlock + threadIdx.x;
+    }
     FCPWGB_D void push(int sp, uint32_t ref, float d) {
-        if (sp < kShortStack) {
+        if (sp < shortN) {
             sRef[sp * kWideBlock] = ref;
             sD[sp * kWideBlock] = d;
         } else {
-            lRef[sp - kShortStack] = ref;
-            lD[sp - kShortStack] = d;
+            lRef[sp - shortN] = ref;
+            lD[sp - shortN] = d;
         }
     }
-    FCPWGB_D float dist(int sp) const { return sp < kShortStack ? sD[sp * kWideBlock] : lD[sp - kShortStack]; }
-    FCPWGB_D uint32_t ref(int sp) const { return sp < kShortStack ? sRef[sp * kWideBlock] : lRef[sp - kShortStack]; }
+    FCPWGB_D float dist(int sp) const { return sp < shortN ? sD[sp * kWideBlock] : lD[sp - shortN]; }
+    FCPWGB_D uint32_t ref(int sp) const { return sp < shortN ? sRef[sp * kWideBlock] : lRef[sp - shortN]; }
 };
+inline size_t wideStackSmemBytes(int shortN) { return (size_t)shortN * kWideBlock * 8; }
 
 // Traversal statistics (expansions, tests, warp loads): compiled in only for
 // the counting launches, so the timed kernels carry no counter registers.
@@ -436,12 +445,11 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                                                                 const uint32_t *__restrict__ roots,
                                                                 DevInteraction *__restrict__ out, uint32_t n,
                                                                 int recordNormal, uint32_t *counter,
-                                                                uint32_t *errorWord, unsigned long long *stats) {
-    __shared__ uint32_t sRef[kShortStack * kWideBlock];
-    __shared__ float sD[kShortStack * kWideBlock];
+                                                                uint32_t *errorWord, unsigned long long *stats,
+                                                                int shortStack) {
+    extern __shared__ __align__(16) unsigned char wideSmem[];
     WideStack st;
-    st.sRef = sRef + threadIdx.x;
-    st.sD = sD + threadIdx.x;
+    st.bind(wideSmem, shortStack);
     Count<STATS> tExp, tTests;
     if (!PERSISTENT) {
         uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
@@ -699,13 +707,12 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
                                                        const DevRay *__restrict__ rays,
                                                        const uint32_t *__restrict__ perm,
                                                        DevInteraction *__restrict__ out, uint32_t n, int occl,
-                                                       uint32_t *errorWord, unsigned long long *stats) {
+                                                       uint32_t *errorWord, unsigned long long *stats,
+                                                       int shortStack) {
     constexpr uint32_t kSlotMask = W - 1;
-    __shared__ uint32_t sRef[kShortStack * kWideBlock];
-    __shared__ float sD[kShortStack * kWideBlock];
+    extern __shared__ __align__(16) unsigned char wideSmem[];
     WideStack st;
-    st.sRef = sRef + threadIdx.x;
-    st.sD = sD + threadIdx.x;
+    st.bind(wideSmem, shortStack);
     const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
     if (i >= n) return;
     const unsigned char *rp = reinterpret_cast<const unsigned char *>(rays + i);
@@ -827,11 +834,13 @@ cudaError_t launchWideClosestKernel(const WideLaunch &l, cudaStream_t s) {
         kWidePacketClosestPoint<W, B, Prim, PRECISE, STATS><<<g, b, 0, s>>>(
             l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.errorWord, l.stats);
     else if (l.counter)
-        kWideClosestPoint<W, B, Prim, PRECISE, true, STATS><<<g, b, 0, s>>>(
-            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats);
+        kWideClosestPoint<W, B, Prim, PRECISE, true, STATS><<<g, b, wideStackSmemBytes(l.shortStack), s>>>(
+            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats,
+            l.shortStack);
     else
-        kWideClosestPoint<W, B, Prim, PRECISE, false, STATS><<<g, b, 0, s>>>(
-            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats);
+        kWideClosestPoint<W, B, Prim, PRECISE, false, STATS><<<g, b, wideStackSmemBytes(l.shortStack), s>>>(
+            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats,
+            l.shortStack);
     return cudaGetLastError();
 }
 template<int W, int B, class Prim>
@@ -863,7 +872,8 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
         if (l.n == 0) return cudaSuccess;                                                                          \
         dim3 g((l.n + 127) / 128), b(128);                                                                         \
         auto go = [&](auto kern) {                                                                                 \
-            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.errorWord, l.stats);     \
+            kern<<<g, b, wideStackSmemBytes(l.shortStack), s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n,      \
+                                                                l.occl, l.errorWord, l.stats, l.shortStack);      \
         };                                                                                                         \
         if (dim == 3) {                                                                                            \
             if (bits == 8) go(kWideRay<W, 8, Tri48Prim>);                                                          \

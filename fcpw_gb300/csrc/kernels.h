@@ -51,6 +51,7 @@ struct WideLaunch {
     int recordNormal = 0;
     uint32_t *counter = nullptr;           // work counter (zero on entry) for persistent blocks, or NULL
     int packet = 0;                        // 1: warp packets (kWidePacketClosestPoint), counter unused
+    int shortStack = 16;                   // per-thread stack entries in shared memory (thread schedules), 0..32
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;   // traversal statistics, or NULL
     uint32_t grid = 0;
@@ -69,6 +70,7 @@ struct WideRayLaunch {
     int occl = 0;
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;
+    int shortStack = 16;
 };
 template<int W> cudaError_t launchWideRayT(int bits, int dim, const WideRayLaunch &l, cudaStream_t s);
 cudaError_t launchWideRays(int W, int bits, int dim, const WideRayLaunch &l, cudaStream_t s);

@@ -36,9 +36,9 @@ cudaError_t launchRequant(int W, int bits, unsigned char *wn, const int32_t *cb,
 
 int GpuScene::ensureWide(cudaStream_t st) {
     const WideConfig &c = wideConfig;
-    if (wide.valid && wide.branching == c.branching && wide.bits == c.bits) return 0;
+    if (wide.valid && wide.branching == c.branching && wide.bits == c.bits && wide.leafSize == c.leafSize) return 0;
     WideHost h;
-    if (!buildWideTree(c.branching, c.bits, hostNP, hostOff, hostBoxes, h))
+    if (!buildWideTree(c.branching, c.bits, hostNP, hostOff, hostBoxes, h, c.leafSize))
         return setError(FCPWGB_ERR_UNSUPPORTED, "this tree cannot be collapsed into the requested wide layout");
     int rc;
     if ((rc = wideNodes.upload(h.nodes.data(), h.nodes.size(), st))) return rc;
@@ -58,6 +58,7 @@ int GpuScene::ensureWide(cudaStream_t st) {
     wide.valid = true;
     wide.branching = c.branching;
     wide.bits = c.bits;
+    wide.leafSize = c.leafSize;
     wide.nNodes = h.nNodes;
     wide.depth = h.depth;
     wide.builtFromVersion = treeVersion;
@@ -101,6 +102,7 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
     }
     uint32_t blocks = (n + 127) / 128;
     l.packet = c.packet;
+    l.shortStack = c.shortStack;
     if (c.persistent && !c.packet) {
         if ((rc = workCounter.ensure(16))) return rc;
         if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
@@ -138,6 +140,7 @@ int GpuScene::wideRays(const DevRay *r, DevInteraction *out, uint32_t n, int occ
     l.n = n;
     l.occl = occl;
     l.errorWord = (uint32_t *)errorWord.ptr;
+    l.shortStack = wideConfig.shortStack;
     cudaError_t e;
     if (wideConfig.sortQueries && n >= 4096) {
         if ((rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;

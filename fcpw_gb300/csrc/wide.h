@@ -28,6 +28,8 @@ struct WideConfig {
     int persistent = 1;  // persistent blocks fetching query chunks from a work counter
     int precise = 1;     // recompute the winning primitive's distance in FP64
     int packet = 0;      // traverse the 32 queries of a warp as one packet
+    int leafSize = 0;    // > 0: binary subtrees of at most this many primitives collapse into one leaf
+    int shortStack = 16; // traversal stack entries per thread held in shared memory (thread schedules)
 };
 
 constexpr int wideHeaderBytes(int bits) { return bits == 32 ? 0 : 16; }
@@ -52,13 +54,16 @@ struct WideHost {
 // max-surface-area rule of the reference's Mbvh collapse,
 // include/fcpw/aggregates/mbvh.inl:57-147). Returns false if a leaf cannot
 // be encoded (more than 15 primitives) or the wide stack could overflow.
+// maxLeafSize > 0 also turns every binary subtree of at most that many
+// primitives (which the pre-order SAH build stores contiguously) into one
+// wide leaf; 0 keeps the binary leaves as they are.
 bool buildWideTree(int W, int bits, const std::vector<uint32_t> &nPrims, const std::vector<uint32_t> &offsets,
-                   const std::vector<float> &boxes, WideHost &out);
+                   const std::vector<float> &boxes, WideHost &out, int maxLeafSize = 0);
 
 // what a scene keeps about its derived wide tree (buffers live in the scene)
 struct WideTree {
     bool valid = false;
-    int branching = 0, bits = 32;
+    int branching = 0, bits = 32, leafSize = 0;
     uint32_t nNodes = 0, depth = 0;
     uint64_t builtFromVersion = 0;
     void clear() { valid = false; }

@@ -16,6 +16,36 @@ struct Collapser {
     WideHost &out;
     bool ok = true;
     size_t nodeBytes;
+    uint32_t maxLeaf = 0;                   // > 0: subtrees of at most this many primitives become one leaf
+    std::vector<uint32_t> subCount, subFirst;  // primitives under a binary node, first of them
+    std::vector<char> subContiguous;        // they form one range subFirst .. subFirst + subCount
+
+    // primitive count and range of every binary subtree (pre-order: children after their parent)
+    void summarise() {
+        const size_t n = nP.size();
+        subCount.assign(n, 0);
+        subFirst.assign(n, 0);
+        subContiguous.assign(n, 1);
+        std::vector<uint32_t> subEnd(n, 0);
+        for (size_t i = n; i-- > 0;) {
+            if (nP[i] > 0) {
+                subCount[i] = nP[i];
+                subFirst[i] = off[i];
+                subEnd[i] = off[i] + nP[i];
+            } else {
+                uint32_t l = (uint32_t)i + 1, r = (uint32_t)i + off[i];
+                subCount[i] = subCount[l] + subCount[r];
+                subFirst[i] = std::min(subFirst[l], subFirst[r]);
+                subEnd[i] = std::max(subEnd[l], subEnd[r]);
+                subContiguous[i] = subContiguous[l] && subContiguous[r] && subEnd[i] - subFirst[i] == subCount[i];
+            }
+        }
+    }
+    // a binary node that becomes a leaf slot of the wide tree
+    bool leafLike(uint32_t b) const {
+        if (nP[b] > 0) return true;
+        return maxLeaf > 0 && subContiguous[b] && subCount[b] <= maxLeaf;
+    }
 
     float area(uint32_t b) const {
         const float *p = &box[(size_t)b * 6];
@@ -31,7 +61,7 @@ struct Collapser {
         out.childBinary.resize((size_t)out.nNodes * W, -1);
 
         std::vector<uint32_t> kids;
-        if (nP[b] > 0) {
+        if (leafLike(b)) {
             kids.push_back(b);  // a leaf root
         } else {
             kids.push_back(b + 1);
@@ -40,7 +70,7 @@ struct Collapser {
                 int best = -1;
                 float bestA = -1.0f;
                 for (size_t i = 0; i < kids.size(); i++) {
-                    if (nP[kids[i]] > 0) continue;
+                    if (leafLike(kids[i])) continue;
                     float a = area(kids[i]);
                     if (a > bestA) { bestA = a; best = (int)i; }
                 }
@@ -68,10 +98,11 @@ struct Collapser {
                 hi[c * 3 + a] = box[(size_t)k * 6 + 3 + a];
             }
             out.childBinary[(size_t)idx * W + c] = (int32_t)k;
-            if (nP[k] > 0) {
-                if (nP[k] > 15 || off[k] >= (1u << 27)) ok = false;
-                ref[c] = off[k];
-                cnt[c] = (uint8_t)std::min<uint32_t>(nP[k], 15);
+            if (leafLike(k)) {
+                uint32_t first = nP[k] > 0 ? off[k] : subFirst[k], count = nP[k] > 0 ? nP[k] : subCount[k];
+                if (count > 15 || first >= (1u << 27)) ok = false;
+                ref[c] = first;
+                cnt[c] = (uint8_t)std::min<uint32_t>(count, 15);
             } else {
                 ref[c] = build(k, depth + 1);
                 cnt[c] = 0;
@@ -101,13 +132,16 @@ struct Collapser {
 }  // namespace
 
 bool buildWideTree(int W, int bits, const std::vector<uint32_t> &nPrims, const std::vector<uint32_t> &offsets,
-                   const std::vector<float> &boxes, WideHost &out) {
+                   const std::vector<float> &boxes, WideHost &out, int maxLeafSize) {
     out = WideHost();
     out.W = W;
     out.bits = bits;
     if (!(W == 2 || W == 4 || W == 8) || !(bits == 8 || bits == 16 || bits == 32) || nPrims.empty()) return false;
+    if (maxLeafSize < 0 || maxLeafSize > 15) return false;
     Collapser c{W, bits, nPrims, offsets, boxes, out};
     c.nodeBytes = (size_t)wideNodeBytes(W, bits);
+    c.maxLeaf = (uint32_t)maxLeafSize;
+    if (c.maxLeaf > 0) c.summarise();
     out.nodes.reserve((size_t)nPrims.size() * c.nodeBytes / std::max(1, W - 1) + c.nodeBytes);
     c.build(0, 0);
     // the per-thread stack holds at most (W - 1) entries per level plus one

@@ -201,14 +201,16 @@ class _GPUScene:
 
     # -- traversal variant -------------------------------------------------
     def set_traversal(self, branching: int = 0, bits: int = 32, sort_queries: bool = True,
-                      persistent: bool = True, precise: bool = True, packet: bool = False) -> None:
+                      persistent: bool = True, precise: bool = True, packet: bool = False, leaf_size: int = 0,
+                      short_stack: int = 16) -> None:
         """Selects the closest point traversal (see fcpwgb_traversal_config):
         branching 0 is the reference-order binary traversal; 2/4/8 use a wide
         tree with 32-, 16- or 8-bit child boxes; packet walks the queries of a
-        warp together."""
+        warp together; leaf_size merges small subtrees into wide leaves;
+        short_stack is the per-thread stack depth kept in shared memory."""
         from ._lib import TraversalConfig
         cfg = TraversalConfig(int(branching), int(bits), 128, int(bool(sort_queries)), int(bool(persistent)),
-                              int(bool(precise)), int(bool(packet)))
+                              int(bool(precise)), int(bool(packet)), int(leaf_size), int(short_stack))
         check(lib().fcpwgb_gpu_scene_set_traversal(self._h, C.byref(cfg)))
 
     def get_traversal(self) -> dict:

@@ -88,14 +88,16 @@ class CpuBvh:
                                                    ptr(sil_vertices) if sil_vertices is not None and len(sil_vertices) else None))
         return index_map, prim_vertices, prim_index, sil_vertices
 
-    def export_wide(self, branching: int, bits: int):
+    def export_wide(self, branching: int, bits: int, leaf_size: int = 0):
         """The wide / quantised tree of the GPU fast path: (raw records as an
         (n_nodes, node_bytes) uint8 array, child_binary (n_nodes, branching))."""
         n, nb = C.c_uint32(0), C.c_uint32(0)
-        check(lib().fcpwgb_cpu_bvh_export_wide(self._h, branching, bits, None, None, C.byref(n), C.byref(nb)))
+        check(lib().fcpwgb_cpu_bvh_export_wide(self._h, branching, bits, leaf_size, None, None, C.byref(n),
+                                               C.byref(nb)))
         nodes = np.zeros((n.value, nb.value), np.uint8)
         cb = np.zeros((n.value, branching), np.int32)
-        check(lib().fcpwgb_cpu_bvh_export_wide(self._h, branching, bits, ptr(nodes), ptr(cb), C.byref(n), C.byref(nb)))
+        check(lib().fcpwgb_cpu_bvh_export_wide(self._h, branching, bits, leaf_size, ptr(nodes), ptr(cb), C.byref(n),
+                                               C.byref(nb)))
         return nodes, cb
 
     def update_positions(self, positions: np.ndarray) -> None:

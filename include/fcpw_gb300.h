@@ -148,9 +148,9 @@ int fcpwgb_cpu_bvh_export_topology(const fcpwgb_cpu_bvh *bvh, int32_t *index_map
  * documented in fcpw_gb300/csrc/wide.h). Call with nodes == NULL to query
  * *n_nodes and *node_bytes; then pass buffers of n_nodes * node_bytes bytes
  * and n_nodes * branching int32 (child_binary: binary node behind every slot,
- * -1 for an empty slot). Returns FCPWGB_ERR_UNSUPPORTED when the tree cannot
- * be encoded. */
-int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *bvh, int branching, int bits, void *nodes,
+ * -1 for an empty slot). leaf_size as in fcpwgb_traversal_config. Returns
+ * FCPWGB_ERR_UNSUPPORTED when the tree cannot be encoded. */
+int fcpwgb_cpu_bvh_export_wide(const fcpwgb_cpu_bvh *bvh, int branching, int bits, int leaf_size, void *nodes,
                                int32_t *child_binary, uint32_t *n_nodes, uint32_t *node_bytes);
 /* updateObjectVertices (fcpw.inl:1129-1143): replaces the vertex positions
  * (caller vertex order) so that a following export yields the moved
@@ -213,9 +213,13 @@ int fcpwgb_gpu_scene_update_vertices_device_static(fcpwgb_gpu_scene *scene, cons
  * precise recomputes the winning primitive's distance and point in FP64;
  * packet traverses the 32 (sorted) queries of a warp together, one record
  * load per warp and step, each query pruning with its own radius (persistent
- * is then ignored). Defaults: {0, 32, 128, 1, 1, 1, 0}. Results differ from
- * the binary order only on equidistant ties (and, with precise, by the FP32
- * rounding removed). */
+ * is then ignored); leaf_size > 0 collapses binary subtrees of at most that
+ * many primitives (up to 15) into one wide leaf; short_stack is the number of
+ * traversal-stack entries per thread kept in shared memory by the
+ * one-thread-per-query schedules (0..32; deeper entries in local memory).
+ * Defaults: {0, 32, 128, 1, 1, 1, 0, 0, 16}. Results differ from the binary
+ * order only on equidistant ties (and, with precise, by the FP32 rounding
+ * removed). */
 typedef struct {
     int branching;     /* 0, 2, 4 or 8 */
     int bits;          /* 32, 16 or 8 */
@@ -224,6 +228,8 @@ typedef struct {
     int persistent;    /* 0 or 1 */
     int precise;       /* 0 or 1 */
     int packet;        /* 0 or 1 */
+    int leaf_size;     /* 0 (binary leaves) or 1..15 */
+    int short_stack;   /* 0..32 */
 } fcpwgb_traversal_config;
 int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *scene, const fcpwgb_traversal_config *config);
 int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *scene, fcpwgb_traversal_config *config);

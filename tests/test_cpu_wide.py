@@ -87,3 +87,30 @@ def test_quantised_boxes_stay_tight(scenes):
             qlo = o + d["q"][i, a, c] * 2.0 ** e
             qhi = o + d["q"][i, 3 + a, c] * 2.0 ** e
             assert qhi - qlo <= (nodes["pMax"][cb[i, c], a] - nodes["pMin"][cb[i, c], a]) + 4 * ext / 255 + 1e-6
+
+
+@pytest.mark.parametrize("leaf_size", [6, 8, 12])
+@pytest.mark.parametrize("branching", [4, 8])
+def test_merged_leaves_cover_every_primitive_once(scenes, branching, leaf_size):
+    """leaf_size > 0 merges binary subtrees of at most leaf_size primitives into
+    one wide leaf: the leaf slots still cover every primitive exactly once, no
+    leaf is larger than allowed, and each merged slot's box is the box of the
+    binary subtree it replaces (its child_binary entry)."""
+    for dim, lst in scenes.items():
+        for s in lst:
+            nodes, prims, _ = s.cpu_bvh.export()
+            raw, cb = s.cpu_bvh.export_wide(branching, 32, leaf_size)
+            d = WF.decode(raw, branching, 32)
+            leaf_slots = (d["cnt"] != 0) & (d["cnt"] != EMPTY)
+            refs, cnts = d["refs"][leaf_slots], d["cnt"][leaf_slots]
+            assert cnts.max() <= max(leaf_size, int(nodes["nPrimitives"].max()))
+            covered = np.zeros(len(prims), np.int32)
+            for r, c in zip(refs.tolist(), cnts.tolist()):
+                covered[r:r + c] += 1
+            assert np.all(covered == 1)
+            raw0, _ = s.cpu_bvh.export_wide(branching, 32, 0)
+            assert len(raw) <= len(raw0)  # merging never adds records
+            valid = cb >= 0
+            lo = np.stack([nodes["pMin"][cb.clip(0)][..., a] for a in range(3)], 1)
+            assert np.array_equal(np.where(valid[:, None, :], d["bounds"][:, :3], 0),
+                                  np.where(valid[:, None, :], lo, 0))
