@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven scenes measurement")
     ap.add_argument("--suite", action="store_true",
                     help="instead of the headline line, one line per other configuration of the scope")
+    ap.add_argument("--only", default="", help="with --suite: comma-separated subset of c1,rays,c3,sil3d")
     return ap.parse_args()
 
 
@@ -328,57 +329,11 @@ def run_suite(args):
                       "cpu_baseline": cpu}
 
     lines = []
-    # C1: 20,480-triangle perturbed icosphere, 1,048,576 queries in [-1.5, 1.5]^3
-    v, f = W.perturbed_sphere(32, W.SEED_BASE + 1)
-    _, _, line = closest_point_config("icosphere 20,480 triangles, 1,048,576 closest-point queries", 3, v, f,
-                                      W.uniform_points(1 << 20, 3, -1.5, 1.5, W.SEED_BASE + 1001))
-    lines.append(line)
+    only = set(args.only.split(",")) if args.only else None
 
-    # C2 rays: 4,194,304 rays on the 1M-triangle torus, origins in [-2, 2]^3, directions uniform on S^2
-    v, f, _ = make_workload(0, 1)
-    s, _ = build_scene(v, f)
-    g = F.GPUScene3D("", False, device=0)
-    g.transfer_to_gpu(s)
-    n = N_QUERIES
-    o = W.uniform_points(n, 3, -2.0, 2.0, W.SEED_BASE + 2002)
-    d = W.uniform_directions(n, 3, W.SEED_BASE + 2003)
-    rays_np = R.make_rays(o, d, R.FLT_MAX)
-    rays = torch.from_numpy(rays_np.view(np.float32).reshape(n, 10).copy()).to(dev)
-    out = torch.empty((n, 10), dtype=torch.float32, device=dev)
-    def ray_run():
-        check(L.fcpwgb_intersect_rays_device(g.handle, rays.data_ptr(), out.data_ptr(), n, 0, sp))
+    def want(name):
+        return only is None or name in only
 
-    g.set_traversal(0)
-    ray_ms = timed(ray_run)
-    hits = float((out[:, 9].view(torch.int32) != -1).float().mean())
-    table = []
-    for wb in [(2, 32, True), (4, 8, True), (4, 16, True), (4, 32, True), (4, 32, False), (8, 8, True),
-               (8, 16, True), (8, 32, True)]:
-        g.set_traversal(*wb[:2], sort_queries=wb[2])
-        table.append((wb, timed(ray_run, reps=3)))
-    (wb_best, _) = min(table, key=lambda t: t[1])
-    g.set_traversal(*wb_best[:2], sort_queries=wb_best[2])
-    fast_ms = timed(ray_run)
-    nodes, prims, _ = s.cpu_bvh.export()
-    cpu = cpu_rate(lambda m: O.intersect_rays_bvh(3, nodes, prims, rays_np[:m], nthreads=threads), n)
-    lines.append({"config": "rays, torus 1,048,576 triangles, 4,194,304 rays (first hit)", "queries": n,
-                  "plain": {"queries_per_s": n / (ray_ms / 1e3), "ms": ray_ms},
-                  "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms,
-                           "variant": {"branching": wb_best[0], "bits": wb_best[1], "sort_queries": wb_best[2]}},
-                  "speedup_vs_plain": ray_ms / fast_ms, "hit_fraction": hits,
-                  "autotune_ms": [[w, b, int(o), round(t, 3)] for (w, b, o), t in table], "cpu_baseline": cpu})
-    del g, s
-
-    # C3: 256 star polylines x 512 segments, 8,388,608 queries in [-3, 3]^2: closest point and silhouettes
-    v, sg = W.star_polylines(256, 512, W.SEED_BASE + 3, extent=3.0, scale=0.14)
-    pts2 = W.uniform_points(8 << 20, 2, -3.0, 3.0, W.SEED_BASE + 3003)
-    s2, g2, line = closest_point_config("2D stars 131,072 segments, 8,388,608 closest-point queries", 2, v, sg,
-                                        pts2, silhouettes=True)
-    lines.append(line)
-    n = len(pts2)
-    sph = sph_tensor(pts2)
-    flip = torch.zeros(n, dtype=torch.int32, device=dev)
-    out = torch.empty((n, 10), dtype=torch.float32, device=dev)
     def sil_run(gs, sph, flip, out, n):
         return lambda: check(L.fcpwgb_find_closest_silhouette_points_device(
             gs.handle, sph.data_ptr(), flip.data_ptr(), out.data_ptr(), n, 0.0, 1e-3, sp))
@@ -392,36 +347,93 @@ def run_suite(args):
                 "fast": {"queries_per_s": n / (fast / 1e3), "ms": fast, "variant": "queries sorted spatially"},
                 "speedup_vs_plain": plain / fast}
 
-    times = sil_times(g2, sph, flip, out, n)
-    nodes, _, sils = s2.cpu_bvh.export()
-    zf = np.zeros(n, np.uint32)
-    cpu = cpu_rate(lambda m: O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts2[:m], R.FLT_MAX), zf[:m],
-                                               nthreads=threads), n)
-    lines.append({"config": "2D stars 131,072 segments, 8,388,608 closest-silhouette queries (flip 0)",
-                  "queries": n, **times, "cpu_baseline": cpu})
-    del g2, s2
+    # C1: 20,480-triangle perturbed icosphere, 1,048,576 queries in [-1.5, 1.5]^3
+    if want("c1"):
+        v, f = W.perturbed_sphere(32, W.SEED_BASE + 1)
+        _, _, line = closest_point_config("icosphere 20,480 triangles, 1,048,576 closest-point queries", 3, v, f,
+                                          W.uniform_points(1 << 20, 3, -1.5, 1.5, W.SEED_BASE + 1001))
+        lines.append(line)
+
+    # C2 rays: 4,194,304 rays on the 1M-triangle torus, origins in [-2, 2]^3, directions uniform on S^2
+    if want("rays"):
+        v, f, _ = make_workload(0, 1)
+        s, _ = build_scene(v, f)
+        g = F.GPUScene3D("", False, device=0)
+        g.transfer_to_gpu(s)
+        n = N_QUERIES
+        o = W.uniform_points(n, 3, -2.0, 2.0, W.SEED_BASE + 2002)
+        d = W.uniform_directions(n, 3, W.SEED_BASE + 2003)
+        rays_np = R.make_rays(o, d, R.FLT_MAX)
+        rays = torch.from_numpy(rays_np.view(np.float32).reshape(n, 10).copy()).to(dev)
+        out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+        def ray_run():
+            check(L.fcpwgb_intersect_rays_device(g.handle, rays.data_ptr(), out.data_ptr(), n, 0, sp))
+
+        g.set_traversal(0)
+        ray_ms = timed(ray_run)
+        hits = float((out[:, 9].view(torch.int32) != -1).float().mean())
+        table = []
+        for wb in [(2, 32, True), (4, 8, True), (4, 16, True), (4, 32, True), (4, 32, False), (8, 8, True),
+                   (8, 16, True), (8, 32, True)]:
+            g.set_traversal(*wb[:2], sort_queries=wb[2])
+            table.append((wb, timed(ray_run, reps=3)))
+        (wb_best, _) = min(table, key=lambda t: t[1])
+        g.set_traversal(*wb_best[:2], sort_queries=wb_best[2])
+        fast_ms = timed(ray_run)
+        nodes, prims, _ = s.cpu_bvh.export()
+        cpu = cpu_rate(lambda m: O.intersect_rays_bvh(3, nodes, prims, rays_np[:m], nthreads=threads), n)
+        lines.append({"config": "rays, torus 1,048,576 triangles, 4,194,304 rays (first hit)", "queries": n,
+                      "plain": {"queries_per_s": n / (ray_ms / 1e3), "ms": ray_ms},
+                      "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms,
+                               "variant": {"branching": wb_best[0], "bits": wb_best[1], "sort_queries": wb_best[2]}},
+                      "speedup_vs_plain": ray_ms / fast_ms, "hit_fraction": hits,
+                      "autotune_ms": [[w, b, int(o), round(t, 3)] for (w, b, o), t in table], "cpu_baseline": cpu})
+        del g, s
+
+    # C3: 256 star polylines x 512 segments, 8,388,608 queries in [-3, 3]^2: closest point and silhouettes
+    if want("c3"):
+        v, sg = W.star_polylines(256, 512, W.SEED_BASE + 3, extent=3.0, scale=0.14)
+        pts2 = W.uniform_points(8 << 20, 2, -3.0, 3.0, W.SEED_BASE + 3003)
+        s2, g2, line = closest_point_config("2D stars 131,072 segments, 8,388,608 closest-point queries", 2, v, sg,
+                                            pts2, silhouettes=True)
+        lines.append(line)
+        n = len(pts2)
+        sph = sph_tensor(pts2)
+        flip = torch.zeros(n, dtype=torch.int32, device=dev)
+        out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+        times = sil_times(g2, sph, flip, out, n)
+        nodes, _, sils = s2.cpu_bvh.export()
+        zf = np.zeros(n, np.uint32)
+        cpu = cpu_rate(lambda m: O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts2[:m], R.FLT_MAX), zf[:m],
+                                                   nthreads=threads), n)
+        lines.append({"config": "2D stars 131,072 segments, 8,388,608 closest-silhouette queries (flip 0)",
+                      "queries": n, **times, "cpu_baseline": cpu})
+        del g2, s2
 
     # 3D silhouettes on the 1M-triangle torus (SNCH), 4,194,304 queries in [-2, 2]^3
-    v, f, pts = make_workload(0, N_QUERIES)
-    s = F.Scene3D()
-    s.set_object_count(1)
-    s.set_object_vertices(v, 0)
-    s.set_object_triangles(f, 0)
-    s.compute_silhouettes()
-    s.build(F.AggregateType.Bvh_SurfaceArea, False)
-    g = F.GPUScene3D("", False, device=0)
-    g.transfer_to_gpu(s)
-    n = len(pts)
-    sph = sph_tensor(pts)
-    flip = torch.zeros(n, dtype=torch.int32, device=dev)
-    out = torch.empty((n, 10), dtype=torch.float32, device=dev)
-    times = sil_times(g, sph, flip, out, n)
-    nodes, _, sils = s.cpu_bvh.export()
-    zf = np.zeros(n, np.uint32)
-    cpu = cpu_rate(lambda m: O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pts[:m], R.FLT_MAX), zf[:m],
-                                               nthreads=threads), n)
-    lines.append({"config": "3D silhouettes, torus 1,048,576 triangles (SNCH), 4,194,304 queries (flip 0)",
-                  "queries": n, **times, "cpu_baseline": cpu})
+    if want("sil3d"):
+        v, f, pts = make_workload(0, args.queries)
+        s = F.Scene3D()
+        s.set_object_count(1)
+        s.set_object_vertices(v, 0)
+        s.set_object_triangles(f, 0)
+        s.compute_silhouettes()
+        s.build(F.AggregateType.Bvh_SurfaceArea, False)
+        g = F.GPUScene3D("", False, device=0)
+        g.transfer_to_gpu(s)
+        n = len(pts)
+        sph = sph_tensor(pts)
+        flip = torch.zeros(n, dtype=torch.int32, device=dev)
+        out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+        times = sil_times(g, sph, flip, out, n)
+        nodes, _, sils = s.cpu_bvh.export()
+        zf = np.zeros(n, np.uint32)
+        cpu = None if args.no_cpu_baseline else cpu_rate(
+            lambda m: O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pts[:m], R.FLT_MAX), zf[:m], nthreads=threads),
+            n)
+        lines.append({"config": f"3D silhouettes, torus 1,048,576 triangles (SNCH), {n:,} queries (flip 0)",
+                      "queries": n, **times, "cpu_baseline": cpu})
+
     for line in lines:
         print(json.dumps(line), flush=True)
 
@@ -471,7 +483,7 @@ def batched_scenes_bench(device_index: int, reps: int = 5):
     batch.set_scenes(scenes)
     set_s = time.perf_counter() - t0
     space = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "packet"], "leaf_size": [8],
-             "short_stack": [8, 32]}
+             "short_stack": [0]}
     best, table = autotune_batch(batch, spheres, offsets, space=space, reps=2)
 
     def timed(fn):

@@ -53,6 +53,10 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_get_traversal": (c_int, [P, P]),
     "fcpwgb_gpu_scene_check_errors": (c_int, [P, C.POINTER(c_uint32)]),
     "fcpwgb_closest_distances_f64_device": (c_int, [P, P, c_uint32, P, P]),
+    "fcpwgb_contains": (c_int, [P, P, c_uint32, P]),
+    "fcpwgb_contains_device": (c_int, [P, P, c_uint32, P, P]),
+    "fcpwgb_has_line_of_sight": (c_int, [P, P, P, c_uint32, P]),
+    "fcpwgb_has_line_of_sight_device": (c_int, [P, P, P, c_uint32, P, P]),
     "fcpwgb_gpu_batch_create": (c_int, [c_int, c_int, C.POINTER(c_void_p)]),
     "fcpwgb_gpu_batch_destroy": (None, [P]),
     "fcpwgb_gpu_batch_set_scenes": (c_int, [P, P, c_uint32]),

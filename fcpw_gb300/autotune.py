@@ -4,8 +4,8 @@ branching factor (2/4/8), the child box precision (8/16/32 bits) and the
 schedule (a thread per query, persistent blocks, or warp packets); stage 2
 tries merged leaves (subtrees of up to 6, 8 or 12 primitives as one leaf) on
 the stage-1 winner; stage 3, for the one-thread-per-query schedules, the
-number of stack entries per thread kept in shared memory (0, 8, 32; 16 is
-the default)."""
+stack placement: 16 entries per thread in shared memory (the default) or the
+whole stack in local memory."""
 from __future__ import annotations
 
 import itertools
@@ -13,14 +13,12 @@ import itertools
 # schedule: "thread" = one thread per query, "persistent" = persistent blocks
 # with neighbour seeding, "packet" = the queries of a warp traverse together
 DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "persistent", "packet"],
-                 "leaf_size": [6, 8, 12], "short_stack": [0, 8, 32]}
+                 "leaf_size": [6, 8, 12], "short_stack": [0]}
 
 
 def candidates(space=None, sort_queries=True, precise=True):
     """The stage-1 grid (leaf_size 0, short_stack 16)."""
     space = dict(DEFAULT_SPACE, **(space or {}))
-    if "persistent" in (space or {}) and "schedule" not in (space or {}):  # older spelling
-        space["schedule"] = ["persistent" if p else "thread" for p in space["persistent"]]
     for b, q, sch in itertools.product(space["branching"], space["bits"], space["schedule"]):
         yield {"branching": b, "bits": q, "persistent": sch == "persistent", "packet": sch == "packet",
                "sort_queries": sort_queries, "precise": precise, "leaf_size": 0, "short_stack": 16}

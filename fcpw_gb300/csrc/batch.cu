@@ -390,8 +390,8 @@ extern "C" int fcpwgb_gpu_batch_set_traversal(fcpwgb_gpu_batch *b, const fcpwgb_
     if (c->block_size != 0 && c->block_size != 128)
         return setError(FCPWGB_ERR_UNSUPPORTED, "block_size must be 128 (or 0 for the default)");
     if (c->leaf_size < 0 || c->leaf_size > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf_size must be 0..15");
-    if (c->short_stack < 0 || c->short_stack > 32)
-        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0..32");
+    if (c->short_stack != 0 && c->short_stack != 16)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0 or 16");
     b->dropGraph();
     b->cfg.branching = c->branching;
     b->cfg.bits = c->bits;

@@ -696,8 +696,8 @@ extern "C" int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *s, const fcpwgb_
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "bits must be 8, 16 or 32");
     if (c->block_size != 128) return setError(FCPWGB_ERR_UNSUPPORTED, "the wide kernels run 128-thread blocks");
     if (c->leaf_size < 0 || c->leaf_size > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf_size must be 0..15");
-    if (c->short_stack < 0 || c->short_stack > 32)
-        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0..32");
+    if (c->short_stack != 0 && c->short_stack != 16)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0 or 16");
     WideConfig w;
     w.branching = c->branching;
     w.bits = c->bits;
@@ -842,4 +842,52 @@ extern "C" int fcpwgb_closest_distances_f64_device(fcpwgb_gpu_scene *s, const fc
     FCPWGB_CUDA(launchBruteF64(s->dim, (const unsigned char *)s->prims.ptr, s->nPrims, (const DevSphere *)spheres, n,
                                distances, s->pick(stream)));
     return FCPWGB_OK;
+}
+
+// --------------------------------------------- contains / line of sight
+extern "C" int fcpwgb_contains_device(fcpwgb_gpu_scene *s, const fcpwgb_float3 *points, uint32_t n, uint32_t *result,
+                                      void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > 0 && (!points || !result)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL point or result array");
+    FCPWGB_CUDA(launchContains(s->view(), (const float *)points, n, result, s->pick(stream)));
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_contains(fcpwgb_gpu_scene *s, const fcpwgb_float3 *points, uint32_t n, uint32_t *result) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n == 0) return FCPWGB_OK;
+    if (!points || !result) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL point or result array");
+    HostQuery h{s};
+    size_t ob = (size_t)n * sizeof(uint32_t);
+    if ((rc = h.begin(points, (size_t)n * 12, nullptr, 0, ob))) return rc;
+    FCPWGB_CUDA(launchContains(s->view(), (const float *)s->qIn0.ptr, n, (uint32_t *)s->qOut.ptr, s->stream));
+    return h.finish(result, ob);
+}
+
+extern "C" int fcpwgb_has_line_of_sight_device(fcpwgb_gpu_scene *s, const fcpwgb_float3 *points_a,
+                                               const fcpwgb_float3 *points_b, uint32_t n, uint32_t *result,
+                                               void *stream) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > 0 && (!points_a || !points_b || !result))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL point or result array");
+    FCPWGB_CUDA(launchLineOfSight(s->view(), (const float *)points_a, (const float *)points_b, n, result,
+                                  s->pick(stream)));
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_has_line_of_sight(fcpwgb_gpu_scene *s, const fcpwgb_float3 *points_a,
+                                        const fcpwgb_float3 *points_b, uint32_t n, uint32_t *result) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n == 0) return FCPWGB_OK;
+    if (!points_a || !points_b || !result) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL point or result array");
+    HostQuery h{s};
+    size_t ob = (size_t)n * sizeof(uint32_t);
+    if ((rc = h.begin(points_a, (size_t)n * 12, points_b, (size_t)n * 12, ob))) return rc;
+    FCPWGB_CUDA(launchLineOfSight(s->view(), (const float *)s->qIn0.ptr, (const float *)s->qIn1.ptr, n,
+                                  (uint32_t *)s->qOut.ptr, s->stream));
+    return h.finish(result, ob);
 }

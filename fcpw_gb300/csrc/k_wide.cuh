@@ -202,39 +202,31 @@ template<> FCPWGB_D void sortNetwork<8>(uint32_t (&k)[8]) {
 }
 
 // Per-thread traversal stack of kWideStack entries (node reference + the
-// child's distance bound). The first `shortN` entries (a launch parameter,
-// 0..kMaxShortStack) live in dynamic shared memory, entry k of thread t at
-// [k * 128 + t] so that a warp's accesses fall in distinct banks; deeper
-// entries go to local memory, which only deep traversals touch. A whole stack
-// in local memory (1 KB per thread) does not fit the L1 of a fully occupied
-// SM and its pushes and pops reach L2 and DRAM.
-constexpr int kMaxShortStack = 32;
+// child's distance bound). With SHORT = 16 the first 16 entries live in
+// shared memory, entry k of thread t at [k * 128 + t] so that a warp's
+// accesses fall in distinct banks, and deeper entries go to local memory,
+// which only deep traversals touch; with SHORT = 0 the whole stack is in
+// local memory. A whole stack in local memory (1 KB per thread) does not fit
+// the L1 of a fully occupied SM and its pushes and pops reach L2 and DRAM.
+constexpr int kShortStack = 16;
 constexpr int kWideBlock = 128;  // threads per block of the wide kernels
-struct WideStack {
+template<int SHORT> struct WideStack {
     uint32_t *sRef;  // shared, stride kWideBlock
     float *sD;
-    int shortN;
-    uint32_t lRef[kWideStack];
-    float lD[kWideStack];
-    // dynamic shared memory: shortN * 128 references, then shortN * 128 distances
-    FCPWGB_D void bind(unsigned char *smem, int n) {
-        shortN = n;
-        sRef = reinterpret_cast<uint32_t *>(smem) + threadIdx.x;
-        sD = reinterpret_cast<float *>(smem) + (size_t)n * kWideBlock + threadIdx.x;
-    }
+    uint32_t lRef[kWideStack - SHORT];
+    float lD[kWideStack - SHORT];
     FCPWGB_D void push(int sp, uint32_t ref, float d) {
-        if (sp < shortN) {
+        if (sp < SHORT) {
             sRef[sp * kWideBlock] = ref;
             sD[sp * kWideBlock] = d;
         } else {
-            lRef[sp - shortN] = ref;
-            lD[sp - shortN] = d;
+            lRef[sp - SHORT] = ref;
+            lD[sp - SHORT] = d;
         }
     }
-    FCPWGB_D float dist(int sp) const { return sp < shortN ? sD[sp * kWideBlock] : lD[sp - shortN]; }
-    FCPWGB_D uint32_t ref(int sp) const { return sp < shortN ? sRef[sp * kWideBlock] : lRef[sp - shortN]; }
+    FCPWGB_D float dist(int sp) const { return sp < SHORT ? sD[sp * kWideBlock] : lD[sp - SHORT]; }
+    FCPWGB_D uint32_t ref(int sp) const { return sp < SHORT ? sRef[sp * kWideBlock] : lRef[sp - SHORT]; }
 };
-inline size_t wideStackSmemBytes(int shortN) { return (size_t)shortN * kWideBlock * 8; }
 
 // Traversal statistics (expansions, tests, warp loads): compiled in only for
 // the counting launches, so the timed kernels carry no counter registers.
@@ -293,10 +285,10 @@ template<> struct NearTie<true> {  // two registers; the band is recomputed from
 // `root` is the tree's root record (always an inner record); `found`/`best`/
 // `selected`/`r2` may arrive holding a candidate already tested (a seed).
 // Boxes are pruned against rp2: r2, or with TRACK r2 widened by the band.
-template<int W, int BITS, class Prim, bool TRACK, bool STATS>
+template<int W, int BITS, class Prim, bool TRACK, bool STATS, int SHORT>
 FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigned char *__restrict__ prims,
                           uint32_t root, float3 c, float r2, bool found, DevInteraction &best, uint32_t &selected,
-                          NearTie<TRACK> &tie, WideStack &st, uint32_t *errorWord, Count<STATS> &nExpanded,
+                          NearTie<TRACK> &tie, WideStack<SHORT> &st, uint32_t *errorWord, Count<STATS> &nExpanded,
                           Count<STATS> &nTests) {
     int sp = 0;
     uint32_t cur = root;
@@ -437,7 +429,7 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
 // radius instead of FLT_MAX. Any tested primitive is a valid candidate, so the
 // result is the same closest distance (ties may pick another primitive).
 constexpr uint32_t kWidePool = 256;
-template<int W, int BITS, class Prim, bool PRECISE, bool PERSISTENT, bool STATS>
+template<int W, int BITS, class Prim, bool PRECISE, bool PERSISTENT, bool STATS, int SHORT>
 __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigned char *__restrict__ nodes,
                                                                 const unsigned char *__restrict__ prims,
                                                                 const DevSphere *__restrict__ spheres,
@@ -445,11 +437,12 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                                                                 const uint32_t *__restrict__ roots,
                                                                 DevInteraction *__restrict__ out, uint32_t n,
                                                                 int recordNormal, uint32_t *counter,
-                                                                uint32_t *errorWord, unsigned long long *stats,
-                                                                int shortStack) {
-    extern __shared__ __align__(16) unsigned char wideSmem[];
-    WideStack st;
-    st.bind(wideSmem, shortStack);
+                                                                uint32_t *errorWord, unsigned long long *stats) {
+    __shared__ uint32_t sRef[SHORT > 0 ? SHORT * kWideBlock : 1];
+    __shared__ float sD[SHORT > 0 ? SHORT * kWideBlock : 1];
+    WideStack<SHORT> st;
+    st.sRef = sRef + threadIdx.x;
+    st.sD = sD + threadIdx.x;
     Count<STATS> tExp, tTests;
     if (!PERSISTENT) {
         uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
@@ -460,7 +453,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
             uint32_t selected = kUintMax;
             uint32_t root = roots ? __ldg(roots + i) : 0u;
             NearTie<PRECISE> tie;
-            bool found = wideClosest<W, BITS, Prim, PRECISE, STATS>(nodes, prims, root, c, s4.w, false, best, selected, tie,
+            bool found = wideClosest<W, BITS, Prim, PRECISE, STATS, SHORT>(nodes, prims, root, c, s4.w, false, best, selected, tie,
                                                              st, errorWord, tExp, tTests);
             finishQuery<Prim, PRECISE>(prims, perm, out, i, c, s4.w, found, selected, recordNormal, best, tie);
         }
@@ -499,7 +492,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                         found = true;
                     }
                 }
-                found = wideClosest<W, BITS, Prim, PRECISE, STATS>(nodes, prims, root, c, r2, found, best, selected, tie,
+                found = wideClosest<W, BITS, Prim, PRECISE, STATS, SHORT>(nodes, prims, root, c, r2, found, best, selected, tie,
                                                             st, errorWord, tExp, tTests);
                 seed = found ? selected : kUintMax;
                 seedRoot = root;
@@ -707,12 +700,13 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
                                                        const DevRay *__restrict__ rays,
                                                        const uint32_t *__restrict__ perm,
                                                        DevInteraction *__restrict__ out, uint32_t n, int occl,
-                                                       uint32_t *errorWord, unsigned long long *stats,
-                                                       int shortStack) {
+                                                       uint32_t *errorWord, unsigned long long *stats) {
     constexpr uint32_t kSlotMask = W - 1;
-    extern __shared__ __align__(16) unsigned char wideSmem[];
-    WideStack st;
-    st.bind(wideSmem, shortStack);
+    __shared__ uint32_t sRef[kShortStack * kWideBlock];
+    __shared__ float sD[kShortStack * kWideBlock];
+    WideStack<kShortStack> st;
+    st.sRef = sRef + threadIdx.x;
+    st.sD = sD + threadIdx.x;
     const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
     if (i >= n) return;
     const unsigned char *rp = reinterpret_cast<const unsigned char *>(rays + i);
@@ -833,14 +827,25 @@ cudaError_t launchWideClosestKernel(const WideLaunch &l, cudaStream_t s) {
     if (l.packet)
         kWidePacketClosestPoint<W, B, Prim, PRECISE, STATS><<<g, b, 0, s>>>(
             l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.errorWord, l.stats);
-    else if (l.counter)
-        kWideClosestPoint<W, B, Prim, PRECISE, true, STATS><<<g, b, wideStackSmemBytes(l.shortStack), s>>>(
-            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats,
-            l.shortStack);
-    else
-        kWideClosestPoint<W, B, Prim, PRECISE, false, STATS><<<g, b, wideStackSmemBytes(l.shortStack), s>>>(
-            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord, l.stats,
-            l.shortStack);
+    else if (l.counter) {
+        if (l.shortStack)
+            kWideClosestPoint<W, B, Prim, PRECISE, true, STATS, kShortStack><<<g, b, 0, s>>>(
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.stats);
+        else
+            kWideClosestPoint<W, B, Prim, PRECISE, true, STATS, 0><<<g, b, 0, s>>>(
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.stats);
+    } else {
+        if (l.shortStack)
+            kWideClosestPoint<W, B, Prim, PRECISE, false, STATS, kShortStack><<<g, b, 0, s>>>(
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.stats);
+        else
+            kWideClosestPoint<W, B, Prim, PRECISE, false, STATS, 0><<<g, b, 0, s>>>(
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.stats);
+    }
     return cudaGetLastError();
 }
 template<int W, int B, class Prim>
@@ -872,8 +877,7 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
         if (l.n == 0) return cudaSuccess;                                                                          \
         dim3 g((l.n + 127) / 128), b(128);                                                                         \
         auto go = [&](auto kern) {                                                                                 \
-            kern<<<g, b, wideStackSmemBytes(l.shortStack), s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n,      \
-                                                                l.occl, l.errorWord, l.stats, l.shortStack);      \
+            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.errorWord, l.stats);     \
         };                                                                                                         \
         if (dim == 3) {                                                                                            \
             if (bits == 8) go(kWideRay<W, 8, Tri48Prim>);                                                          \

@@ -35,6 +35,12 @@ cudaError_t launchSilhouetteBinary(const SceneView &v, const DevSphere *spheres,
                                    float precision, cudaStream_t s);
 cudaError_t launchFillDefault(DevInteraction *out, uint32_t n, cudaStream_t s);
 
+// Scene::contains and hasLineOfSight with the reference CPU arithmetic (k_inside.cu);
+// points are 3 floats each, results 0 / 1 (contains: 2 when a ray had too many hits)
+cudaError_t launchContains(const SceneView &v, const float *points, uint32_t n, uint32_t *out, cudaStream_t s);
+cudaError_t launchLineOfSight(const SceneView &v, const float *a, const float *b, uint32_t n, uint32_t *out,
+                              cudaStream_t s);
+
 // FP64 brute-force closest distance of every query over all primitives (k_check.cu)
 cudaError_t launchBruteF64(int dim, const unsigned char *prims, uint32_t nPrims, const DevSphere *spheres,
                            uint32_t n, double *out, cudaStream_t s);
@@ -51,7 +57,7 @@ struct WideLaunch {
     int recordNormal = 0;
     uint32_t *counter = nullptr;           // work counter (zero on entry) for persistent blocks, or NULL
     int packet = 0;                        // 1: warp packets (kWidePacketClosestPoint), counter unused
-    int shortStack = 16;                   // per-thread stack entries in shared memory (thread schedules), 0..32
+    int shortStack = 16;                   // per-thread stack entries in shared memory (thread schedules): 0 or 16
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;   // traversal statistics, or NULL
     uint32_t grid = 0;
@@ -70,7 +76,6 @@ struct WideRayLaunch {
     int occl = 0;
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;
-    int shortStack = 16;
 };
 template<int W> cudaError_t launchWideRayT(int bits, int dim, const WideRayLaunch &l, cudaStream_t s);
 cudaError_t launchWideRays(int W, int bits, int dim, const WideRayLaunch &l, cudaStream_t s);

@@ -140,7 +140,6 @@ int GpuScene::wideRays(const DevRay *r, DevInteraction *out, uint32_t n, int occ
     l.n = n;
     l.occl = occl;
     l.errorWord = (uint32_t *)errorWord.ptr;
-    l.shortStack = wideConfig.shortStack;
     cudaError_t e;
     if (wideConfig.sortQueries && n >= 4096) {
         if ((rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;

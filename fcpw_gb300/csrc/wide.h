@@ -29,7 +29,7 @@ struct WideConfig {
     int precise = 1;     // recompute the winning primitive's distance in FP64
     int packet = 0;      // traverse the 32 queries of a warp as one packet
     int leafSize = 0;    // > 0: binary subtrees of at most this many primitives collapse into one leaf
-    int shortStack = 16; // traversal stack entries per thread held in shared memory (thread schedules)
+    int shortStack = 16; // traversal stack entries per thread in shared memory (thread schedules): 0 or 16
 };
 
 constexpr int wideHeaderBytes(int bits) { return bits == 32 ? 0 : 16; }

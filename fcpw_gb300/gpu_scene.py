@@ -207,7 +207,7 @@ class _GPUScene:
         branching 0 is the reference-order binary traversal; 2/4/8 use a wide
         tree with 32-, 16- or 8-bit child boxes; packet walks the queries of a
         warp together; leaf_size merges small subtrees into wide leaves;
-        short_stack is the per-thread stack depth kept in shared memory."""
+        short_stack (0 or 16) is the per-thread stack depth kept in shared memory."""
         from ._lib import TraversalConfig
         cfg = TraversalConfig(int(branching), int(bits), 128, int(bool(sort_queries)), int(bool(persistent)),
                               int(bool(precise)), int(bool(packet)), int(leaf_size), int(short_stack))
@@ -402,6 +402,50 @@ class _GPUScene:
         check(lib().fcpwgb_intersect_rays_device(self._h, rays.data_ptr(), raw.data_ptr(), n,
                                                  int(bool(check_for_occlusion)), self._stream(rays)))
         return _split_records(raw)
+
+    # -- inside / line of sight (Scene::contains / hasLineOfSight, CPU-only in the reference)
+    @staticmethod
+    def _points3(points) -> np.ndarray:
+        p = np.asarray(points, np.float32)
+        if p.ndim != 2 or p.shape[1] not in (2, 3):
+            raise ValueError("points must have shape (N, 2) or (N, 3)")
+        out = np.zeros((len(p), 3), np.float32)
+        out[:, : p.shape[1]] = p
+        return out
+
+    def contains(self, points) -> np.ndarray:
+        """1 where a point is inside the (watertight) boundary, else 0 (fcpw.inl:1443-1460)."""
+        pts = self._points3(points)
+        res = np.zeros(len(pts), np.uint32)
+        check(lib().fcpwgb_contains(self._h, ptr(pts), len(pts), ptr(res)))
+        return res
+
+    def has_line_of_sight(self, points_a, points_b) -> np.ndarray:
+        """1 where the segment between the paired points hits no primitive (fcpw.inl:1501-1520)."""
+        a, b = self._points3(points_a), self._points3(points_b)
+        if len(a) != len(b):
+            raise ValueError("points_a and points_b must have the same length")
+        res = np.zeros(len(a), np.uint32)
+        check(lib().fcpwgb_has_line_of_sight(self._h, ptr(a), ptr(b), len(a), ptr(res)))
+        return res
+
+    def contains_tensor(self, points, out=None):
+        """points: (N, 3) float32 CUDA tensor; returns an int32 CUDA tensor of 0/1."""
+        import torch
+        self._check_tensor(points, 3)
+        res = out if out is not None else torch.empty(points.shape[0], dtype=torch.int32, device=points.device)
+        check(lib().fcpwgb_contains_device(self._h, points.data_ptr(), points.shape[0], res.data_ptr(),
+                                           self._stream(points)))
+        return res
+
+    def has_line_of_sight_tensor(self, points_a, points_b, out=None):
+        import torch
+        self._check_tensor(points_a, 3)
+        self._check_tensor(points_b, 3)
+        res = out if out is not None else torch.empty(points_a.shape[0], dtype=torch.int32, device=points_a.device)
+        check(lib().fcpwgb_has_line_of_sight_device(self._h, points_a.data_ptr(), points_b.data_ptr(),
+                                                    points_a.shape[0], res.data_ptr(), self._stream(points_a)))
+        return res
 
     def closest_distances_f64_tensor(self, spheres):
         """FP64 brute-force closest distances of the (N, 4) query tensor's centres over

@@ -216,7 +216,7 @@ int fcpwgb_gpu_scene_update_vertices_device_static(fcpwgb_gpu_scene *scene, cons
  * is then ignored); leaf_size > 0 collapses binary subtrees of at most that
  * many primitives (up to 15) into one wide leaf; short_stack is the number of
  * traversal-stack entries per thread kept in shared memory by the
- * one-thread-per-query schedules (0..32; deeper entries in local memory).
+ * one-thread-per-query schedules (0 or 16; the others in local memory).
  * Defaults: {0, 32, 128, 1, 1, 1, 0, 0, 16}. Results differ from the binary
  * order only on equidistant ties (and, with precise, by the FP32 rounding
  * removed). */
@@ -229,7 +229,7 @@ typedef struct {
     int precise;       /* 0 or 1 */
     int packet;        /* 0 or 1 */
     int leaf_size;     /* 0 (binary leaves) or 1..15 */
-    int short_stack;   /* 0..32 */
+    int short_stack;   /* 0 or 16 */
 } fcpwgb_traversal_config;
 int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *scene, const fcpwgb_traversal_config *config);
 int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *scene, fcpwgb_traversal_config *config);
@@ -319,6 +319,24 @@ int fcpwgb_gpu_scene_check_errors(fcpwgb_gpu_scene *scene, uint32_t *error_word)
  * arrays, asynchronous on stream; O(n x primitives), n <= 2^24. */
 int fcpwgb_closest_distances_f64_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                         uint32_t n, double *distances, void *stream);
+
+/* ------------------------------------------- inside / line of sight ----- */
+/* Scene<DIM>::contains and hasLineOfSight (fcpw.inl:1443-1460, 1501-1520;
+ * Aggregate::contains / hasLineOfSight, core/primitive.h:173-207), CPU-only in
+ * the reference, as GPU batches over the transferred binary tree with the
+ * reference CPU arithmetic (results equal the reference's). contains: 1 when
+ * rays from the point along +x and +y both cross the boundary an odd number
+ * of times (a watertight boundary is assumed, as in the reference), else 0;
+ * 2 when a ray had more than 64 hits. has_line_of_sight: 1 when the segment
+ * from points_a[i] to points_b[i] hits no primitive. Points are 3 floats (z
+ * ignored in 2D). Host arrays: synchronous; _device: asynchronous on stream. */
+int fcpwgb_contains(fcpwgb_gpu_scene *scene, const fcpwgb_float3 *points, uint32_t n, uint32_t *result);
+int fcpwgb_contains_device(fcpwgb_gpu_scene *scene, const fcpwgb_float3 *points, uint32_t n, uint32_t *result,
+                           void *stream);
+int fcpwgb_has_line_of_sight(fcpwgb_gpu_scene *scene, const fcpwgb_float3 *points_a,
+                             const fcpwgb_float3 *points_b, uint32_t n, uint32_t *result);
+int fcpwgb_has_line_of_sight_device(fcpwgb_gpu_scene *scene, const fcpwgb_float3 *points_a,
+                                    const fcpwgb_float3 *points_b, uint32_t n, uint32_t *result, void *stream);
 
 /* ------------------------------------------------- batches of scenes ----- */
 /* No counterpart in the reference (its GPUScene holds one object). A batch

@@ -20,6 +20,9 @@
  *     silhouette_edges.inl:83-143, silhouette_vertices.inl:59-117
  *   - Bvh sphere sampling, bvh.inl:1140-1288, Triangle/LineSegment::samplePoint
  *   - Bvh refit boxes, bvh.inl:548-599; mergeBoundingCones, bounding_volumes.h:334-387
+ *   - Aggregate::contains / hasLineOfSight, core/primitive.h:173-207, with the
+ *     all-hits ray traversal bvh.inl:888-1029 and removeDuplicates,
+ *     core/interaction.h:20-25,75-94
  * plus an FP64 brute force used as the accuracy yardstick.
  *
  * Inputs are the flattened tree and records in the reference's GPU interop
@@ -503,6 +506,114 @@ static oint ray_bvh_one(int dim, int snch, const void *nodes, const void *prims,
     return best;
 }
 
+/* ------------------------------------------- contains / line of sight */
+/* all hits of a ray (bvh.inl:888-1029 with recordAllHits: no tMax pruning,
+   every primitive hit kept), sorted by distance, consecutive duplicates
+   (|d - d'| < 1e-6 and |p - p'|^2 < 1e-6, core/interaction.h:20-25,75-94)
+   removed; returns the count, or -1 past OHITS hits */
+#define OHITS 256
+static int ray_hit_count(int dim, int snch, const void *nodes, const void *prims, oray r) {
+    float ds[OHITS];
+    of3 ps[OHITS];
+    int nh = 0, i, j, count;
+    uint32_t stackNode[OSTACK];
+    float stackDist[OSTACK];
+    float bh[4];
+    obox root = load_node(snch, nodes, 0);
+    if (box_ray(dim, root.pMin, root.pMax, &r, &bh[0], &bh[1])) {
+        int sp = 0;
+        stackNode[0] = 0;
+        stackDist[0] = bh[0];
+        while (sp >= 0) {
+            uint32_t ni = stackNode[sp];
+            obox node;
+            sp--;
+            node = load_node(snch, nodes, ni);
+            if (node.nPrims > 0) {
+                uint32_t p;
+                for (p = 0; p < node.nPrims; p++) {
+                    oprim pr = load_prim(dim, prims, node.offset + p);
+                    oint c = default_interaction();
+                    int hit = dim == 3 ? intersect_triangle(pr.pa, pr.pb, pr.pc, &r, 0, &c)
+                                       : intersect_segment(pr.pa, pr.pb, &r, 0, &c);
+                    if (hit) {
+                        if (nh >= OHITS) return -1;
+                        ds[nh] = c.d;
+                        ps[nh] = c.p;
+                        nh++;
+                    }
+                }
+            } else {
+                uint32_t li = ni + 1, ri = ni + node.offset;
+                obox l = load_node(snch, nodes, li), rr = load_node(snch, nodes, ri);
+                int hit0 = box_ray(dim, l.pMin, l.pMax, &r, &bh[0], &bh[1]);
+                int hit1 = box_ray(dim, rr.pMin, rr.pMax, &r, &bh[2], &bh[3]);
+                if (sp + 2 >= OSTACK) return -1;
+                if (hit0 && hit1) {
+                    uint32_t closer = li, other = ri;
+                    if (bh[2] < bh[0]) {
+                        float t = bh[0]; bh[0] = bh[2]; bh[2] = t;
+                        closer = ri; other = li;
+                    }
+                    sp++; stackNode[sp] = other; stackDist[sp] = bh[2];
+                    sp++; stackNode[sp] = closer; stackDist[sp] = bh[0];
+                } else if (hit0) {
+                    sp++; stackNode[sp] = li; stackDist[sp] = bh[0];
+                } else if (hit1) {
+                    sp++; stackNode[sp] = ri; stackDist[sp] = bh[2];
+                }
+            }
+        }
+    }
+    /* sort by distance (insertion sort; equal distances are duplicates or
+       coincident hits, whose order does not change the count) */
+    for (i = 1; i < nh; i++) {
+        float d = ds[i];
+        of3 p = ps[i];
+        for (j = i - 1; j >= 0 && ds[j] > d; j--) { ds[j + 1] = ds[j]; ps[j + 1] = ps[j]; }
+        ds[j + 1] = d;
+        ps[j + 1] = p;
+    }
+    count = nh;
+    for (i = 0; i + 1 < nh; i++) {
+        of3 dp = sub3(ps[i], ps[i + 1]);
+        if (fabsf(ds[i] - ds[i + 1]) < 1e-6f && dotd(dim, dp, dp) < 1e-6f) count--;
+    }
+    return count;
+}
+
+static oray make_ray(int dim, of3 o, of3 d, float tMax) {
+    oray r;
+    r.o = o;
+    r.d = d;
+    r.dInv = v3(1.0f / d.x, 1.0f / d.y, dim == 3 ? 1.0f / d.z : 1.0f / d.z);
+    r.tMax = tMax;
+    return r;
+}
+
+/* Aggregate::contains, core/primitive.h:173-193: rays along +x and +y, inside
+   when both cross the boundary an odd number of times; -1 on overflow */
+static int contains_one(int dim, int snch, const void *nodes, const void *prims, of3 x) {
+    int h1 = ray_hit_count(dim, snch, nodes, prims, make_ray(dim, x, v3(1.0f, 0.0f, 0.0f), OMAXF));
+    int h2 = ray_hit_count(dim, snch, nodes, prims, make_ray(dim, x, v3(0.0f, 1.0f, 0.0f), OMAXF));
+    if (h1 < 0 || h2 < 0) return -1;
+    return (h1 % 2 == 1 && h2 % 2 == 1) ? 1 : 0;
+}
+
+/* Aggregate::hasLineOfSight, core/primitive.h:196-207: an occlusion ray from xi
+   towards xj with tMax = |xj - xi| */
+static int line_of_sight_one(int dim, int snch, const void *nodes, const void *prims, of3 xi, of3 xj) {
+    of3 dir = sub3(xj, xi);
+    float dNorm = normd(dim, dir);
+    int hit;
+    oray r;
+    dir = div3(dir, dNorm);
+    if (dim == 2) dir.z = 0.0f;
+    r = make_ray(dim, xi, dir, dNorm);
+    ray_bvh_one(dim, snch, nodes, prims, r, 1, &hit);
+    return hit ? 0 : 1;
+}
+
 /* ------------------------------------------------------------ silhouettes */
 /* BoundingCone::overlap, bounding_volumes.h:262-321 */
 static float project_to_plane(int dim, of3 n, of3 e) {
@@ -957,6 +1068,17 @@ static void run_range(ojob *j) {
                                                    ((const osphere *)j->queries)[q],
                                                    ((const uint32_t *)j->aux)[q] != 0, j->f0, j->f1);
                 break;
+            case 7: {
+                const of3 *pts = (const of3 *)j->queries;
+                int r = contains_one(j->dim, j->snch, j->nodes, j->prims, pts[q]);
+                j->u32out[q] = r < 0 ? 2u : (uint32_t)r;
+                break;
+            }
+            case 8: {
+                const of3 *a = (const of3 *)j->queries, *b = (const of3 *)j->aux;
+                j->u32out[q] = (uint32_t)line_of_sight_one(j->dim, j->snch, j->nodes, j->prims, a[q], b[q]);
+                break;
+            }
             case 6: j->out[q] = sphere_sample_bvh_one(j->dim, j->snch, j->nodes, j->prims,
                                                       ((const osphere *)j->queries)[q], ((const of3 *)j->aux)[q],
                                                       &j->hits[q]);
@@ -1080,4 +1202,22 @@ int oracle_record_sizes(int *sizes) {
     sizes[3] = (int)sizeof(oseg); sizes[4] = (int)sizeof(overt); sizes[5] = (int)sizeof(oedge);
     sizes[6] = (int)sizeof(osphere); sizes[7] = (int)sizeof(oray); sizes[8] = (int)sizeof(oint);
     return 9;
+}
+
+/* contains: out[q] = 1 inside, 0 outside, 2 if a ray had more than OHITS hits */
+int oracle_contains_bvh(int dim, int snch, const void *nodes, const void *prims, const void *points, uint32_t n,
+                        uint32_t *out, int nthreads) {
+    ojob j;
+    memset(&j, 0, sizeof(j));
+    j.kind = 7; j.dim = dim; j.snch = snch; j.nodes = nodes; j.prims = prims; j.queries = points; j.u32out = out;
+    return run_threaded(j, n, nthreads);
+}
+
+int oracle_line_of_sight_bvh(int dim, int snch, const void *nodes, const void *prims, const void *points_a,
+                             const void *points_b, uint32_t n, uint32_t *out, int nthreads) {
+    ojob j;
+    memset(&j, 0, sizeof(j));
+    j.kind = 8; j.dim = dim; j.snch = snch; j.nodes = nodes; j.prims = prims; j.queries = points_a;
+    j.aux = points_b; j.u32out = out;
+    return run_threaded(j, n, nthreads);
 }

@@ -33,6 +33,8 @@ def _load():
             "oracle_sphere_sample_bvh": [i, i, P, P, P, P, u, P, P, i],
             "oracle_refit": [i, i, P, P, P],
             "oracle_prim_distance_f64": [i, P, u, P, P, u, P],
+            "oracle_contains_bvh": [i, i, P, P, P, u, P, i],
+            "oracle_line_of_sight_bvh": [i, i, P, P, P, P, u, P, i],
             "oracle_record_sizes": [P],
         }
         for name, args in sig.items():
@@ -79,6 +81,35 @@ def closest_points_brute_f64(dim, prims, spheres, nthreads=None):
     _load().oracle_closest_points_brute_f64(dim, _p(prims), len(prims), _p(spheres), len(spheres), _p(d), _p(idx),
                                             threads(nthreads))
     return d, idx
+
+
+def _pts3(points):
+    p = np.asarray(points, np.float32)
+    out = np.zeros((len(p), 3), np.float32)
+    out[:, : p.shape[1]] = p
+    return out
+
+
+def contains_bvh(dim, nodes, prims, points, nthreads=None):
+    """Aggregate::contains for every point: 1 inside, 0 outside (2 if a ray had
+    more hits than the oracle keeps)."""
+    R = _records()
+    snch = nodes.dtype == R.SNCH_NODE
+    pts = _pts3(points)
+    out = np.zeros(len(pts), np.uint32)
+    _load().oracle_contains_bvh(dim, int(snch), _p(nodes), _p(prims), _p(pts), len(pts), _p(out), threads(nthreads))
+    return out
+
+
+def line_of_sight_bvh(dim, nodes, prims, points_a, points_b, nthreads=None):
+    """Aggregate::hasLineOfSight for every pair: 1 visible, 0 occluded."""
+    R = _records()
+    snch = nodes.dtype == R.SNCH_NODE
+    a, b = _pts3(points_a), _pts3(points_b)
+    out = np.zeros(len(a), np.uint32)
+    _load().oracle_line_of_sight_bvh(dim, int(snch), _p(nodes), _p(prims), _p(a), _p(b), len(a), _p(out),
+                                     threads(nthreads))
+    return out
 
 
 def intersect_rays_bvh(dim, nodes, prims, rays, occlusion=False, nthreads=None):

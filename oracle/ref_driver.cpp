@@ -330,4 +330,39 @@ int ref_update_and_refit(void *h, const float *positions, int nV) {
     return 0;
 }
 
+// Scene<DIM>::contains / hasLineOfSight (fcpw.inl:1443-1460, 1501-1520): points are
+// 3 floats each (the first DIM used); out receives 0 or 1
+int ref_contains(void *h, const float *points, int n, uint32_t *out) {
+    RefScene *r = (RefScene *)h;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        std::vector<Vector<D>> pts(n);
+        for (int q = 0; q < n; q++) pts[q] = vecOf<D>(points + 3 * q);
+        std::vector<uint32_t> res;
+        scene.contains(pts, res);
+        for (int q = 0; q < n; q++) out[q] = res[q];
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return 0;
+}
+
+int ref_line_of_sight(void *h, const float *pa, const float *pb, int n, uint32_t *out) {
+    RefScene *r = (RefScene *)h;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        std::vector<Vector<D>> a(n), b(n);
+        for (int q = 0; q < n; q++) {
+            a[q] = vecOf<D>(pa + 3 * q);
+            b[q] = vecOf<D>(pb + 3 * q);
+        }
+        std::vector<uint32_t> res;
+        scene.hasLineOfSight(a, b, res);
+        for (int q = 0; q < n; q++) out[q] = res[q];
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return 0;
+}
+
 }  // extern "C"

@@ -33,7 +33,8 @@ def _load():
         _lib.ref_scene_destroy.argtypes = [P]
         for name, args in {"ref_export": [P, P, P, P, P], "ref_closest_points": [P, P, i, i, P, P],
                            "ref_intersect_rays": [P, P, i, i, P, P], "ref_silhouettes": [P, P, P, i, f, f, P],
-                           "ref_sphere_sample": [P, P, P, i, P, P], "ref_update_and_refit": [P, P, i]}.items():
+                           "ref_sphere_sample": [P, P, P, i, P, P], "ref_update_and_refit": [P, P, i],
+                           "ref_contains": [P, P, i, P], "ref_line_of_sight": [P, P, P, i, P]}.items():
             fn = getattr(_lib, name)
             fn.restype = i
             fn.argtypes = args
@@ -104,6 +105,25 @@ class RefScene:
         rn = np.ascontiguousarray(rand_nums, np.float32)
         _load().ref_sphere_sample(self._h, _p(self._sph(spheres)), _p(rn), len(spheres), _p(out), _p(hit))
         return out, hit.astype(bool)
+
+    @staticmethod
+    def _pts3(points):
+        p = np.asarray(points, np.float32)
+        out = np.zeros((len(p), 3), np.float32)
+        out[:, : p.shape[1]] = p
+        return out
+
+    def contains(self, points):
+        pts = self._pts3(points)
+        out = np.zeros(len(pts), np.uint32)
+        _load().ref_contains(self._h, _p(pts), len(pts), _p(out))
+        return out
+
+    def line_of_sight(self, points_a, points_b):
+        a, b = self._pts3(points_a), self._pts3(points_b)
+        out = np.zeros(len(a), np.uint32)
+        _load().ref_line_of_sight(self._h, _p(a), _p(b), len(a), _p(out))
+        return out
 
     def update_and_refit(self, positions):
         pos = np.ascontiguousarray(positions, np.float32)

@@ -66,6 +66,10 @@ def make(name, dim, verts, idx, aggregate, silhouettes, box, n=1500):
     so, sh = ref.sphere_sample(R.make_spheres(c, rr), rn)
     out.update(ss_c=c, ss_r2=rr, ss_rand=rn, ss_out=so, ss_hit=sh)
 
+    # Scene::contains / hasLineOfSight (CPU-only in the reference; batched on the GPU here)
+    b = _queries(dim, n, lo, hi, SEED + 12)
+    out.update(in_points=pts, in_out=ref.contains(pts), los_a=pts, los_b=b, los_out=ref.line_of_sight(pts, b))
+
     if silhouettes:
         flip = (W.rng(SEED + 8).uniform(0, 1, n) < 0.5).astype(np.uint32)
         out.update(sil_points=pts, sil_flip=flip,

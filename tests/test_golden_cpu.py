@@ -95,3 +95,13 @@ def test_oracle_refit_boxes_bit_exact(fx):
     assert np.array_equal(got["pMin"], ref["pMin"]) and np.array_equal(got["pMax"], ref["pMax"])
     sp = R.make_spheres(fx["cp_points"], R.FLT_MAX)
     _same(O.closest_points_bvh(dim, got, fx["refit_prims"], sp), fx["refit_cp_out"])
+
+
+def test_oracle_contains_and_line_of_sight_bit_exact(fx):
+    """Scene::contains (two all-hits rays, duplicates removed) and
+    Scene::hasLineOfSight, against the reference's answers."""
+    dim = int(fx["dim"])
+    nodes, prims = fx["nodes"], fx["prims"]
+    assert np.array_equal(O.contains_bvh(dim, nodes, prims, fx["in_points"]), fx["in_out"])
+    assert np.array_equal(O.line_of_sight_bvh(dim, nodes, prims, fx["los_a"], fx["los_b"]), fx["los_out"])
+    assert 0 < fx["in_out"].sum() < len(fx["in_out"]) and 0 < fx["los_out"].sum() < len(fx["los_out"])

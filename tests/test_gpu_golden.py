@@ -100,3 +100,12 @@ def test_refit_boxes_bit_exact_with_reference(loaded):
     out = F.GPUInteractionList()
     g.find_closest_points(pts, np.full(len(pts), R.FLT_MAX, np.float32), out)
     compare_closest(dim, fx["refit_prims"], pts, out.array(), fx["refit_cp_out"], "closest point after refit")
+
+
+def test_contains_and_line_of_sight_equal_reference(loaded):
+    """Scene::contains / hasLineOfSight as GPU batches, computed with the
+    reference CPU arithmetic: equal to the reference's answers."""
+    fx, g, dim = loaded
+    assert np.array_equal(g.contains(fx["in_points"]), fx["in_out"])
+    assert np.array_equal(g.has_line_of_sight(fx["los_a"], fx["los_b"]), fx["los_out"])
+    assert g.check_errors() == 0

@@ -202,8 +202,8 @@ def test_precise_mode_near_ties_2d_within_1e6(packet):
     assert rel.max() <= 1e-6, f"max relative error {rel.max():.3e}"
 
 
-@pytest.mark.parametrize("leaf_size,short_stack,packet", [(8, 16, False), (12, 0, False), (6, 32, False),
-                                                          (8, 16, True), (0, 8, False)])
+@pytest.mark.parametrize("leaf_size,short_stack,packet", [(8, 16, False), (12, 0, False), (6, 16, False),
+                                                          (8, 16, True), (0, 0, False)])
 def test_leaf_size_and_stack_placement_match_oracle(torus, leaf_size, short_stack, packet):
     s, g, pts, ref, prims = torus
     g.set_traversal(4, 16, sort_queries=True, precise=False, packet=packet, leaf_size=leaf_size,
