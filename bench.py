@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven scenes measurement")
     ap.add_argument("--suite", action="store_true",
                     help="instead of the headline line, one line per other configuration of the scope")
-    ap.add_argument("--only", default="", help="with --suite: comma-separated subset of c1,rays,c3,sil3d")
+    ap.add_argument("--only", default="", help="with --suite: comma-separated subset of c1,rays,c3,sil3d,inside")
     return ap.parse_args()
 
 
@@ -433,6 +433,31 @@ def run_suite(args):
             n)
         lines.append({"config": f"3D silhouettes, torus 1,048,576 triangles (SNCH), {n:,} queries (flip 0)",
                       "queries": n, **times, "cpu_baseline": cpu})
+
+    # contains / line of sight (CPU-only in the reference) on the 1M-triangle torus
+    if want("inside"):
+        v, f, pts = make_workload(0, N_QUERIES)
+        s, _ = build_scene(v, f)
+        g = F.GPUScene3D("", False, device=0)
+        g.transfer_to_gpu(s)
+        n = len(pts)
+        pb = W.uniform_points(n, 3, -2.0, 2.0, W.SEED_BASE + 4004)
+        ta = torch.from_numpy(pts).to(dev)
+        tb = torch.from_numpy(pb).to(dev)
+        res = torch.empty(n, dtype=torch.int32, device=dev)
+        in_ms = timed(lambda: g.contains_tensor(ta, out=res))
+        inside = float(res.float().mean())
+        los_ms = timed(lambda: g.has_line_of_sight_tensor(ta, tb, out=res))
+        visible = float(res.float().mean())
+        nodes, prims, _ = s.cpu_bvh.export()
+        cpu_in = cpu_rate(lambda m: O.contains_bvh(3, nodes, prims, pts[:m], nthreads=threads), n)
+        cpu_los = cpu_rate(lambda m: O.line_of_sight_bvh(3, nodes, prims, pts[:m], pb[:m], nthreads=threads), n)
+        lines.append({"config": "contains, torus 1,048,576 triangles, 4,194,304 points (two all-hits rays each)",
+                      "queries": n, "gpu": {"queries_per_s": n / (in_ms / 1e3), "ms": in_ms},
+                      "inside_fraction": inside, "cpu_baseline": cpu_in})
+        lines.append({"config": "line of sight, torus 1,048,576 triangles, 4,194,304 point pairs", "queries": n,
+                      "gpu": {"queries_per_s": n / (los_ms / 1e3), "ms": los_ms}, "visible_fraction": visible,
+                      "cpu_baseline": cpu_los})
 
     for line in lines:
         print(json.dumps(line), flush=True)

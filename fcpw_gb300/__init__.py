@@ -9,11 +9,11 @@ from .batch import GPUSceneBatch2D, GPUSceneBatch3D
 from .gpu_scene import (GPUBoundingSphere, GPUBoundingSphereList, GPUFloat2, GPUFloat3, GPUFloat3List,
                         GPUInteraction, GPUInteractionList, GPURay, GPURayList, GPUScene2D, GPUScene3D,
                         TensorInteractions, Uint32List)
-from .scene import AggregateType, CpuBvh, PrimitiveType, Scene2D, Scene3D
+from .scene import AggregateType, CpuBvh, PrimitiveType, Scene2D, Scene3D, scene_file_info
 
 __all__ = [
     "AggregateType", "PrimitiveType", "Scene2D", "Scene3D", "CpuBvh", "GPUScene2D", "GPUScene3D",
     "GPUFloat2", "GPUFloat3", "GPURay", "GPUBoundingSphere", "GPUInteraction", "GPUFloat3List", "GPURayList",
     "GPUBoundingSphereList", "GPUInteractionList", "Uint32List", "TensorInteractions", "FcpwError",
-    "library_path", "GPUSceneBatch2D", "GPUSceneBatch3D",
+    "library_path", "GPUSceneBatch2D", "GPUSceneBatch3D", "scene_file_info",
 ]

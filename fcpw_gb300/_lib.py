@@ -53,6 +53,9 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_get_traversal": (c_int, [P, P]),
     "fcpwgb_gpu_scene_check_errors": (c_int, [P, C.POINTER(c_uint32)]),
     "fcpwgb_closest_distances_f64_device": (c_int, [P, P, c_uint32, P, P]),
+    "fcpwgb_cpu_bvh_save": (c_int, [P, C.c_char_p, P, c_uint32]),
+    "fcpwgb_gpu_scene_load": (c_int, [P, C.c_char_p]),
+    "fcpwgb_scene_file_info": (c_int, [C.c_char_p, P, C.POINTER(c_uint32)]),
     "fcpwgb_contains": (c_int, [P, P, c_uint32, P]),
     "fcpwgb_contains_device": (c_int, [P, P, c_uint32, P, P]),
     "fcpwgb_has_line_of_sight": (c_int, [P, P, P, c_uint32, P]),

@@ -38,8 +38,14 @@ int GpuScene::ensureWide(cudaStream_t st) {
     const WideConfig &c = wideConfig;
     if (wide.valid && wide.branching == c.branching && wide.bits == c.bits && wide.leafSize == c.leafSize) return 0;
     WideHost h;
-    if (!buildWideTree(c.branching, c.bits, hostNP, hostOff, hostBoxes, h, c.leafSize))
+    const WideHost *pre = nullptr;
+    for (const auto &p : preloadedWide)
+        if (p.second.W == c.branching && p.second.bits == c.bits && p.first == c.leafSize) pre = &p.second;
+    if (pre) {
+        h = *pre;  // read from a scene file: no collapse
+    } else if (!buildWideTree(c.branching, c.bits, hostNP, hostOff, hostBoxes, h, c.leafSize)) {
         return setError(FCPWGB_ERR_UNSUPPORTED, "this tree cannot be collapsed into the requested wide layout");
+    }
     int rc;
     if ((rc = wideNodes.upload(h.nodes.data(), h.nodes.size(), st))) return rc;
     if ((rc = wideChildBinary.upload(h.childBinary.data(), h.childBinary.size() * sizeof(int32_t), st))) return rc;

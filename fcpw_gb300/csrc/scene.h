@@ -97,9 +97,12 @@ struct GpuScene {
     int activate() const;
     SceneView view() const;
     cudaStream_t pick(void *s) const;
+    // wide trees read from a scene file: (leaf size, tree), used instead of the host collapse
+    std::vector<std::pair<int, WideHost>> preloadedWide;
     void resetTree() {
         transferred = false;
         wide.clear();
+        preloadedWide.clear();
     }
 
     // query dispatch (variant chosen by wideConfig)

@@ -236,6 +236,17 @@ class _GPUScene:
         self._n_nodes = bvh.info.n_nodes
         self._snch = bvh.snch
 
+    def load(self, path) -> None:
+        """Uploads a scene file written by CpuBvh.save (fcpwgb_gpu_scene_load): no CPU
+        build, and no wide collapse for the layouts the file holds."""
+        check(lib().fcpwgb_gpu_scene_load(self._h, str(path).encode()))
+        from .scene import scene_file_info
+        info = scene_file_info(path)
+        self._cpu_bvh = None
+        self._n_vertices = info["n_vertices"]
+        self._n_nodes = info["n_nodes"]
+        self._snch = info["bvh_type"] in (R.LINE_SEGMENT_SNCH, R.TRIANGLE_SNCH)
+
     def transfer_arrays(self, bvh_type: int, nodes, primitives, silhouettes=None, prim_vertices=None,
                         n_vertices: int = 0) -> None:
         """Uploads an already flattened tree in the interop layouts."""

@@ -100,6 +100,18 @@ class CpuBvh:
                                                C.byref(nb)))
         return nodes, cb
 
+    def save(self, path, wide=()) -> None:
+        """Writes a scene file (fcpwgb_cpu_bvh_save): the tree, primitives,
+        silhouettes, topology and the wide trees of the given
+        (branching, bits, leaf_size) layouts."""
+        from ._lib import TraversalConfig
+        cfgs = (TraversalConfig * max(len(wide), 1))()
+        for k, w in enumerate(wide):
+            b, q = int(w[0]), int(w[1])
+            leaf = int(w[2]) if len(w) > 2 else 0
+            cfgs[k] = TraversalConfig(b, q, 128, 1, 0, 1, 0, leaf, 16)
+        check(lib().fcpwgb_cpu_bvh_save(self._h, str(path).encode(), cfgs, len(wide)))
+
     def update_positions(self, positions: np.ndarray) -> None:
         positions = np.ascontiguousarray(positions, np.float32)
         if positions.shape != (self.info.n_vertices, self.dim):
@@ -188,3 +200,12 @@ class Scene3D(_Scene):
 
     def set_object_triangles(self, indices, object_index: int) -> None:
         self._set_indices(indices, object_index)
+
+
+def scene_file_info(path) -> dict:
+    """Header of a scene file (checksum verified)."""
+    from ._lib import BvhInfo
+    info, nw = BvhInfo(), C.c_uint32(0)
+    check(lib().fcpwgb_scene_file_info(str(path).encode(), C.byref(info), C.byref(nw)))
+    return {"dim": info.dim, "bvh_type": info.bvh_type, "n_nodes": info.n_nodes, "n_primitives": info.n_primitives,
+            "n_silhouettes": info.n_silhouettes, "n_vertices": info.n_vertices, "n_wide": int(nw.value)}

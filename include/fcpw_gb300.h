@@ -320,6 +320,20 @@ int fcpwgb_gpu_scene_check_errors(fcpwgb_gpu_scene *scene, uint32_t *error_word)
 int fcpwgb_closest_distances_f64_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                         uint32_t n, double *distances, void *stream);
 
+/* ----------------------------------------------------- scene files ----- */
+/* No counterpart in the reference. A scene file holds a host-built tree in
+ * the interop layouts (nodes, primitives, silhouettes), its topology, and the
+ * wide trees of the n_wide given traversal configurations (branching, bits
+ * and leaf_size are used), with a checksum. fcpwgb_gpu_scene_load uploads it
+ * through the validating transfer and keeps the wide trees for the matching
+ * configurations, so neither the CPU build nor the wide collapse runs. */
+int fcpwgb_cpu_bvh_save(const fcpwgb_cpu_bvh *bvh, const char *path, const fcpwgb_traversal_config *wide,
+                        uint32_t n_wide);
+int fcpwgb_gpu_scene_load(fcpwgb_gpu_scene *scene, const char *path);
+/* Reads and checks a scene file's header and checksum: the counts in info
+ * (n_leaves and max_depth are 0), the number of wide trees in *n_wide. */
+int fcpwgb_scene_file_info(const char *path, fcpwgb_bvh_info *info, uint32_t *n_wide);
+
 /* ------------------------------------------- inside / line of sight ----- */
 /* Scene<DIM>::contains and hasLineOfSight (fcpw.inl:1443-1460, 1501-1520;
  * Aggregate::contains / hasLineOfSight, core/primitive.h:173-207), CPU-only in

@@ -212,3 +212,42 @@ def test_leaf_size_and_stack_placement_match_oracle(torus, leaf_size, short_stac
     compare_closest(3, prims, pts, got, ref, f"leaf {leaf_size} stack {short_stack} packet {packet}")
     assert g.check_errors() == 0
     g.set_traversal(0)
+
+
+@pytest.mark.parametrize("dim", [3, 2])
+def test_scene_file_load_matches_transfer(tmp_path, dim):
+    """A scene loaded from a file (no CPU build, preloaded wide trees) answers
+    exactly like the scene transferred from the host BVH, on the binary and the
+    wide paths, and refits from device vertices like it."""
+    import torch
+    if dim == 3:
+        v, f = W.torus(96, 48, W.SEED_BASE + 72)
+        lo, hi = -2.0, 2.0
+    else:
+        v, f = W.star_polylines(16, 64, W.SEED_BASE + 73)
+        lo, hi = -3.0, 3.0
+    s = build_scene(dim, v, f, silhouettes=True)
+    path = tmp_path / "scene.fcpwgb"
+    s.cpu_bvh.save(path, wide=[(4, 32), (4, 8, 8)])
+    a = F.GPUScene3D() if dim == 3 else F.GPUScene2D()
+    b = F.GPUScene3D() if dim == 3 else F.GPUScene2D()
+    a.transfer_to_gpu(s)
+    b.load(path)
+    pts = W.uniform_points(30000, dim, lo, hi, 74)
+    for cfg in [dict(branching=0), dict(branching=4, bits=32, packet=True), dict(branching=4, bits=8, leaf_size=8),
+                dict(branching=8, bits=16)]:
+        a.set_traversal(**cfg)
+        b.set_traversal(**cfg)
+        ra, rb = _run(a, pts), _run(b, pts)
+        assert ra.tobytes() == rb.tobytes(), cfg
+    assert np.array_equal(a.export_nodes().tobytes(), b.export_nodes().tobytes())
+    flip = np.zeros(len(pts), np.uint32)
+    sa, sb = F.GPUInteractionList(), F.GPUInteractionList()
+    a.find_closest_silhouette_points(pts, np.full(len(pts), R.FLT_MAX, np.float32), flip, sa)
+    b.find_closest_silhouette_points(pts, np.full(len(pts), R.FLT_MAX, np.float32), flip, sb)
+    assert sa.array().tobytes() == sb.array().tobytes()
+    moved = torch.from_numpy((v * 1.01).astype(np.float32)).cuda()
+    a.update_vertices_tensor(moved)
+    b.update_vertices_tensor(moved)
+    torch.cuda.synchronize()
+    assert np.array_equal(a.export_nodes().tobytes(), b.export_nodes().tobytes())
