@@ -32,6 +32,9 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_destroy": (None, [P]),
     "fcpwgb_gpu_scene_transfer": (c_int, [P, c_int, P, c_uint32, P, c_uint32, P, c_uint32, P, c_uint32]),
     "fcpwgb_gpu_scene_transfer_cpu_bvh": (c_int, [P, P]),
+    "fcpwgb_gpu_scene_build": (c_int, [P, P, c_uint32, P, c_uint32, c_uint32]),
+    "fcpwgb_gpu_scene_build_device": (c_int, [P, P, c_uint32, P, c_uint32, c_uint32, P]),
+    "fcpwgb_gpu_scene_info": (c_int, [P, P]),
     "fcpwgb_gpu_scene_refit": (c_int, [P, P, P]),
     "fcpwgb_gpu_scene_update_vertices_device": (c_int, [P, P, c_uint32, P]),
     "fcpwgb_gpu_scene_update_vertices_device_static": (c_int, [P, P, c_uint32, P]),

@@ -439,6 +439,80 @@ extern "C" int fcpwgb_gpu_scene_transfer_cpu_bvh(fcpwgb_gpu_scene *s, const fcpw
     return FCPWGB_OK;
 }
 
+// ------------------------------------------------------------------ GPU build
+// Builds the tree on the device (k_build.cu), reads the interop arrays back
+// and hands them to the validating transfer, so the scene is set up exactly
+// as for a host-built tree.
+static int gpuBuild(fcpwgb_gpu_scene *s, const float *positions, uint32_t nVertices, const int32_t *indices,
+                    uint32_t nPrims, uint32_t maxLeaf, cudaStream_t st) {
+    const int dim = s->dim;
+    if (!positions || !indices || nPrims == 0 || nVertices == 0)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "non-empty positions and indices are required");
+    if (maxLeaf == 0 || maxLeaf > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "max_leaf_size must be 1..15");
+    if (nPrims >= (1u << 27)) return setError(FCPWGB_ERR_UNSUPPORTED, "too many primitives for the GPU build");
+    const size_t recBytes = dim == 3 ? sizeof(fcpwgb_triangle) : sizeof(fcpwgb_line_segment);
+    DeviceBuffer scratch, nodes, prims, verts, counters;
+    int rc;
+    if ((rc = scratch.ensure(lbvhScratchWords(nPrims) * sizeof(uint32_t)))) return rc;
+    if ((rc = nodes.ensure((2 * (size_t)nPrims) * sizeof(fcpwgb_bvh_node)))) return rc;
+    if ((rc = prims.ensure((size_t)nPrims * recBytes))) return rc;
+    if ((rc = verts.ensure((size_t)nPrims * dim * sizeof(int32_t)))) return rc;
+    if ((rc = counters.ensure(16 * sizeof(uint32_t)))) return rc;
+    uint32_t *cnt = (uint32_t *)counters.ptr;
+    uint32_t host[16] = {0};
+    FCPWGB_CUDA(launchCheckIndices(indices, (size_t)nPrims * dim, nVertices, cnt + 8, s->smCount(), st));
+    FCPWGB_CUDA(cudaMemcpyAsync(host + 8, cnt + 8, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FCPWGB_CUDA(cudaStreamSynchronize(st));
+    if (host[8]) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "vertex index out of range");
+    FCPWGB_CUDA(cudaMemsetAsync(cnt + 9, 0, sizeof(uint32_t), st));
+    FCPWGB_CUDA(launchBuildLbvh(positions, indices, dim, nPrims, maxLeaf, (uint32_t *)scratch.ptr,
+                                (unsigned char *)nodes.ptr, (unsigned char *)prims.ptr, (int32_t *)verts.ptr, cnt,
+                                cnt + 9, s->smCount(), st));
+    FCPWGB_CUDA(cudaMemcpyAsync(host, cnt, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FCPWGB_CUDA(cudaStreamSynchronize(st));
+    if (host[9]) return setError(FCPWGB_ERR_TRAVERSAL, "GPU build: a bottom-up pass ran past its step bound");
+    const uint32_t nLeaves = host[0];
+    if (nLeaves == 0 || nLeaves > nPrims) return setError(FCPWGB_ERR_TRAVERSAL, "GPU build: bad leaf count");
+    const uint32_t nNodes = 2 * nLeaves - 1;
+    std::vector<unsigned char> hNodes((size_t)nNodes * sizeof(fcpwgb_bvh_node)), hPrims((size_t)nPrims * recBytes);
+    std::vector<int32_t> hVerts((size_t)nPrims * dim);
+    FCPWGB_CUDA(cudaMemcpyAsync(hNodes.data(), nodes.ptr, hNodes.size(), cudaMemcpyDeviceToHost, st));
+    FCPWGB_CUDA(cudaMemcpyAsync(hPrims.data(), prims.ptr, hPrims.size(), cudaMemcpyDeviceToHost, st));
+    FCPWGB_CUDA(cudaMemcpyAsync(hVerts.data(), verts.ptr, hVerts.size() * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                st));
+    FCPWGB_CUDA(cudaStreamSynchronize(st));
+    return fcpwgb_gpu_scene_transfer(s, dim == 3 ? FCPWGB_TRIANGLE_BVH : FCPWGB_LINE_SEGMENT_BVH, hNodes.data(),
+                                     nNodes, hPrims.data(), nPrims, nullptr, 0, hVerts.data(), nVertices);
+}
+
+extern "C" int fcpwgb_gpu_scene_build_device(fcpwgb_gpu_scene *s, const float *positions, uint32_t n_vertices,
+                                             const int32_t *indices, uint32_t n_primitives, uint32_t max_leaf_size,
+                                             void *stream) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    int rc = s->activate();
+    if (rc) return rc;
+    return gpuBuild(s, positions, n_vertices, indices, n_primitives, max_leaf_size, s->pick(stream));
+}
+
+extern "C" int fcpwgb_gpu_scene_build(fcpwgb_gpu_scene *s, const float *positions, uint32_t n_vertices,
+                                      const int32_t *indices, uint32_t n_primitives, uint32_t max_leaf_size) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    int rc = s->activate();
+    if (rc) return rc;
+    if (!positions || !indices || n_primitives == 0 || n_vertices == 0)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "non-empty positions and indices are required");
+    for (uint64_t k = 0; k < (uint64_t)n_primitives * s->dim; k++)
+        if (indices[k] < 0 || (uint32_t)indices[k] >= n_vertices)
+            return setError(FCPWGB_ERR_INVALID_ARGUMENT, "vertex index out of range");
+    DeviceBuffer pos, idx;
+    if ((rc = pos.upload(positions, (size_t)n_vertices * s->dim * sizeof(float), s->stream))) return rc;
+    if ((rc = idx.upload(indices, (size_t)n_primitives * s->dim * sizeof(int32_t), s->stream))) return rc;
+    rc = gpuBuild(s, (const float *)pos.ptr, n_vertices, (const int32_t *)idx.ptr, n_primitives, max_leaf_size,
+                  s->stream);
+    cudaStreamSynchronize(s->stream);
+    return rc;
+}
+
 static int requireTree(fcpwgb_gpu_scene *s) {
     if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
     if (!s->transferred) return setError(FCPWGB_ERR_NOT_TRANSFERRED, "transferToGPU has not been called");
@@ -793,6 +867,22 @@ extern "C" int fcpwgb_gpu_scene_kernel_time(fcpwgb_gpu_scene *s, double *total_m
     *launches = (uint32_t)s->timedEvents.size();
     s->freeEvents.insert(s->freeEvents.end(), s->timedEvents.begin(), s->timedEvents.end());
     s->timedEvents.clear();
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_info(fcpwgb_gpu_scene *s, fcpwgb_bvh_info *info) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (!info) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL info");
+    info->dim = s->dim;
+    info->bvh_type = s->dim == 3 ? (s->snch ? FCPWGB_TRIANGLE_SNCH : FCPWGB_TRIANGLE_BVH)
+                                 : (s->snch ? FCPWGB_LINE_SEGMENT_SNCH : FCPWGB_LINE_SEGMENT_BVH);
+    info->n_nodes = s->nNodes;
+    info->n_leaves = s->nLeaves;
+    info->max_depth = s->maxDepth;
+    info->n_primitives = s->nPrims;
+    info->n_silhouettes = s->nSils;
+    info->n_vertices = s->nVertices;
     return FCPWGB_OK;
 }
 

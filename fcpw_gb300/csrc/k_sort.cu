@@ -7,8 +7,11 @@
 // whatever the query distribution. Threads of a warp then traverse
 // neighbouring queries, which keeps their paths through the tree alike. The
 // order inside a cell is whatever the scatter's atomics give; results are
-// written back to each query's own slot, so the order never shows in the
-// output.
+// written back to each query's own slot, and the wide kernels break exact
+// distance ties by primitive index, so the order never shows in the output.
+//
+// The stable radix sort further down orders the Morton codes of the GPU BVH
+// build, where equal codes must keep primitive order.
 #include <algorithm>
 
 #include "kernels.h"
@@ -97,21 +100,36 @@ FCPWGB_D void copyRecord(const DevRay *q, uint32_t i, DevRay *dst, uint32_t j) {
     for (int k = 0; k < 5; k++) d[k] = ldg2(p + 8 * k);
 }
 
-// min/max of the finite record positions: a warp reduction, then one atomic
-// per warp and axis into qb (initialised to +3.4e38 / -3.4e38 by a byte memset)
-template<class Rec> __global__ void kQueryBounds(const Rec *__restrict__ q, uint32_t n, int *qb) {
-    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float3 s = recordPosition(q, i);
-        float v[3] = {s.x, s.y, s.z};
+// min/max of the finite record positions: four independent loads in flight
+// per thread, a warp and then a block reduction, one atomic per block and
+// axis into qb (initialised to +3.4e38 / -3.4e38 by a byte memset)
+FCPWGB_D void boundsAdd(float3 s, float (&lo)[3], float (&hi)[3]) {
+    float v[3] = {s.x, s.y, s.z};
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (isfinite(v[a])) {
-                lo[a] = fminf(lo[a], v[a]);
-                hi[a] = fmaxf(hi[a], v[a]);
-            }
+    for (int a = 0; a < 3; a++) {
+        if (isfinite(v[a])) {
+            lo[a] = fminf(lo[a], v[a]);
+            hi[a] = fmaxf(hi[a], v[a]);
         }
     }
+}
+
+constexpr uint32_t kBoundsBlock = 256;
+template<class Rec> __global__ void __launch_bounds__(kBoundsBlock) kQueryBounds(const Rec *__restrict__ q, uint32_t n,
+                                                                              int *qb) {
+    __shared__ float sLo[kBoundsBlock / 32][3], sHi[kBoundsBlock / 32][3];
+    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    const uint32_t stride = gridDim.x * kBoundsBlock;
+    uint32_t i = blockIdx.x * kBoundsBlock + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        float3 s0 = recordPosition(q, i), s1 = recordPosition(q, i + stride);
+        float3 s2 = recordPosition(q, i + 2 * stride), s3 = recordPosition(q, i + 3 * stride);
+        boundsAdd(s0, lo, hi);
+        boundsAdd(s1, lo, hi);
+        boundsAdd(s2, lo, hi);
+        boundsAdd(s3, lo, hi);
+    }
+    for (; i < n; i += stride) boundsAdd(recordPosition(q, i), lo, hi);
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         for (int o = 16; o > 0; o >>= 1) {
@@ -119,12 +137,22 @@ template<class Rec> __global__ void kQueryBounds(const Rec *__restrict__ q, uint
             hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
         }
     }
-    if ((threadIdx.x & 31u) == 0) {
-#pragma unroll
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (lane == 0)
         for (int a = 0; a < 3; a++) {
-            atomicMin(qb + a, orderedInt(lo[a]));
-            atomicMax(qb + 3 + a, orderedInt(hi[a]));
+            sLo[warp][a] = lo[a];
+            sHi[warp][a] = hi[a];
         }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        float l = sLo[0][a], h = sHi[0][a];
+        for (uint32_t w = 1; w < kBoundsBlock / 32; w++) {
+            l = fminf(l, sLo[w][a]);
+            h = fmaxf(h, sHi[w][a]);
+        }
+        atomicMin(qb + a, orderedInt(l));
+        atomicMax(qb + 3 + a, orderedInt(h));
     }
 }
 
@@ -160,7 +188,8 @@ cudaError_t sortRecords(const SortLimits &lim, const Rec *recs, uint32_t n, uint
     if (e == cudaSuccess) e = cudaMemsetAsync(qb + 3, 0x80, 3 * sizeof(int), s);
     if (e != cudaSuccess) return e;
     uint32_t blocks = (n + 255) / 256;
-    kQueryBounds<Rec><<<std::min<uint32_t>(blocks, (uint32_t)std::max(numSMs, 1) * 8u), 256, 0, s>>>(recs, n, qb);
+    kQueryBounds<Rec><<<std::min<uint32_t>(blocks, (uint32_t)std::max(numSMs, 1) * 8u), kBoundsBlock, 0, s>>>(recs, n,
+                                                                                                     qb);
     kCellHistogram<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells);
     if ((e = scanCounts(cells, kSortCells, cells + kSortCells + 8, s)) != cudaSuccess) return e;
     kScatterQueries<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, sorted, perm);
@@ -305,6 +334,172 @@ cudaError_t launchSortBatchQueries(int dim, const BatchSceneGrid *grids, const u
     kBatchHistogram<<<blocks, 256, 0, s>>>(dim, grids, offsets, nScenes, spheres, n, cells);
     if ((e = scanCounts(cells, nCells, tileSums, s)) != cudaSuccess) return e;
     kBatchScatter<<<blocks, 256, 0, s>>>(dim, grids, offsets, nScenes, spheres, n, cells, sorted, perm, roots);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- radix sort
+// Stable LSD radix sort of 32-bit keys carrying their input index. A pass
+// handles one digit of at most 9 bits over tiles of kRadixTileKeys
+// consecutive keys: a digit histogram per tile, stored digit-major so that
+// one exclusive scan gives every tile its first output slot per digit, then a
+// scatter that orders the tile by digit in shared memory and writes each
+// digit's run out contiguously. Inside a tile each warp owns a contiguous
+// quarter: per-warp digit counts, one exclusive scan over (digit, warp), then
+// every key's slot is its warp's running slot for the digit plus its rank
+// among the lanes of its round with the same digit (per-bit ballots). Equal
+// keys keep their input order, so the output is the same on every run.
+constexpr uint32_t kRadixTileKeys = 4096;
+constexpr uint32_t kRadixHistBlock = 256;
+constexpr uint32_t kRadixBlock = 128, kRadixWarps = kRadixBlock / 32, kRadixWarpKeys = kRadixTileKeys / kRadixWarps;
+constexpr int kRadixMaxDigitBits = 9;
+constexpr uint32_t kRadixMaxDigits = 1u << kRadixMaxDigitBits;
+
+// lanes of the warp holding the same digit as this lane (0 for an invalid
+// lane): one ballot per digit bit, the lanes agreeing on every bit
+FCPWGB_D uint32_t digitPeers(uint32_t digit, int bits, bool valid) {
+    uint32_t m = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+    for (int b = 0; b < kRadixMaxDigitBits; b++) {
+        if (b < bits) {
+            const bool set = (digit >> b) & 1u;
+            const uint32_t v = __ballot_sync(0xffffffffu, set);
+            m &= set ? v : ~v;
+        }
+    }
+    return valid ? m : 0u;
+}
+
+__global__ void __launch_bounds__(kRadixHistBlock) kRadixHistogram(const uint32_t *__restrict__ keys, uint32_t n,
+                                                                   int shift, int bits, uint32_t nTiles,
+                                                                   uint32_t *hist) {
+    const uint32_t mask = (1u << bits) - 1u;
+    __shared__ uint32_t h[kRadixMaxDigits];
+    for (uint32_t d = threadIdx.x; d <= mask; d += kRadixHistBlock) h[d] = 0;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, base = blockIdx.x * kRadixTileKeys;
+    for (uint32_t r = 0; r < kRadixTileKeys / kRadixHistBlock; r++) {
+        const uint32_t i = base + r * kRadixHistBlock + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t digit = valid ? (__ldg(keys + i) >> shift) & mask : 0u;
+        const uint32_t peers = digitPeers(digit, bits, valid);
+        if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[digit], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d <= mask; d += kRadixHistBlock) hist[(size_t)d * nTiles + blockIdx.x] = h[d];
+}
+
+// valsIn null: the value of key i is i
+__global__ void __launch_bounds__(kRadixBlock) kRadixScatter(const uint32_t *__restrict__ keysIn,
+                                                             const uint32_t *__restrict__ valsIn, uint32_t n,
+                                                             int shift, int bits, uint32_t nTiles,
+                                                             const uint32_t *__restrict__ offsets, uint32_t *keysOut,
+                                                             uint32_t *valsOut) {
+    constexpr uint32_t kRounds = kRadixWarpKeys / 32;
+    const uint32_t mask = (1u << bits) - 1u;
+    __shared__ uint32_t sKeys[kRadixTileKeys], sVals[kRadixTileKeys];
+    __shared__ uint32_t start[kRadixMaxDigits * kRadixWarps];  // (digit, warp): running slot in the tile
+    __shared__ uint32_t tileStart[kRadixMaxDigits], globalStart[kRadixMaxDigits];
+    __shared__ uint32_t warpSums[kRadixWarps];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, tile = blockIdx.x;
+    const uint32_t base = tile * kRadixTileKeys, nd = mask + 1u, nEntries = nd * kRadixWarps;
+    const uint32_t tileN = min(kRadixTileKeys, n - base);
+    for (uint32_t k = threadIdx.x; k < nEntries; k += kRadixBlock) start[k] = 0;
+    for (uint32_t d = threadIdx.x; d < nd; d += kRadixBlock) globalStart[d] = __ldg(offsets + (size_t)d * nTiles + tile);
+    __syncthreads();
+    // 1. digit counts of the warp's keys (read again in step 3, then from L1)
+    const uint32_t wBase = base + warp * kRadixWarpKeys;
+#pragma unroll 4
+    for (uint32_t r = 0; r < kRounds; r++) {
+        const uint32_t i = wBase + r * 32 + lane;
+        const bool valid = i < n;
+        const uint32_t digit = valid ? (__ldg(keysIn + i) >> shift) & mask : 0u;
+        const uint32_t peers = digitPeers(digit, bits, valid);
+        if (valid && (peers & ((1u << lane) - 1u)) == 0) start[digit * kRadixWarps + warp] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // 2. exclusive scan of start[] in (digit, warp) order
+    const uint32_t per = (nEntries + kRadixBlock - 1) / kRadixBlock, e0 = threadIdx.x * per;
+    uint32_t sum = 0;
+    for (uint32_t k = 0; k < per; k++)
+        if (e0 + k < nEntries) sum += start[e0 + k];
+    uint32_t incl = sum;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        uint32_t x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += x;
+    }
+    if (lane == 31) warpSums[warp] = incl;
+    __syncthreads();
+    uint32_t run = incl - sum;
+    for (uint32_t w = 0; w < warp; w++) run += warpSums[w];
+    for (uint32_t k = 0; k < per; k++) {
+        if (e0 + k < nEntries) {
+            uint32_t c = start[e0 + k];
+            start[e0 + k] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d < nd; d += kRadixBlock) tileStart[d] = start[d * kRadixWarps];
+    __syncthreads();
+    // 3. stage the tile in digit order
+#pragma unroll 4
+    for (uint32_t r = 0; r < kRounds; r++) {
+        const uint32_t i = wBase + r * 32 + lane;
+        const bool valid = i < n;
+        const uint32_t key = valid ? __ldg(keysIn + i) : 0u;
+        const uint32_t digit = valid ? (key >> shift) & mask : 0u;
+        const uint32_t peers = digitPeers(digit, bits, valid);
+        const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid) {
+            const uint32_t slot = start[digit * kRadixWarps + warp] + rank;
+            sKeys[slot] = key;
+            sVals[slot] = valsIn ? __ldg(valsIn + i) : i;
+        }
+        __syncwarp();
+        if (valid && rank == 0) start[digit * kRadixWarps + warp] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // 4. every digit's run of the tile goes out contiguously
+    for (uint32_t s = threadIdx.x; s < tileN; s += kRadixBlock) {
+        const uint32_t k = sKeys[s], d = (k >> shift) & mask;
+        const uint32_t pos = globalStart[d] + s - tileStart[d];
+        keysOut[pos] = k;
+        valsOut[pos] = sVals[s];
+    }
+}
+
+uint32_t radixTiles(uint32_t n) { return (n + kRadixTileKeys - 1) / kRadixTileKeys; }
+
+size_t radixScratchWords(uint32_t n) {
+    const uint32_t hist = kRadixMaxDigits * std::max(radixTiles(n), 1u);
+    return (size_t)hist + batchScanTiles(hist) + 4;
+}
+
+cudaError_t radixSortIndices(uint32_t *keys0, uint32_t *keys1, uint32_t n, int keyBits, uint32_t *valsOut,
+                             uint32_t *valsAlt, uint32_t *scratch, const uint32_t **sortedKeys, cudaStream_t s) {
+    if (sortedKeys) *sortedKeys = keys0;
+    if (n == 0) return cudaSuccess;
+    keyBits = std::min(std::max(keyBits, 1), 32);
+    const int passes = (keyBits + kRadixMaxDigitBits - 1) / kRadixMaxDigitBits;
+    const int digitBits = (keyBits + passes - 1) / passes;
+    const uint32_t mask = (1u << digitBits) - 1u, tiles = radixTiles(n), nHist = (mask + 1u) * tiles;
+    uint32_t *hist = scratch, *tileSums = scratch + (size_t)kRadixMaxDigits * tiles;
+    uint32_t *keys[2] = {keys0, keys1};
+    const uint32_t *vin = nullptr;
+    cudaError_t e;
+    for (int p = 0; p < passes; p++) {
+        const int shift = p * digitBits;
+        uint32_t *vout = (passes - 1 - p) % 2 == 0 ? valsOut : valsAlt;  // the last pass writes valsOut
+        kRadixHistogram<<<tiles, kRadixHistBlock, 0, s>>>(keys[p & 1], n, shift, digitBits, tiles, hist);
+        if ((e = scanCounts(hist, nHist, tileSums, s)) != cudaSuccess) return e;
+        kRadixScatter<<<tiles, kRadixBlock, 0, s>>>(keys[p & 1], vin, n, shift, digitBits, tiles, hist, keys[(p + 1) & 1],
+                                                     vout);
+        vin = vout;
+    }
+    if (sortedKeys) *sortedKeys = keys[passes & 1];
     return cudaGetLastError();
 }
 

@@ -270,18 +270,34 @@ template<> struct NearTie<true> {  // two registers; the band is recomputed from
         d2nd = d;
         sel2nd = sel;
     }
-    // a primitive that did not beat the winner (the caller's radius is checked at the end)
+    // a primitive that did not beat the winner (the caller's radius is checked
+    // at the end); ranked like the winner, by distance and then leaf position
     FCPWGB_D void offer(float d, uint32_t sel) {
-        if (d < d2nd) {
+        if (d < d2nd || (d == d2nd && sel < sel2nd)) {
             d2nd = d;
             sel2nd = sel;
         }
     }
 };
 
+// Whether a tested primitive (distance d, leaf position sel) becomes the
+// winner: before the first hit when d*d <= r2 (the caller's radius, or a
+// child's far distance); after it (r2 is then the winner's d*d) on a smaller
+// distance, or on an equal one with an earlier leaf position. Boxes hold
+// their primitives with a margin (vertices widened by FLT_EPSILON, outward
+// quantisation) and visits are inclusive (d2Min <= r2), so every primitive at
+// the winner's distance is visited and an exact tie resolves to the same
+// primitive in any visiting order: the result depends neither on the order
+// of the queries, nor on which queries share a warp, nor on the wide layout.
+// The runner-up of NearTie is ranked the same way.
+FCPWGB_D bool beatsWinner(bool found, float d, float r2, float bestD, uint32_t sel, uint32_t selected) {
+    return found ? (d < bestD || (d == bestD && sel < selected)) : d * d <= r2;
+}
+
 // Closest point of one query on a wide tree (bvh.slang:395-502 semantics:
 // inclusive d2Min <= r2 pruning, r2 shrunk by child d2Max, primitives accepted
-// when d*d <= r2, the later of equal distances wins).
+// when d*d <= r2; exact distance ties go to the earlier leaf position, see
+// beatsWinner).
 // `root` is the tree's root record (always an inner record); `found`/`best`/
 // `selected`/`r2` may arrive holding a candidate already tested (a seed).
 // Boxes are pruned against rp2: r2, or with TRACK r2 widened by the band.
@@ -352,7 +368,7 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
                 float3 pt;
                 float2 uv;
                 float d = prim.closestPoint(c, pt, uv);
-                if (d * d <= r2) {
+                if (beatsWinner(found, d, r2, best.d, off + p, selected)) {
                     if (found) tie.replaced(best.d, selected);
                     r2 = fminf(r2, d * d);
                     rp2 = tie.pruneHit(d, c);
@@ -635,7 +651,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                         float3 pt;
                         float2 uv;
                         float d = prim.closestPoint(c, pt, uv);
-                        if (d * d <= r2) {
+                        if (beatsWinner(found, d, r2, best.d, off + p, selected)) {
                             if (found) tie.replaced(best.d, selected);
                             r2 = fminf(r2, d * d);
                             rp2 = tie.pruneHit(d, c);

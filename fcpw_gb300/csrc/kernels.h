@@ -95,6 +95,15 @@ cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, u
 // the same for rays, by origin
 cudaError_t launchSortRays(const SortLimits &lim, const DevRay *rays, uint32_t n, uint32_t *cells, DevRay *sorted,
                            uint32_t *perm, int numSMs, cudaStream_t s);
+// exclusive scan of nCells counters in place; tileSums holds batchScanTiles(nCells) words
+cudaError_t scanCounts(uint32_t *cells, uint32_t nCells, uint32_t *tileSums, cudaStream_t s);
+// stable radix sort of n keys (low keyBits bits) carrying their input index:
+// the indices in sorted order end in valsOut (valsAlt: n more words), the
+// keys ping-pong between keys0 and keys1 (*sortedKeys: the sorted ones);
+// scratch holds radixScratchWords(n) words
+size_t radixScratchWords(uint32_t n);
+cudaError_t radixSortIndices(uint32_t *keys0, uint32_t *keys1, uint32_t n, int keyBits, uint32_t *valsOut,
+                             uint32_t *valsAlt, uint32_t *scratch, const uint32_t **sortedKeys, cudaStream_t s);
 cudaError_t launchPackTri48(const DevTriangle *tris, uint32_t n, float4 *out, cudaStream_t s);
 
 // batches of scenes: per-scene sort grid (cells cellBase .. cellBase + 2^(dim*bits))
@@ -110,6 +119,17 @@ cudaError_t launchSortBatchQueries(int dim, const BatchSceneGrid *grids, const u
                                    const DevSphere *spheres, uint32_t n, uint32_t *cells, uint32_t nCells,
                                    uint32_t *tileSums, DevSphere *sorted, uint32_t *perm, uint32_t *roots,
                                    cudaStream_t s);
+
+// GPU BVH construction (k_build.cu)
+size_t lbvhScratchWords(uint32_t n);
+cudaError_t launchCheckIndices(const int32_t *indices, size_t nIdx, uint32_t nVertices, uint32_t *bad, int numSMs,
+                               cudaStream_t s);
+// nodesOut: room for 2n - 1 interop nodes; primsOut: n interop primitives;
+// primVertsOut: n * dim vertex indices; counters: 8 words ([0] leaves, [1] depth)
+cudaError_t launchBuildLbvh(const float *positions, const int32_t *indices, int dim, uint32_t n, uint32_t maxLeaf,
+                            uint32_t *scratch, unsigned char *nodesOut, unsigned char *primsOut,
+                            int32_t *primVertsOut, uint32_t *counters, uint32_t *errorWord, int numSMs,
+                            cudaStream_t s);
 
 // backward of the differentiable queries (k_grad.cu)
 struct GradView {

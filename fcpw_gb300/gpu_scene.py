@@ -247,6 +247,48 @@ class _GPUScene:
         self._n_nodes = info["n_nodes"]
         self._snch = info["bvh_type"] in (R.LINE_SEGMENT_SNCH, R.TRIANGLE_SNCH)
 
+    def build_on_gpu(self, positions, indices, max_leaf_size: int = 4) -> None:
+        """Builds the tree on the device and sets the scene up from it
+        (fcpwgb_gpu_scene_build): positions (V, DIM) float32, indices (P, DIM)
+        int32, as numpy arrays or contiguous CUDA tensors (built on the current
+        torch stream). A linear BVH: distances agree with the host SAH build,
+        the primitive chosen on an exact tie may differ. No silhouettes."""
+        try:
+            import torch
+            on_device = isinstance(positions, torch.Tensor) and positions.is_cuda
+        except ImportError:  # pragma: no cover
+            on_device = False
+        if on_device:
+            if (positions.dtype != torch.float32 or indices.dtype != torch.int32 or not indices.is_cuda
+                    or not positions.is_contiguous() or not indices.is_contiguous()):
+                raise ValueError("positions (float32) and indices (int32) must be contiguous CUDA tensors")
+            if positions.dim() != 2 or positions.shape[1] != self.DIM or indices.dim() != 2 \
+                    or indices.shape[1] != self.DIM:
+                raise ValueError(f"positions and indices must have {self.DIM} columns")
+            stream = torch.cuda.current_stream(positions.device).cuda_stream
+            check(lib().fcpwgb_gpu_scene_build_device(self._h, positions.data_ptr(), positions.shape[0],
+                                                      indices.data_ptr(), indices.shape[0], int(max_leaf_size),
+                                                      C.c_void_p(stream)))
+            n_vertices = positions.shape[0]
+        else:
+            pos = np.ascontiguousarray(positions, np.float32)
+            idx = np.ascontiguousarray(indices, np.int32)
+            if pos.ndim != 2 or pos.shape[1] != self.DIM or idx.ndim != 2 or idx.shape[1] != self.DIM:
+                raise ValueError(f"positions and indices must have {self.DIM} columns")
+            check(lib().fcpwgb_gpu_scene_build(self._h, ptr(pos), len(pos), ptr(idx), len(idx), int(max_leaf_size)))
+            n_vertices = len(pos)
+        self._cpu_bvh = None
+        self._n_vertices = int(n_vertices)
+        self._n_nodes = self.info()["n_nodes"]
+        self._snch = False
+
+    def info(self) -> dict:
+        """Sizes of the scene's binary tree (fcpwgb_gpu_scene_info)."""
+        from ._lib import BvhInfo
+        info = BvhInfo()
+        check(lib().fcpwgb_gpu_scene_info(self._h, C.byref(info)))
+        return {f: getattr(info, f) for f, _ in BvhInfo._fields_}
+
     def transfer_arrays(self, bvh_type: int, nodes, primitives, silhouettes=None, prim_vertices=None,
                         n_vertices: int = 0) -> None:
         """Uploads an already flattened tree in the interop layouts."""

@@ -178,6 +178,24 @@ int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *scene, int bvh_type,
 /* convenience: transferToGPU straight from a host-built BVH */
 int fcpwgb_gpu_scene_transfer_cpu_bvh(fcpwgb_gpu_scene *scene, const fcpwgb_cpu_bvh *bvh);
 
+/* Scene::build(AggregateType::Bvh, ...) + transferToGPU (fcpw.h:95,
+ * fcpw_gpu.h:21) with the tree built on the device: a linear BVH over the
+ * Morton codes of the primitive centroids (30-bit in 3D, 32-bit in 2D),
+ * subtrees of at most max_leaf_size (1..15) primitives merged into leaves,
+ * boxes widened by FLT_EPSILON per vertex as the host build does. The tree
+ * differs from the host SAH build, so query results agree with it in
+ * distance but may pick another primitive on ties; the scene is set up
+ * through fcpwgb_gpu_scene_transfer (with prim_vertices, so device vertex
+ * updates work). BVH only, no silhouettes. positions: n_vertices * dim
+ * floats, indices: n_primitives * dim. The _device form takes device arrays
+ * and builds on stream (NULL: the scene's stream); both return when the scene
+ * is ready. */
+int fcpwgb_gpu_scene_build(fcpwgb_gpu_scene *scene, const float *positions, uint32_t n_vertices,
+                           const int32_t *indices, uint32_t n_primitives, uint32_t max_leaf_size);
+int fcpwgb_gpu_scene_build_device(fcpwgb_gpu_scene *scene, const float *positions, uint32_t n_vertices,
+                                  const int32_t *indices, uint32_t n_primitives, uint32_t max_leaf_size,
+                                  void *stream);
+
 /* refit, fcpw_gpu.h:27 / bvh_interop_structures.h:891-934. When primitives
  * (and, for SNCH, silhouettes) are non-NULL they replace the device copies
  * first (updateGeometry=true); with NULL the device geometry is refit as is
@@ -308,6 +326,10 @@ int fcpwgb_gpu_scene_kernel_time(fcpwgb_gpu_scene *scene, double *total_ms, uint
  * the interop layout it was transferred in (fcpwgb_bvh_node or
  * fcpwgb_snch_node records, n_nodes of them). Synchronous. */
 int fcpwgb_gpu_scene_export_nodes(fcpwgb_gpu_scene *scene, void *nodes);
+/* Sizes of the scene's binary tree: *info receives the fcpwgb_bvh_info fields
+ * (dim, bvh_type, n_nodes, n_leaves, max_depth, n_primitives, n_silhouettes,
+ * n_vertices), however the tree got there (transfer, file or GPU build). */
+int fcpwgb_gpu_scene_info(fcpwgb_gpu_scene *scene, fcpwgb_bvh_info *info);
 
 /* Reads and clears the device error word of the scene (stack overflow or
  * step budget exhausted in a traversal). Synchronises the scene stream. */

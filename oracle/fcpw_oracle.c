@@ -23,7 +23,8 @@
  *   - Aggregate::contains / hasLineOfSight, core/primitive.h:173-207, with the
  *     all-hits ray traversal bvh.inl:888-1029 and removeDuplicates,
  *     core/interaction.h:20-25,75-94
- * plus an FP64 brute force used as the accuracy yardstick.
+ * plus an FP64 brute force used as the accuracy yardstick, and a sequential
+ * model of the device linear-BVH build (which has no reference counterpart).
  *
  * Inputs are the flattened tree and records in the reference's GPU interop
  * layouts (include/fcpw/gpu/bvh_interop_structures.h:55-162,730-774).
@@ -1220,4 +1221,155 @@ int oracle_line_of_sight_bvh(int dim, int snch, const void *nodes, const void *p
     j.kind = 8; j.dim = dim; j.snch = snch; j.nodes = nodes; j.prims = prims; j.queries = points_a;
     j.aux = points_b; j.u32out = out;
     return run_threaded(j, n, nthreads);
+}
+
+/* ------------------------------------------------------------------------
+ * Sequential model of the device linear-BVH build (fcpwgb_gpu_scene_build).
+ * The reference has no such builder (it builds with binned SAH on the host,
+ * bvh.inl:40-234); this model states what the device build must produce so
+ * that its output can be checked byte for byte: FP32 centroids
+ * ((0 + v0 + v1 [+ v2]) * (1/dim)), Morton codes of 10 (3D) or 16 (2D) bits
+ * per axis within the centroid bounds, primitives ordered by (code, index),
+ * the binary radix tree over those keys defined top-down (a range splits
+ * where the highest bit of (code, index) that differs inside it changes),
+ * subtrees of at most max_leaf primitives as leaves, leaf boxes of the
+ * vertices widened by FLT_EPSILON (bounding_volumes.h:38-49), pre-order node
+ * records (inner: offset = 1 + nodes of the left subtree), primitives in leaf
+ * order with their original index. */
+typedef struct { uint64_t key; } okey;
+static int cmp_key(const void *a, const void *b) {
+    uint64_t x = ((const okey *)a)->key, y = ((const okey *)b)->key;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+static uint32_t spread_bits(uint32_t v, int dim) {
+    uint32_t r = 0;
+    for (int b = 0; b < (dim == 3 ? 10 : 16); b++)
+        if (v & (1u << b)) r |= 1u << (b * dim);
+    return r;
+}
+static int clz32(uint32_t v) {
+    int n = 0;
+    if (v == 0) return 32;
+    while (!(v & 0x80000000u)) { v <<= 1; n++; }
+    return n;
+}
+typedef struct {
+    int dim;
+    uint32_t n, max_leaf;
+    const float *pos;
+    const int32_t *idx;
+    const uint32_t *codes, *order;
+    onode *nodes;
+    uint32_t count;
+} olbvh;
+static int lb_delta(const olbvh *b, uint32_t i, uint32_t j) {
+    uint32_t a = b->codes[i], c = b->codes[j];
+    return a != c ? clz32(a ^ c) : 32 + clz32(i ^ j);
+}
+static of3 lb_vertex(const olbvh *b, int32_t v) {
+    const float *p = b->pos + (size_t)v * b->dim;
+    return v3(p[0], p[1], b->dim == 3 ? p[2] : 0.0f);
+}
+/* emits the subtree over sorted positions [lo, hi]; returns its node count */
+static uint32_t lb_emit(olbvh *b, uint32_t lo, uint32_t hi) {
+    uint32_t me = b->count++;
+    onode *nd = &b->nodes[me];
+    if (hi - lo + 1 <= b->max_leaf) {
+        float l[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, h[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (uint32_t k = lo; k <= hi; k++) {
+            uint32_t p = b->order[k];
+            for (int j = 0; j < b->dim; j++) {
+                of3 v = lb_vertex(b, b->idx[(size_t)p * b->dim + j]);
+                for (int a = 0; a < b->dim; a++) {
+                    float c = comp(v, a);
+                    l[a] = minf_(l[a], c - FLT_EPSILON);
+                    h[a] = maxf_(h[a], c + FLT_EPSILON);
+                }
+            }
+        }
+        if (b->dim == 2) l[2] = h[2] = 0.0f;
+        b->nodes[me].pMin = v3(l[0], l[1], l[2]);
+        b->nodes[me].pMax = v3(h[0], h[1], h[2]);
+        b->nodes[me].nPrims = hi - lo + 1;
+        b->nodes[me].offset = lo;
+        return 1;
+    }
+    int common = lb_delta(b, lo, hi);
+    uint32_t s = lo, e = hi; /* last position whose key shares more than `common` bits with lo */
+    while (e - s > 1) {
+        uint32_t m = s + (e - s) / 2;
+        if (lb_delta(b, lo, m) > common) s = m;
+        else e = m;
+    }
+    uint32_t nl = lb_emit(b, lo, s);
+    uint32_t left = me + 1, right = b->count;
+    uint32_t nr = lb_emit(b, s + 1, hi);
+    nd = &b->nodes[me];
+    const onode *L = &b->nodes[left], *R = &b->nodes[right];
+    nd->pMin = v3(minf_(L->pMin.x, R->pMin.x), minf_(L->pMin.y, R->pMin.y), minf_(L->pMin.z, R->pMin.z));
+    nd->pMax = v3(maxf_(L->pMax.x, R->pMax.x), maxf_(L->pMax.y, R->pMax.y), maxf_(L->pMax.z, R->pMax.z));
+    nd->nPrims = 0;
+    nd->offset = 1 + nl;
+    return 1 + nl + nr;
+}
+/* nodes_out: room for 2n - 1 records; prims_out: n triangles (3D) or segments
+ * (2D); prim_verts_out: n * dim. Returns the node count (0 on bad input). */
+uint32_t oracle_lbvh_build(int dim, const float *pos, const int32_t *idx, uint32_t n, uint32_t max_leaf,
+                           void *nodes_out, void *prims_out, int32_t *prim_verts_out) {
+    if (n == 0 || max_leaf == 0) return 0;
+    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    of3 *cent = (of3 *)malloc(sizeof(of3) * n);
+    uint32_t *codes = (uint32_t *)malloc(sizeof(uint32_t) * n), *order = (uint32_t *)malloc(sizeof(uint32_t) * n);
+    uint32_t *sorted = (uint32_t *)malloc(sizeof(uint32_t) * n);
+    okey *keys = (okey *)malloc(sizeof(okey) * n);
+    olbvh b;
+    for (uint32_t p = 0; p < n; p++) {
+        of3 c = v3(0.0f, 0.0f, 0.0f);
+        for (int j = 0; j < dim; j++) {
+            const float *v = pos + (size_t)idx[(size_t)p * dim + j] * dim;
+            c = add3(c, v3(v[0], v[1], dim == 3 ? v[2] : 0.0f));
+        }
+        c = mul3(c, 1.0f / (float)dim);
+        cent[p] = c;
+        for (int a = 0; a < 3; a++) {
+            lo[a] = fminf(lo[a], comp(c, a));
+            hi[a] = fmaxf(hi[a], comp(c, a));
+        }
+    }
+    const float cells = dim == 3 ? 1024.0f : 65536.0f;
+    for (uint32_t p = 0; p < n; p++) {
+        uint32_t q[3];
+        for (int a = 0; a < 3; a++) {
+            float t = (comp(cent[p], a) - lo[a]) / fmaxf(hi[a] - lo[a], 1e-30f) * cells;
+            q[a] = (uint32_t)fminf(fmaxf(t, 0.0f), cells - 1.0f);
+        }
+        codes[p] = dim == 3 ? (spread_bits(q[0], 3) | (spread_bits(q[1], 3) << 1) | (spread_bits(q[2], 3) << 2))
+                            : (spread_bits(q[0], 2) | (spread_bits(q[1], 2) << 1));
+        keys[p].key = ((uint64_t)codes[p] << 32) | p;
+    }
+    qsort(keys, n, sizeof(okey), cmp_key);
+    for (uint32_t k = 0; k < n; k++) {
+        order[k] = (uint32_t)(keys[k].key & 0xffffffffu);
+        sorted[k] = (uint32_t)(keys[k].key >> 32);
+    }
+    b.dim = dim; b.n = n; b.max_leaf = max_leaf; b.pos = pos; b.idx = idx; b.codes = sorted; b.order = order;
+    b.nodes = (onode *)nodes_out; b.count = 0;
+    lb_emit(&b, 0, n - 1);
+    for (uint32_t k = 0; k < n; k++) {
+        uint32_t p = order[k];
+        of3 v[3];
+        for (int j = 0; j < dim; j++) {
+            prim_verts_out[(size_t)k * dim + j] = idx[(size_t)p * dim + j];
+            v[j] = lb_vertex(&b, idx[(size_t)p * dim + j]);
+        }
+        if (dim == 3) {
+            otri *t = (otri *)prims_out + k;
+            t->pa = v[0]; t->pb = v[1]; t->pc = v[2]; t->index = p;
+        } else {
+            oseg *s = (oseg *)prims_out + k;
+            s->pa = v[0]; s->pb = v[1]; s->index = p;
+        }
+    }
+    free(cent); free(codes); free(order); free(sorted); free(keys);
+    return b.count;
 }

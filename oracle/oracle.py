@@ -37,6 +37,8 @@ def _load():
             "oracle_line_of_sight_bvh": [i, i, P, P, P, P, u, P, i],
             "oracle_record_sizes": [P],
         }
+        _lib.oracle_lbvh_build.restype = C.c_uint32
+        _lib.oracle_lbvh_build.argtypes = [i, P, P, u, u, P, P, P]
         for name, args in sig.items():
             fn = getattr(_lib, name)
             fn.restype = C.c_int
@@ -166,6 +168,20 @@ def prim_distance_f64(dim, prims, positions_in_array, points):
     out = np.zeros(len(pos), np.float64)
     _load().oracle_prim_distance_f64(dim, _p(prims), len(prims), _p(pos), _p(x), len(pos), _p(out))
     return out
+
+
+def lbvh_build(dim, positions, indices, max_leaf=4):
+    """Sequential model of the device linear-BVH build: (nodes, primitives,
+    prim_vertices) exactly as fcpwgb_gpu_scene_build must produce them."""
+    R = _records()
+    pos = np.ascontiguousarray(positions, np.float32)
+    idx = np.ascontiguousarray(indices, np.int32)
+    n = len(idx)
+    nodes = np.zeros(max(2 * n - 1, 1), R.BVH_NODE)
+    prims = np.zeros(n, R.TRIANGLE if dim == 3 else R.LINE_SEGMENT)
+    pv = np.zeros((n, dim), np.int32)
+    cnt = _load().oracle_lbvh_build(dim, _p(pos), _p(idx), n, int(max_leaf), _p(nodes), _p(prims), _p(pv))
+    return nodes[:cnt], prims, pv
 
 
 def record_sizes():

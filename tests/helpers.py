@@ -63,6 +63,22 @@ def compare_closest(dim, prims, points, got, ref, what="closest point"):
             "max_abs_dd": float(dd.max()) if len(dd) else 0.0}
 
 
+def compare_rays(got, ref_out, ref_hit, occl=False):
+    """Ray parity: hit flags (grazing rays through shared edges or vertices
+    may flip between two FP32 implementations: at most 1e-4 of the rays),
+    hit distances within 1e-5 relative (absolute below 1), indices equal for
+    99.9% of the common hits."""
+    g_hit = got["index"] != R.UINT_MAX
+    mism = g_hit != ref_hit
+    assert mism.sum() <= max(2, int(1e-4 * len(got))), f"{mism.sum()} hit/miss disagreements"
+    both = g_hit & ref_hit
+    if not occl:
+        tol = 1e-5 * np.maximum(ref_out["d"][both], 1.0)
+        assert np.all(np.abs(got["d"][both] - ref_out["d"][both]) <= tol)
+        same = got["index"][both] == ref_out["index"][both]
+        assert same.mean() > 0.999
+
+
 def relative_error(d, d64):
     d64 = np.asarray(d64, np.float64)
     m = np.isfinite(d64) & (d64 > 0)

@@ -214,6 +214,39 @@ def test_leaf_size_and_stack_placement_match_oracle(torus, leaf_size, short_stac
     g.set_traversal(0)
 
 
+def test_warp_cooperative_results_repeat_exactly(torus):
+    """Exact distance ties go to the earlier leaf position, so the packet
+    kernel's answer does not depend on which queries share a warp, although
+    the order inside a sort cell changes from run to run."""
+    s, g, pts, ref, prims = torus
+    g.set_traversal(4, 32, sort_queries=True, precise=True, packet=True)
+    clustered = np.repeat(pts[:4000], 30, axis=0)  # many queries per sort cell
+    first = _run(g, clustered).tobytes()
+    for _ in range(3):
+        assert _run(g, clustered).tobytes() == first
+    g.set_traversal(0)
+
+
+@pytest.mark.parametrize("precise", [False, True])
+def test_every_wide_layout_and_schedule_agrees_exactly(torus, precise):
+    """The winner (and in precise mode the runner-up) is the first primitive
+    in leaf order among those at the smallest distance, which every layout
+    and schedule visits: results are byte-identical across all of them."""
+    s, g, pts, ref, prims = torus
+    sub = pts[:40000]
+    outs = {}
+    for cfg in [dict(branching=4, bits=32, packet=True), dict(branching=4, bits=32, persistent=False),
+                dict(branching=4, bits=32, persistent=True), dict(branching=2, bits=16),
+                dict(branching=8, bits=8), dict(branching=4, bits=8, leaf_size=8, short_stack=0),
+                dict(branching=8, bits=32, packet=True), dict(branching=4, bits=16, sort_queries=False)]:
+        g.set_traversal(precise=precise, **cfg)
+        outs[str(cfg)] = _run(g, sub).tobytes()
+    g.set_traversal(0)
+    first = next(iter(outs.values()))
+    differ = [k for k, v in outs.items() if v != first]
+    assert not differ, f"configurations that differ from the first: {differ}"
+
+
 @pytest.mark.parametrize("dim", [3, 2])
 def test_scene_file_load_matches_transfer(tmp_path, dim):
     """A scene loaded from a file (no CPU build, preloaded wide trees) answers
