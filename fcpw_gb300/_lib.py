@@ -33,6 +33,14 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_transfer": (c_int, [P, c_int, P, c_uint32, P, c_uint32, P, c_uint32, P, c_uint32]),
     "fcpwgb_gpu_scene_transfer_cpu_bvh": (c_int, [P, P]),
     "fcpwgb_gpu_scene_build": (c_int, [P, P, c_uint32, P, c_uint32, c_uint32]),
+    "fcpwgb_cpu_instances_build": (c_int, [c_int, c_int, P, c_uint32, P, P, P, c_uint32, P]),
+    "fcpwgb_cpu_instances_destroy": (None, [P]),
+    "fcpwgb_cpu_instances_export": (c_int, [P, P, P, P, P]),
+    "fcpwgb_gpu_scene_transfer_instanced": (c_int, [P, P]),
+    "fcpwgb_find_closest_points_instanced": (c_int, [P, P, P, P, c_uint32, c_int]),
+    "fcpwgb_find_closest_points_instanced_device": (c_int, [P, P, P, P, c_uint32, c_int, P]),
+    "fcpwgb_intersect_rays_instanced": (c_int, [P, P, P, P, c_uint32, c_int]),
+    "fcpwgb_intersect_rays_instanced_device": (c_int, [P, P, P, P, c_uint32, c_int, P]),
     "fcpwgb_gpu_scene_build_device": (c_int, [P, P, c_uint32, P, c_uint32, c_uint32, P]),
     "fcpwgb_gpu_scene_info": (c_int, [P, P]),
     "fcpwgb_gpu_scene_refit": (c_int, [P, P, P]),

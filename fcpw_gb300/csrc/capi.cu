@@ -515,6 +515,9 @@ extern "C" int fcpwgb_gpu_scene_build(fcpwgb_gpu_scene *s, const float *position
 
 static int requireTree(fcpwgb_gpu_scene *s) {
     if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    if (s->inst)
+        return setError(FCPWGB_ERR_UNSUPPORTED,
+                        "a scene of several objects or instances takes closest point and ray queries only");
     if (!s->transferred) return setError(FCPWGB_ERR_NOT_TRANSFERRED, "transferToGPU has not been called");
     return s->activate();
 }
@@ -601,6 +604,13 @@ extern "C" int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *s, cons
 extern "C" int fcpwgb_find_closest_points_device(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
                                                  fcpwgb_interaction *out, uint32_t n, int record_normals,
                                                  void *stream) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc) return rc;
+        if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedClosest(s, (const DevSphere *)spheres, (DevInteraction *)out, nullptr, n, record_normals,
+                                s->pick(stream));
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
@@ -609,6 +619,12 @@ extern "C" int fcpwgb_find_closest_points_device(fcpwgb_gpu_scene *s, const fcpw
 
 extern "C" int fcpwgb_intersect_rays_device(fcpwgb_gpu_scene *s, const fcpwgb_ray *rays, fcpwgb_interaction *out,
                                             uint32_t n, int occl, void *stream) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc) return rc;
+        if (n > 0 && (!rays || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedRays(s, (const DevRay *)rays, (DevInteraction *)out, nullptr, n, occl, s->pick(stream));
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n > 0 && (!rays || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
@@ -689,6 +705,12 @@ struct HostQuery {
 
 extern "C" int fcpwgb_find_closest_points(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
                                           fcpwgb_interaction *out, uint32_t n, int record_normals) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc || n == 0) return rc;
+        if (!spheres || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedHost(s, spheres, (size_t)n * sizeof(DevSphere), out, nullptr, n, false, record_normals);
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n == 0) return FCPWGB_OK;
@@ -698,6 +720,12 @@ extern "C" int fcpwgb_find_closest_points(fcpwgb_gpu_scene *s, const fcpwgb_boun
 
 extern "C" int fcpwgb_intersect_rays(fcpwgb_gpu_scene *s, const fcpwgb_ray *rays, fcpwgb_interaction *out,
                                      uint32_t n, int occl) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc || n == 0) return rc;
+        if (!rays || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedHost(s, rays, (size_t)n * sizeof(DevRay), out, nullptr, n, true, occl);
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n == 0) return FCPWGB_OK;

@@ -231,6 +231,60 @@ template<int D> void HostBvh::buildAll() {
     if (withSilhouettes_) assignSilhouettesAfterBuild();
 }
 
+std::unique_ptr<HostBvh> HostBvh::fromBoxes(int dim, const float *boxes, const float *centroids, uint32_t n,
+                                            Heuristic heuristic, int leafSize, int nBuckets) {
+    if (dim != 2 && dim != 3) throw std::runtime_error("dim must be 2 or 3");
+    if (n == 0) throw std::runtime_error("cannot construct a BVH without references");
+    if (leafSize < 1 || nBuckets < 2) throw std::runtime_error("invalid leaf size or bucket count");
+    std::unique_ptr<HostBvh> b(new HostBvh(dim, heuristic, leafSize, nBuckets));
+    if (dim == 3) b->buildFromBoxes<3>(boxes, centroids, n);
+    else b->buildFromBoxes<2>(boxes, centroids, n);
+    return b;
+}
+
+template<int D> void HostBvh::buildFromBoxes(const float *boxes, const float *centroids, uint32_t n) {
+    primOrder_.resize(n);
+    for (uint32_t i = 0; i < n; i++) primOrder_[i] = (int)i;
+    std::vector<Box<D>> refBoxes(n);
+    std::vector<Vec<D>> refCentroids(n);
+    for (uint32_t i = 0; i < n; i++) {
+        for (int a = 0; a < D; a++) {
+            refBoxes[i].pMin.c[a] = boxes[(size_t)i * 6 + a];
+            refBoxes[i].pMax.c[a] = boxes[(size_t)i * 6 + 3 + a];
+            refCentroids[i].c[a] = centroids[(size_t)i * 3 + a];
+        }
+    }
+    nodes_.reserve((size_t)n * 2);
+    buildRecursive<D>(refBoxes, refCentroids, -1, 0, (int)n, 0);
+}
+
+void HostBvh::rootBox(float pMin[3], float pMax[3]) const {
+    for (int a = 0; a < 3; a++) {
+        pMin[a] = nodes_.empty() ? FLT_MAX : nodes_[0].pMin[a];
+        pMax[a] = nodes_.empty() ? -FLT_MAX : nodes_[0].pMax[a];
+    }
+}
+
+void HostBvh::primitiveCentroidMean(float c[3]) const {
+    const int D = dim_;
+    float sum[3] = {0.0f, 0.0f, 0.0f};
+    const size_t n = primOrder_.size();
+    for (size_t k = 0; k < n; k++) {
+        const int *v = &primVerts_[(size_t)primOrder_[k] * D];
+        for (int a = 0; a < D; a++) {
+            float x;
+            if (D == 3) {  // Triangle::centroid, (pa + pb + pc) / 3
+                x = ((positions_[(size_t)v[0] * D + a] + positions_[(size_t)v[1] * D + a]) +
+                     positions_[(size_t)v[2] * D + a]) / 3.0f;
+            } else {       // LineSegment::centroid, (pa + pb) * 0.5
+                x = (positions_[(size_t)v[0] * D + a] + positions_[(size_t)v[1] * D + a]) * 0.5f;
+            }
+            sum[a] += x;
+        }
+    }
+    for (int a = 0; a < 3; a++) c[a] = a < D && n > 0 ? sum[a] / (float)n : 0.0f;
+}
+
 // Renumbers vertices in leaf order, fcpw.inl:613-689.
 void HostBvh::sortSoupPositions() {
     int V = (int)(positions_.size() / dim_);

@@ -67,7 +67,22 @@ public:
     // updateObjectVertices: positions in caller vertex order
     void updatePositions(const float *positions);
 
+    // A tree over given reference boxes (n x [pMin xyz, pMax xyz]) and
+    // centroids (n x xyz): the reference's Bvh over aggregate instances
+    // (fcpw.inl:1093-1101, bvh.inl:213-234). It holds no primitives;
+    // primOrder() maps leaf order to the input reference index.
+    static std::unique_ptr<HostBvh> fromBoxes(int dim, const float *boxes, const float *centroids, uint32_t n,
+                                              Heuristic heuristic, int leafSize = 4, int nBuckets = 8);
+    const std::vector<int> &primOrder() const { return primOrder_; }
+    // Bvh::boundingBox (bvh.inl:615-618) and Bvh::centroid, the mean of the
+    // primitive centroids in leaf order (bvh.inl:621-631)
+    void rootBox(float pMin[3], float pMax[3]) const;
+    void primitiveCentroidMean(float c[3]) const;
+
 private:
+    HostBvh(int dim, Heuristic heuristic, int leafSize, int nBuckets)
+        : dim_(dim), heuristic_(heuristic), withSilhouettes_(false), leafSize_(leafSize), nBuckets_(nBuckets) {}
+    template<int D> void buildFromBoxes(const float *boxes, const float *centroids, uint32_t n);
     template<int D> void buildAll();
     template<int D> void buildRecursive(std::vector<Box<D>> &refBoxes, std::vector<Vec<D>> &refCentroids,
                                         int parent, int start, int end, int depth);

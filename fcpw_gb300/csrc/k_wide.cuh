@@ -710,32 +710,17 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
 // first; a stacked child is skipped when its entry distance exceeds tMax;
 // hits are accepted when 0 <= t <= tMax (a later equal t wins), and an
 // occlusion query stops at its first hit.
-template<int W, int BITS, class Prim>
-__global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *__restrict__ nodes,
-                                                       const unsigned char *__restrict__ prims,
-                                                       const DevRay *__restrict__ rays,
-                                                       const uint32_t *__restrict__ perm,
-                                                       DevInteraction *__restrict__ out, uint32_t n, int occl,
-                                                       uint32_t *errorWord, unsigned long long *stats) {
+// Ray traversal of one wide tree from record `root` (the loop of kWideRay);
+// r.tMax shrinks to the nearest hit, `best` receives it. Returns whether the
+// ray hit (with occl: whether it is occluded; only best.index is set then).
+template<int W, int BITS, class Prim, int SHORT>
+FCPWGB_D bool wideRay(const unsigned char *__restrict__ nodes, const unsigned char *__restrict__ prims,
+                      uint32_t root, DevRay &r, int occl, DevInteraction &best, WideStack<SHORT> &st,
+                      uint32_t *errorWord, uint32_t &tExp, uint32_t &tTests) {
     constexpr uint32_t kSlotMask = W - 1;
-    __shared__ uint32_t sRef[kShortStack * kWideBlock];
-    __shared__ float sD[kShortStack * kWideBlock];
-    WideStack<kShortStack> st;
-    st.sRef = sRef + threadIdx.x;
-    st.sD = sD + threadIdx.x;
-    const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
-    if (i >= n) return;
-    const unsigned char *rp = reinterpret_cast<const unsigned char *>(rays + i);
-    float2 a = ldg2(rp), b = ldg2(rp + 8), cc = ldg2(rp + 16), d = ldg2(rp + 24), e = ldg2(rp + 32);
-    DevRay r;
-    r.o = make_float3(a.x, a.y, b.x);
-    r.d = make_float3(b.y, cc.x, cc.y);
-    r.dInv = make_float3(d.x, d.y, e.x);
-    r.tMax = e.y;
-    DevInteraction best = defaultInteraction();
-    uint32_t tExp = 0, tTests = 0;
+    bool anyHit = false;
     WideNodeRegs<W, BITS> node;
-    uint32_t cur = 0;
+    uint32_t cur = root;
     int sp = 0;
     bool done = false;
     while (!done) {
@@ -781,6 +766,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
                 DevInteraction c = defaultInteraction();
                 if (prim.intersect(r, occl != 0, c)) {
                     c.index = prim.index;
+                    anyHit = true;
                     if (occl) {
                         best.index = c.index;
                         done = true;
@@ -803,6 +789,33 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
         }
         if (!next) break;
     }
+    return anyHit;
+}
+
+template<int W, int BITS, class Prim>
+__global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *__restrict__ nodes,
+                                                       const unsigned char *__restrict__ prims,
+                                                       const DevRay *__restrict__ rays,
+                                                       const uint32_t *__restrict__ perm,
+                                                       DevInteraction *__restrict__ out, uint32_t n, int occl,
+                                                       uint32_t *errorWord, unsigned long long *stats) {
+    __shared__ uint32_t sRef[kShortStack * kWideBlock];
+    __shared__ float sD[kShortStack * kWideBlock];
+    WideStack<kShortStack> st;
+    st.sRef = sRef + threadIdx.x;
+    st.sD = sD + threadIdx.x;
+    const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
+    if (i >= n) return;
+    const unsigned char *rp = reinterpret_cast<const unsigned char *>(rays + i);
+    float2 a = ldg2(rp), b = ldg2(rp + 8), cc = ldg2(rp + 16), d = ldg2(rp + 24), e = ldg2(rp + 32);
+    DevRay r;
+    r.o = make_float3(a.x, a.y, b.x);
+    r.d = make_float3(b.y, cc.x, cc.y);
+    r.dInv = make_float3(d.x, d.y, e.x);
+    r.tMax = e.y;
+    DevInteraction best = defaultInteraction();
+    uint32_t tExp = 0, tTests = 0;
+    wideRay<W, BITS, Prim, kShortStack>(nodes, prims, 0u, r, occl, best, st, errorWord, tExp, tTests);
     out[perm ? __ldg(perm + i) : i] = best;
     if (stats) {
         atomicAdd(stats + 1, (unsigned long long)tExp);

@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <string>
 #include <utility>
+#include <memory>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -50,6 +51,8 @@ struct DeviceBuffer {
         return e == cudaSuccess ? 0 : cudaFail(e, "cudaMemcpyAsync");
     }
 };
+
+struct InstancedState;  // several objects / instances (instanced.cu)
 
 struct GpuScene {
     int dim = 3;
@@ -103,7 +106,10 @@ struct GpuScene {
         transferred = false;
         wide.clear();
         preloadedWide.clear();
+        inst.reset();
     }
+    // set by fcpwgb_gpu_scene_transfer_instanced instead of a single tree
+    std::shared_ptr<InstancedState> inst;
 
     // query dispatch (variant chosen by wideConfig)
     int closestPoints(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t st);
@@ -130,4 +136,11 @@ struct fcpwgb_gpu_scene : fcpwgb::GpuScene {};
 
 namespace fcpwgb {
 int runRefit(fcpwgb_gpu_scene *s, cudaStream_t st);
+// instanced scenes (instanced.cu); instOut may be NULL
+int instancedClosest(fcpwgb_gpu_scene *s, const DevSphere *spheres, DevInteraction *out, uint32_t *instOut,
+                     uint32_t n, int recordNormal, cudaStream_t st);
+int instancedRays(fcpwgb_gpu_scene *s, const DevRay *rays, DevInteraction *out, uint32_t *instOut, uint32_t n,
+                  int occl, cudaStream_t st);
+int instancedHost(fcpwgb_gpu_scene *s, const void *queries, size_t queryBytes, void *out, uint32_t *instOut,
+                  uint32_t n, bool rays, int flag);
 }

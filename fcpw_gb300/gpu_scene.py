@@ -182,6 +182,7 @@ class _GPUScene:
         check(lib().fcpwgb_gpu_scene_create(self.DIM, self.device, C.byref(handle)))
         self._h = handle
         self._cpu_bvh = None
+        self._instances = None
         self._n_vertices = 0
         self._n_nodes = 0
         self._snch = False
@@ -229,6 +230,16 @@ class _GPUScene:
         if scene._vectorized:
             raise ValueError("transfer_to_gpu needs a scene built with vectorize=False "
                              "(include/fcpw/fcpw_gpu.h:17-20)")
+        if scene.instances is not None:
+            # several objects or instances (fcpwgb_gpu_scene_transfer_instanced)
+            check(lib().fcpwgb_gpu_scene_transfer_instanced(self._h, scene.instances.handle))
+            self._cpu_bvh = None
+            self._instances = scene.instances
+            self._n_vertices = 0
+            self._n_nodes = 0
+            self._snch = False
+            return
+        self._instances = None
         bvh = scene.cpu_bvh
         check(lib().fcpwgb_gpu_scene_transfer_cpu_bvh(self._h, bvh.handle))
         self._cpu_bvh = bvh
@@ -398,6 +409,36 @@ class _GPUScene:
         out = self._out(interactions, len(spheres))
         check(lib().fcpwgb_find_closest_points(self._h, ptr(spheres), ptr(out), len(spheres),
                                                int(bool(record_normals))))
+
+    # -- scenes of several objects or instances ------------------------------
+    def find_closest_points_instanced(self, query_points, squared_max_radii, interactions,
+                                      record_normals: bool = False) -> np.ndarray:
+        """find_closest_points on a scene of several objects or instances, also
+        returning the instance of every answer (UINT_MAX where none); indices
+        are primitive indices within the instance's object."""
+        spheres = R.make_spheres(query_points, squared_max_radii)
+        out = self._out(interactions, len(spheres))
+        inst = np.zeros(len(spheres), np.uint32)
+        check(lib().fcpwgb_find_closest_points_instanced(self._h, ptr(spheres), ptr(out), ptr(inst), len(spheres),
+                                                         int(bool(record_normals))))
+        return inst
+
+    def intersect_rays_instanced(self, ray_origins, ray_directions, ray_distance_bounds, interactions,
+                                 check_for_occlusion: bool = False) -> np.ndarray:
+        """Ray queries on a scene of several objects or instances, returning
+        the instance hit by every ray (UINT_MAX where none)."""
+        rays = R.make_rays(ray_origins, ray_directions, ray_distance_bounds)
+        out = self._out(interactions, len(rays))
+        inst = np.zeros(len(rays), np.uint32)
+        check(lib().fcpwgb_intersect_rays_instanced(self._h, ptr(rays), ptr(out), ptr(inst), len(rays),
+                                                    int(bool(check_for_occlusion))))
+        return inst
+
+    def instance_objects(self) -> np.ndarray:
+        """Object of every instance of the transferred scene."""
+        if getattr(self, "_instances", None) is None:
+            raise RuntimeError("no scene of several objects or instances was transferred")
+        return self._instances.instance_objects.copy()
 
     def find_closest_silhouette_points(self, *args, **kwargs) -> None:
         """python/fcpw_bindings.cpp:622-629"""

@@ -119,6 +119,62 @@ class CpuBvh:
         check(lib().fcpwgb_cpu_bvh_update_positions(self._h, ptr(positions)))
 
 
+class CpuInstances:
+    """Owner of a native instanced structure (fcpwgb_cpu_instances): the
+    objects' host trees, the instances and the top-level tree, as the
+    reference's Scene::build makes them for several objects or instances
+    (fcpw.inl:1053-1102)."""
+
+    def __init__(self, dim: int, objects: list, instance_objects, transforms, aggregate_type: int):
+        self.dim = dim
+        self.objects = list(objects)            # CpuBvh per object (kept alive with this owner)
+        self.instance_objects = np.ascontiguousarray(instance_objects, np.uint32)
+        n = len(self.instance_objects)
+        self.transformed = np.ascontiguousarray([t is not None for t in transforms], np.uint32)
+        mats = np.zeros((n, dim, dim + 1), np.float32)
+        for i, t in enumerate(transforms):
+            if t is not None:
+                m = np.asarray(t, np.float32)
+                if m.shape not in ((dim + 1, dim + 1), (dim, dim + 1)):
+                    raise ValueError(f"instance transforms must be ({dim + 1}, {dim + 1}) or ({dim}, {dim + 1})")
+                mats[i] = m[:dim]
+        self.matrices = np.ascontiguousarray(mats)
+        handles = (C.c_void_p * len(self.objects))(*[o.handle.value for o in self.objects])
+        h = C.c_void_p()
+        check(lib().fcpwgb_cpu_instances_build(dim, int(aggregate_type), C.cast(handles, C.c_void_p),
+                                               len(self.objects), ptr(self.instance_objects), ptr(self.matrices),
+                                               ptr(self.transformed), n, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __len__(self):
+        return len(self.instance_objects)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().fcpwgb_cpu_instances_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def export(self):
+        """(top-level nodes, leaf references (instance indices), (n, 24) float
+        matrices: the 3x4 rows of each transform, then of its inverse)."""
+        nn = C.c_uint32(0)
+        check(lib().fcpwgb_cpu_instances_export(self._h, None, None, None, C.byref(nn)))
+        nodes = np.zeros(nn.value, R.BVH_NODE)
+        refs = np.zeros(len(self) if nn.value else 0, np.uint32)
+        mats = np.zeros((len(self), 24), np.float32)
+        check(lib().fcpwgb_cpu_instances_export(self._h, ptr(nodes) if nn.value else None,
+                                                ptr(refs) if nn.value else None, ptr(mats), C.byref(nn)))
+        return nodes, refs, mats
+
+
 class _Scene:
     DIM = 3
 
@@ -129,12 +185,25 @@ class _Scene:
         self._bvh: CpuBvh | None = None
         self._vectorized = False
         self._aggregate_type = None
+        self._transforms: list = []
+        self._instances: CpuInstances | None = None
 
     # -- geometry ---------------------------------------------------------
     def set_object_count(self, n_objects: int) -> None:
         self._positions = [None] * int(n_objects)
         self._indices = [None] * int(n_objects)
+        self._transforms = [[] for _ in range(int(n_objects))]
         self._bvh = None
+        self._instances = None
+
+    def set_object_instance_transforms(self, transforms, object_index: int) -> None:
+        """Scene::setObjectInstanceTransforms (fcpw.h:70, fcpw.inl:393-397):
+        appends (DIM+1)x(DIM+1) affine matrices (uniform scale) for an object."""
+        for t in transforms:
+            m = np.asarray(t, np.float32)
+            if m.shape != (self.DIM + 1, self.DIM + 1):
+                raise ValueError(f"instance transforms must be ({self.DIM + 1}, {self.DIM + 1}) matrices")
+            self._transforms[object_index].append(m.copy())
 
     def set_object_vertices(self, positions, object_index: int) -> None:
         p = np.asarray(positions, np.float32)
@@ -156,12 +225,37 @@ class _Scene:
 
     def build(self, aggregate_type, vectorize: bool, print_stats: bool = False,
               reduce_memory_footprint: bool = False) -> None:
-        if len(self._positions) != 1 or self._positions[0] is None or self._indices[0] is None:
-            raise ValueError("the GPU path supports scenes with exactly one object "
-                             "(include/fcpw/fcpw_gpu.h:17-20)")
+        """Scene::build (fcpw.inl:1053-1126). One object without instance
+        transforms gives one tree; several objects or instance transforms give
+        a tree per object, the instances in the reference's order (objects in
+        turn; an object without transforms is one untransformed instance) and
+        a top-level tree over them."""
+        if not self._positions or any(p is None for p in self._positions) or \
+                any(i is None for i in self._indices):
+            raise ValueError("every object needs vertices and primitives")
         self._vectorized = bool(vectorize)
         self._aggregate_type = AggregateType(int(aggregate_type))
-        self._bvh = CpuBvh(self.DIM, self._positions[0], self._indices[0], int(aggregate_type), self._silhouettes)
+        self._instances = None
+        if len(self._positions) == 1 and not self._transforms[0]:
+            self._bvh = CpuBvh(self.DIM, self._positions[0], self._indices[0], int(aggregate_type),
+                               self._silhouettes)
+        else:
+            if self._silhouettes:
+                raise NotImplementedError("silhouettes are not supported on scenes of several objects or instances")
+            objs = [CpuBvh(self.DIM, p, f, int(aggregate_type), False) for p, f in zip(self._positions, self._indices)]
+            inst_obj, mats = [], []
+            for k, ts in enumerate(self._transforms):
+                if not ts:
+                    inst_obj.append(k)
+                    mats.append(None)
+                for t in ts:
+                    inst_obj.append(k)
+                    mats.append(t)
+            self._instances = CpuInstances(self.DIM, objs, inst_obj, mats, int(aggregate_type))
+            self._bvh = None
+            if print_stats:
+                print(f"{len(objs)} objects, {len(inst_obj)} instances")
+            return
         if print_stats:
             i = self._bvh.info
             print(f"BVH stats: {i.n_nodes} nodes, {i.n_leaves} leaves, {i.max_depth} max depth, "
@@ -178,8 +272,16 @@ class _Scene:
     @property
     def cpu_bvh(self) -> CpuBvh:
         if self._bvh is None:
+            if self._instances is not None:
+                raise RuntimeError("a scene of several objects or instances has one tree per object "
+                                   "(Scene.instances)")
             raise RuntimeError("Scene.build has not been called")
         return self._bvh
+
+    @property
+    def instances(self) -> CpuInstances | None:
+        """The instanced structure of a scene of several objects or instances (None otherwise)."""
+        return self._instances
 
     def positions(self, object_index: int = 0) -> np.ndarray:
         return self._positions[object_index]

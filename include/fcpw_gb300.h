@@ -178,6 +178,65 @@ int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *scene, int bvh_type,
 /* convenience: transferToGPU straight from a host-built BVH */
 int fcpwgb_gpu_scene_transfer_cpu_bvh(fcpwgb_gpu_scene *scene, const fcpwgb_cpu_bvh *bvh);
 
+/* ----------------------------------------- several objects, instances
+ * Scene<DIM> with several objects and instance transforms
+ * (setObjectCount / setObjectInstanceTransforms, fcpw.h:29-70; the build,
+ * fcpw.inl:1053-1102: one BVH per object, a TransformedAggregate per instance,
+ * core/primitive.h:289-478, and a top-level BVH over the instances). The
+ * reference's GPU path takes single-object scenes only (fcpw_gpu.h:17-20);
+ * here such scenes run on the GPU too.
+ *
+ * fcpwgb_cpu_instances_build: objects are host-built trees (one per object,
+ * fcpwgb_cpu_bvh_build), borrowed until fcpwgb_gpu_scene_transfer_instanced
+ * returns. Instance i uses object instance_objects[i]; transforms (may be
+ * NULL) hold dim x (dim + 1) floats per instance, the rows of the affine map
+ * [A | b] from object to world space (uniform scale, as the reference
+ * requires); transformed (may be NULL: all, when transforms are given) marks
+ * the instances that use their transform; an untransformed instance is the
+ * object itself, like an object without instance transforms in the
+ * reference. Instances are listed in the reference's order: objects in turn,
+ * an object's transforms in turn. The top-level tree is built with the
+ * aggregate type's heuristic over the instance boxes (the object's root box,
+ * or its eight corners mapped and widened by FLT_EPSILON) and centroids (the
+ * mean primitive centroid, mapped), as the reference builds it; a single
+ * instance has no top-level tree. */
+typedef struct fcpwgb_cpu_instances fcpwgb_cpu_instances;
+int fcpwgb_cpu_instances_build(int dim, int aggregate_type, const fcpwgb_cpu_bvh *const *objects,
+                               uint32_t n_objects, const uint32_t *instance_objects,
+                               const float *transforms, const uint32_t *transformed,
+                               uint32_t n_instances, fcpwgb_cpu_instances **out);
+void fcpwgb_cpu_instances_destroy(fcpwgb_cpu_instances *instances);
+/* The top-level tree (n_top_nodes fcpwgb_bvh_node, 0 for a single instance),
+ * its leaf references (instance indices, one per instance in leaf order) and
+ * per instance 24 floats: the 3 x 4 rows of t, then of its inverse (2D: the
+ * z row and column are the identity's). Any output may be NULL. */
+int fcpwgb_cpu_instances_export(const fcpwgb_cpu_instances *instances, void *top_nodes, uint32_t *top_refs,
+                                float *instance_matrices, uint32_t *n_top_nodes);
+/* transferToGPU for such a scene: every object's tree is uploaded as by
+ * fcpwgb_gpu_scene_transfer_cpu_bvh, with the instances and the top-level
+ * tree. Closest point and ray queries (the regular entry points, and the
+ * _instanced ones below that also give each answer's instance) then walk the
+ * top-level tree in the reference's CPU order, each instance's object in
+ * object space on its 4-wide tree (the configured box precision; branching
+ * does not apply), with FP32 results like the reference's. The other query
+ * kinds, refit and exports refuse such a scene (FCPWGB_ERR_UNSUPPORTED). */
+int fcpwgb_gpu_scene_transfer_instanced(fcpwgb_gpu_scene *scene, const fcpwgb_cpu_instances *instances);
+/* instance_out (may be NULL): the instance of each answer, FCPWGB_UINT_MAX
+ * where nothing was found; interactions hold world-space points and normals
+ * and the primitive index within the instance's object */
+int fcpwgb_find_closest_points_instanced(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                         fcpwgb_interaction *interactions, uint32_t *instance_out, uint32_t n,
+                                         int record_normals);
+int fcpwgb_find_closest_points_instanced_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                                fcpwgb_interaction *interactions, uint32_t *instance_out,
+                                                uint32_t n, int record_normals, void *stream);
+int fcpwgb_intersect_rays_instanced(fcpwgb_gpu_scene *scene, const fcpwgb_ray *rays,
+                                    fcpwgb_interaction *interactions, uint32_t *instance_out, uint32_t n,
+                                    int check_for_occlusion);
+int fcpwgb_intersect_rays_instanced_device(fcpwgb_gpu_scene *scene, const fcpwgb_ray *rays,
+                                           fcpwgb_interaction *interactions, uint32_t *instance_out, uint32_t n,
+                                           int check_for_occlusion, void *stream);
+
 /* Scene::build(AggregateType::Bvh, ...) + transferToGPU (fcpw.h:95,
  * fcpw_gpu.h:21) with the tree built on the device: a linear BVH over the
  * Morton codes of the primitive centroids (30-bit in 3D, 32-bit in 2D),

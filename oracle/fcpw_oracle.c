@@ -23,8 +23,10 @@
  *   - Aggregate::contains / hasLineOfSight, core/primitive.h:173-207, with the
  *     all-hits ray traversal bvh.inl:888-1029 and removeDuplicates,
  *     core/interaction.h:20-25,75-94
- * plus an FP64 brute force used as the accuracy yardstick, and a sequential
- * model of the device linear-BVH build (which has no reference counterpart).
+ * plus an FP64 brute force used as the accuracy yardstick, a sequential
+ * model of the device linear-BVH build (which has no reference counterpart)
+ * and the instanced scenes of Scene::build (fcpw.inl:1053-1102) with
+ * TransformedAggregate (core/primitive.h:289-478).
  *
  * Inputs are the flattened tree and records in the reference's GPU interop
  * layouts (include/fcpw/gpu/bvh_interop_structures.h:55-162,730-774).
@@ -280,9 +282,11 @@ static obox load_node(int snch, const void *nodes, uint32_t i) {
 }
 
 /* ------------------------------------------------------ closest point */
-/* bvh.inl:1291-1418 */
-static oint closest_point_bvh_one(int dim, int snch, const void *nodes, const void *prims, osphere s,
-                                  int recordNormal, uint32_t *visited) {
+/* bvh.inl:1291-1418; the sphere's r2 is shrunk in place (as the reference
+   does on its BoundingSphere&), *bestOut receives the winner; returns found */
+static int closest_point_bvh_core(int dim, int snch, const void *nodes, const void *prims, osphere *sp_,
+                                  int recordNormal, oint *bestOut, uint32_t *visited) {
+    osphere s = *sp_;
     oint best = default_interaction();
     int found = 0;
     uint32_t selected = OUMAX;
@@ -351,6 +355,15 @@ static oint closest_point_bvh_one(int dim, int snch, const void *nodes, const vo
         best.n = prim_normal(dim, &pr);
     }
     if (visited) *visited = nv;
+    *sp_ = s;
+    *bestOut = best;
+    return found;
+}
+
+static oint closest_point_bvh_one(int dim, int snch, const void *nodes, const void *prims, osphere s,
+                                  int recordNormal, uint32_t *visited) {
+    oint best;
+    closest_point_bvh_core(dim, snch, nodes, prims, &s, recordNormal, &best, visited);
     return best;
 }
 
@@ -446,7 +459,16 @@ static double ray_segment_f64(od3 pa, od3 pb, od3 o, od3 d, double tMax) {
 }
 
 /* ------------------------------------------------------------------ rays */
-/* bvh.inl:655-771 */
+/* bvh.inl:655-771; r.tMax is shrunk in place, *bestOut receives the hit */
+static oint ray_bvh_one(int dim, int snch, const void *nodes, const void *prims, oray r, int occl, int *hitOut);
+static int ray_bvh_core(int dim, int snch, const void *nodes, const void *prims, oray *rp, int occl, oint *bestOut) {
+    int hit;
+    oint b = ray_bvh_one(dim, snch, nodes, prims, *rp, occl, &hit);
+    /* the traversal's final tMax: the hit distance when something was hit, else unchanged */
+    if (hit && !occl) rp->tMax = minf_(rp->tMax, b.d);
+    *bestOut = b;
+    return hit;
+}
 static oint ray_bvh_one(int dim, int snch, const void *nodes, const void *prims, oray r, int occl, int *hitOut) {
     oint best = default_interaction();
     int didHit = 0;
@@ -1372,4 +1394,265 @@ uint32_t oracle_lbvh_build(int dim, const float *pos, const int32_t *idx, uint32
     }
     free(cent); free(codes); free(order); free(sorted); free(keys);
     return b.count;
+}
+
+/* ------------------------------------------------------------------------
+ * Scenes of several objects and instances (Scene::build, fcpw.inl:1053-1102):
+ * a top-level Bvh whose leaves are aggregates (bvh.inl:1291-1418 and 655-771
+ * with primitiveTypeIsAggregate), an untransformed object queried as it is,
+ * an instance through TransformedAggregate (core/primitive.h:289-478): the
+ * query mapped to object space with tInv (BoundingSphere::transform,
+ * bounding_volumes.h:13-24; Ray::transform, ray.h:19-25), the answer mapped
+ * back with t (Interaction::applyTransform, interaction.h:52-60). With a
+ * single instance the instance is the scene's aggregate (no top-level tree).
+ * Transform arithmetic as the affine Transform of the Eigen API the
+ * reference is compiled against here: row i of t*p is
+ * t(i,D) + t(i,0)*p0 + t(i,1)*p1 [+ t(i,2)*p2], in that order.
+ * Matrices: 24 floats per instance, the 3x4 rows of t then of tInv (2D: the
+ * translation in column 3). */
+typedef struct {
+    const float *t, *ti;
+    uint32_t object, transformed;
+} oinst;
+
+static of3 xf_point(int dim, const float *m, of3 p) {
+    float r[3] = {0.0f, 0.0f, 0.0f};
+    int i;
+    for (i = 0; i < dim; i++) {
+        float acc = m[i * 4 + 3];
+        acc += m[i * 4 + 0] * p.x;
+        acc += m[i * 4 + 1] * p.y;
+        if (dim == 3) acc += m[i * 4 + 2] * p.z;
+        r[i] = acc;
+    }
+    return v3(r[0], r[1], dim == 3 ? r[2] : 0.0f);
+}
+
+static osphere xf_sphere(int dim, const float *m, osphere s) {
+    osphere o;
+    o.c = xf_point(dim, m, s.c);
+    o.r2 = OMAXF;
+    if (s.r2 < OMAXF) {
+        of3 e = v3(s.c.x + sqrtf(s.r2), s.c.y + 0.0f, s.c.z + 0.0f);
+        of3 d = sub3(xf_point(dim, m, e), o.c);
+        o.r2 = dotd(dim, d, d);
+    }
+    return o;
+}
+
+static oray xf_ray(int dim, const float *m, oray r) {
+    of3 to = xf_point(dim, m, r.o);
+    float s = r.tMax < OMAXF ? r.tMax : 1.0f;
+    of3 td = sub3(xf_point(dim, m, add3(r.o, mul3(r.d, s))), to);
+    float nrm = sqrtf(dotd(dim, td, td));
+    return make_ray(dim, to, div3(td, nrm), r.tMax < OMAXF ? nrm : OMAXF);
+}
+
+static void xf_interaction(int dim, const oinst *in, of3 query, oint *c) {
+    float r[3] = {0.0f, 0.0f, 0.0f}, z;
+    of3 d, n;
+    int i;
+    c->p = xf_point(dim, in->t, c->p);
+    d = sub3(c->p, query);
+    c->d = sqrtf(dotd(dim, d, d));
+    /* Transform(tInv^T) * n: row i is tInv(D, i) = 0 plus the column sums */
+    for (i = 0; i < dim; i++) {
+        float acc = 0.0f;
+        acc += in->ti[0 * 4 + i] * c->n.x;
+        acc += in->ti[1 * 4 + i] * c->n.y;
+        if (dim == 3) acc += in->ti[2 * 4 + i] * c->n.z;
+        r[i] = acc;
+    }
+    n = v3(r[0], r[1], dim == 3 ? r[2] : 0.0f);
+    z = dotd(dim, n, n);
+    if (z > 0.0f) n = div3(n, sqrtf(z));
+    c->n = n;
+}
+
+static int inst_closest(int dim, const oinst *in, const void *const *objNodes, const void *const *objPrims,
+                        osphere *s, int recordNormal, oint *c) {
+    const void *nodes = objNodes[in->object], *prims = objPrims[in->object];
+    osphere sInv;
+    int found;
+    if (!in->transformed) return closest_point_bvh_core(dim, 0, nodes, prims, s, recordNormal, c, NULL);
+    sInv = xf_sphere(dim, in->ti, *s);
+    found = closest_point_bvh_core(dim, 0, nodes, prims, &sInv, recordNormal, c, NULL);
+    s->r2 = xf_sphere(dim, in->t, sInv).r2;
+    if (found) xf_interaction(dim, in, s->c, c);
+    return found;
+}
+
+static int inst_ray(int dim, const oinst *in, const void *const *objNodes, const void *const *objPrims, oray *r,
+                    int occl, oint *c) {
+    const void *nodes = objNodes[in->object], *prims = objPrims[in->object];
+    oray rInv;
+    int hit;
+    if (!in->transformed) return ray_bvh_core(dim, 0, nodes, prims, r, occl, c);
+    rInv = xf_ray(dim, in->ti, *r);
+    hit = ray_bvh_core(dim, 0, nodes, prims, &rInv, occl, c);
+    r->tMax = xf_ray(dim, in->t, rInv).tMax;
+    if (hit) xf_interaction(dim, in, r->o, c);
+    return hit;
+}
+
+static oinst inst_of(const float *mats, const uint32_t *object, const uint32_t *transformed, uint32_t k) {
+    oinst in;
+    in.t = mats + (size_t)k * 24;
+    in.ti = mats + (size_t)k * 24 + 12;
+    in.object = object[k];
+    in.transformed = transformed[k];
+    return in;
+}
+
+/* out: n interactions; inst_out: the instance of each answer (OUMAX: none) */
+int oracle_instanced_closest_points(int dim, const void *topNodes, const uint32_t *topRefs, uint32_t nInst,
+                                    const float *mats, const uint32_t *object, const uint32_t *transformed,
+                                    const void *const *objNodes, const void *const *objPrims, const void *spheres,
+                                    uint32_t n, int recordNormal, void *out, uint32_t *instOut) {
+    uint32_t q;
+    for (q = 0; q < n; q++) {
+        osphere s = ((const osphere *)spheres)[q];
+        oint best = default_interaction();
+        uint32_t bi = OUMAX;
+        if (nInst == 1) {
+            oinst in = inst_of(mats, object, transformed, 0);
+            oint c = default_interaction();
+            if (inst_closest(dim, &in, objNodes, objPrims, &s, recordNormal, &c)) { best = c; bi = 0; }
+        } else {
+            uint32_t stackNode[OSTACK];
+            float stackDist[OSTACK], bh[4];
+            obox root = load_node(0, topNodes, 0);
+            box_sq_dist(dim, root.pMin, root.pMax, s.c, &bh[0], &bh[1]);
+            if (bh[0] <= s.r2) {
+                int sp = 0;
+                s.r2 = minf_(s.r2, bh[1]);
+                stackNode[0] = 0;
+                stackDist[0] = bh[0];
+                while (sp >= 0) {
+                    uint32_t ni = stackNode[sp];
+                    float cur = stackDist[sp];
+                    obox node;
+                    sp--;
+                    if (cur > s.r2) continue;
+                    node = load_node(0, topNodes, ni);
+                    if (node.nPrims > 0) {
+                        uint32_t p;
+                        for (p = 0; p < node.nPrims; p++) {
+                            uint32_t k = topRefs[node.offset + p];
+                            oinst in = inst_of(mats, object, transformed, k);
+                            oint c = default_interaction();
+                            if (inst_closest(dim, &in, objNodes, objPrims, &s, recordNormal, &c)) {
+                                s.r2 = minf_(s.r2, c.d * c.d);
+                                best = c;
+                                bi = k;
+                            }
+                        }
+                    } else {
+                        uint32_t li = ni + 1, ri = ni + node.offset, closer, other;
+                        obox l = load_node(0, topNodes, li), r = load_node(0, topNodes, ri);
+                        int hit0, hit1;
+                        box_sq_dist(dim, l.pMin, l.pMax, s.c, &bh[0], &bh[1]);
+                        hit0 = bh[0] <= s.r2;
+                        s.r2 = minf_(s.r2, bh[1]);
+                        box_sq_dist(dim, r.pMin, r.pMax, s.c, &bh[2], &bh[3]);
+                        hit1 = bh[2] <= s.r2;
+                        s.r2 = minf_(s.r2, bh[3]);
+                        if (hit0 && hit1) {
+                            closer = li; other = ri;
+                            if (bh[0] == 0.0f && bh[2] == 0.0f) {
+                                if (bh[3] < bh[1]) { closer = ri; other = li; }
+                            } else if (bh[2] < bh[0]) {
+                                float t = bh[0]; bh[0] = bh[2]; bh[2] = t;
+                                closer = ri; other = li;
+                            }
+                            sp++; stackNode[sp] = other; stackDist[sp] = bh[2];
+                            sp++; stackNode[sp] = closer; stackDist[sp] = bh[0];
+                        } else if (hit0) {
+                            sp++; stackNode[sp] = li; stackDist[sp] = bh[0];
+                        } else if (hit1) {
+                            sp++; stackNode[sp] = ri; stackDist[sp] = bh[2];
+                        }
+                    }
+                }
+            }
+        }
+        ((oint *)out)[q] = best;
+        if (instOut) instOut[q] = bi;
+    }
+    return 0;
+}
+
+/* hit: 1 when the ray hit (with occl: is occluded) */
+int oracle_instanced_rays(int dim, const void *topNodes, const uint32_t *topRefs, uint32_t nInst,
+                          const float *mats, const uint32_t *object, const uint32_t *transformed,
+                          const void *const *objNodes, const void *const *objPrims, const void *rays, uint32_t n,
+                          int occl, void *out, int *hitOut, uint32_t *instOut) {
+    uint32_t q;
+    for (q = 0; q < n; q++) {
+        oray r = ((const oray *)rays)[q];
+        oint best = default_interaction();
+        uint32_t bi = OUMAX;
+        int didHit = 0;
+        r = make_ray(dim, r.o, r.d, r.tMax);
+        if (nInst == 1) {
+            oinst in = inst_of(mats, object, transformed, 0);
+            oint c = default_interaction();
+            if (inst_ray(dim, &in, objNodes, objPrims, &r, occl, &c)) { best = c; bi = 0; didHit = 1; }
+        } else {
+            uint32_t stackNode[OSTACK];
+            float stackDist[OSTACK], bh[4];
+            obox root = load_node(0, topNodes, 0);
+            if (box_ray(dim, root.pMin, root.pMax, &r, &bh[0], &bh[1])) {
+                int sp = 0, done = 0;
+                stackNode[0] = 0;
+                stackDist[0] = bh[0];
+                while (sp >= 0 && !done) {
+                    uint32_t ni = stackNode[sp];
+                    float cur = stackDist[sp];
+                    obox node;
+                    sp--;
+                    if (cur > r.tMax) continue;
+                    node = load_node(0, topNodes, ni);
+                    if (node.nPrims > 0) {
+                        uint32_t p;
+                        for (p = 0; p < node.nPrims; p++) {
+                            uint32_t k = topRefs[node.offset + p];
+                            oinst in = inst_of(mats, object, transformed, k);
+                            oint c = default_interaction();
+                            if (inst_ray(dim, &in, objNodes, objPrims, &r, occl, &c)) {
+                                didHit = 1;
+                                bi = k;
+                                best = c;
+                                if (occl) { done = 1; break; }
+                                r.tMax = minf_(r.tMax, c.d);
+                            }
+                        }
+                    } else {
+                        uint32_t li = ni + 1, ri = ni + node.offset;
+                        obox l = load_node(0, topNodes, li), rr = load_node(0, topNodes, ri);
+                        int hit0 = box_ray(dim, l.pMin, l.pMax, &r, &bh[0], &bh[1]);
+                        int hit1 = box_ray(dim, rr.pMin, rr.pMax, &r, &bh[2], &bh[3]);
+                        if (hit0 && hit1) {
+                            uint32_t closer = li, other = ri;
+                            if (bh[2] < bh[0]) {
+                                float t = bh[0]; bh[0] = bh[2]; bh[2] = t;
+                                t = bh[1]; bh[1] = bh[3]; bh[3] = t;
+                                closer = ri; other = li;
+                            }
+                            sp++; stackNode[sp] = other; stackDist[sp] = bh[2];
+                            sp++; stackNode[sp] = closer; stackDist[sp] = bh[0];
+                        } else if (hit0) {
+                            sp++; stackNode[sp] = li; stackDist[sp] = bh[0];
+                        } else if (hit1) {
+                            sp++; stackNode[sp] = ri; stackDist[sp] = bh[2];
+                        }
+                    }
+                }
+            }
+        }
+        ((oint *)out)[q] = best;
+        if (hitOut) hitOut[q] = didHit;
+        if (instOut) instOut[q] = bi;
+    }
+    return 0;
 }

@@ -36,6 +36,8 @@ def _load():
             "oracle_contains_bvh": [i, i, P, P, P, u, P, i],
             "oracle_line_of_sight_bvh": [i, i, P, P, P, P, u, P, i],
             "oracle_record_sizes": [P],
+            "oracle_instanced_closest_points": [i, P, P, u, P, P, P, P, P, P, u, i, P, P],
+            "oracle_instanced_rays": [i, P, P, u, P, P, P, P, P, P, u, i, P, P, P],
         }
         _lib.oracle_lbvh_build.restype = C.c_uint32
         _lib.oracle_lbvh_build.argtypes = [i, P, P, u, u, P, P, P]
@@ -182,6 +184,55 @@ def lbvh_build(dim, positions, indices, max_leaf=4):
     pv = np.zeros((n, dim), np.int32)
     cnt = _load().oracle_lbvh_build(dim, _p(pos), _p(idx), n, int(max_leaf), _p(nodes), _p(prims), _p(pv))
     return nodes[:cnt], prims, pv
+
+
+def _instanced_args(top_nodes, top_refs, mats, inst_object, inst_transformed, objects):
+    k = len(objects)
+    nodes = [np.ascontiguousarray(o[0]) for o in objects]
+    prims = [np.ascontiguousarray(o[1]) for o in objects]
+    np_ = (C.c_void_p * k)(*[a.ctypes.data for a in nodes])
+    pp_ = (C.c_void_p * k)(*[a.ctypes.data for a in prims])
+    keep = (nodes, prims, np_, pp_)
+    tn = np.ascontiguousarray(top_nodes) if len(top_nodes) else None
+    tr = np.ascontiguousarray(top_refs, np.uint32) if len(top_refs) else None
+    return (keep, tn, tr, np.ascontiguousarray(mats, np.float32), np.ascontiguousarray(inst_object, np.uint32),
+            np.ascontiguousarray(inst_transformed, np.uint32), np_, pp_)
+
+
+def instanced_closest_points(dim, top_nodes, top_refs, mats, inst_object, inst_transformed, objects, spheres,
+                             record_normals=False):
+    """Closest points on a scene of several objects / instances (the
+    reference's top-level walk with TransformedAggregate leaves). objects:
+    per object (nodes, primitives) in the interop layouts; mats: (n, 24) as
+    fcpwgb_cpu_instances_export gives them. Returns (interactions, instance)."""
+    R = _records()
+    keep, tn, tr, m, io, it, np_, pp_ = _instanced_args(top_nodes, top_refs, mats, inst_object, inst_transformed,
+                                                        objects)
+    out = R.default_interactions(len(spheres))
+    inst = np.zeros(len(spheres), np.uint32)
+    sp = np.ascontiguousarray(spheres)
+    _load().oracle_instanced_closest_points(dim, _p(tn), _p(tr), len(io), _p(m), _p(io), _p(it),
+                                            C.cast(np_, C.c_void_p), C.cast(pp_, C.c_void_p), _p(sp), len(sp),
+                                            int(record_normals), _p(out), _p(inst))
+    del keep
+    return out, inst
+
+
+def instanced_rays(dim, top_nodes, top_refs, mats, inst_object, inst_transformed, objects, rays, occlusion=False):
+    """Ray queries on a scene of several objects / instances. Returns
+    (interactions, hit, instance)."""
+    R = _records()
+    keep, tn, tr, m, io, it, np_, pp_ = _instanced_args(top_nodes, top_refs, mats, inst_object, inst_transformed,
+                                                        objects)
+    out = R.default_interactions(len(rays))
+    hit = np.zeros(len(rays), np.int32)
+    inst = np.zeros(len(rays), np.uint32)
+    rr = np.ascontiguousarray(rays)
+    _load().oracle_instanced_rays(dim, _p(tn), _p(tr), len(io), _p(m), _p(io), _p(it), C.cast(np_, C.c_void_p),
+                                  C.cast(pp_, C.c_void_p), _p(rr), len(rr), int(occlusion), _p(out), _p(hit),
+                                  _p(inst))
+    del keep
+    return out, hit.astype(bool), inst
 
 
 def record_sizes():

@@ -227,6 +227,54 @@ void *ref_scene_create(int dim, const float *positions, int nV, const int *indic
     return r;
 }
 
+// A scene of several objects (Scene::setObjectCount, fcpw.h:29-58), each with
+// its own positions and indices, and per object a list of instance
+// transforms (setObjectInstanceTransforms, fcpw.h:70): nTransforms[k]
+// matrices of (DIM+1)^2 row-major floats, concatenated in object order in
+// transforms. An object with no transforms is one untransformed instance.
+void *ref_scene_create_multi(int dim, int nObjects, const float *const *positions, const int *nV,
+                             const int *const *indices, const int *nP, const int *nTransforms,
+                             const float *transforms, int aggregate) {
+    RefScene *r = new RefScene;
+    r->dim = dim;
+    r->snch = false;
+    const float *tm = transforms;
+    auto fill = [&](auto &scene, auto dimTag) {
+        constexpr int D = (int)decltype(dimTag)::value;
+        scene.setObjectCount(nObjects);
+        for (int k = 0; k < nObjects; k++) {
+            std::vector<Vector<D>> pos(nV[k]);
+            for (int i = 0; i < nV[k]; i++) pos[i] = vecOf<D>(positions[k] + (size_t)D * i);
+            scene.setObjectVertices(pos, k);
+            if constexpr (D == 3) {
+                std::vector<Vector3i> idx(nP[k]);
+                for (int i = 0; i < nP[k]; i++)
+                    idx[i] = Vector3i(indices[k][3 * i], indices[k][3 * i + 1], indices[k][3 * i + 2]);
+                scene.setObjectTriangles(idx, k);
+            } else {
+                std::vector<Vector2i> idx(nP[k]);
+                for (int i = 0; i < nP[k]; i++) idx[i] = Vector2i(indices[k][2 * i], indices[k][2 * i + 1]);
+                scene.setObjectLineSegments(idx, k);
+            }
+            if (nTransforms[k] > 0) {
+                std::vector<Transform<D>> ts;
+                for (int t = 0; t < nTransforms[k]; t++) {
+                    Transform<D> x;
+                    for (int a = 0; a <= D; a++)
+                        for (int b = 0; b <= D; b++) x.matrix()(a, b) = tm[a * (D + 1) + b];
+                    tm += (D + 1) * (D + 1);
+                    ts.push_back(x);
+                }
+                scene.setObjectInstanceTransforms(ts, k);
+            }
+        }
+        scene.build((AggregateType)aggregate, false);
+    };
+    if (dim == 3) fill(r->s3, std::integral_constant<size_t, 3>());
+    else fill(r->s2, std::integral_constant<size_t, 2>());
+    return r;
+}
+
 void ref_scene_destroy(void *h) { delete (RefScene *)h; }
 
 // info: nNodes, nLeafs, maxDepth, nPrimitives, nSilhouetteRefs
@@ -249,6 +297,78 @@ int ref_closest_points(void *h, const float *spheres, int n, int recordNormal, v
             agg->findClosestPointFromNode(s, i, 0, agg->getIndex(), nv, recordNormal != 0);
             writeInteraction<D>(i, (unsigned char *)out + 40 * (size_t)q);
             if (visited) visited[q] = nv;
+        });
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return 0;
+}
+
+// The top-level Bvh of a scene of several instances (its primitives are the
+// instances' aggregates): 32 B interop nodes and, per leaf reference, the
+// aggregate's index (objects 0..K-1 in order, then transformed instances in
+// creation order). Returns the node count, 0 when the scene has no top level.
+int ref_export_top(void *h, void *nodes, int *refs) {
+    RefScene *r = (RefScene *)h;
+    auto run = [&](auto &scene, auto dimTag) -> int {
+        constexpr size_t D = decltype(dimTag)::value;
+        using B = Bvh<D, BvhNode<D>, Aggregate<D>, SilhouettePrimitive<D>>;
+        using X = CPUBvhDataExtractor<D, BvhNode<D>, Aggregate<D>, SilhouettePrimitive<D>, RefTag, RefTag, RefTag>;
+        const B *b = dynamic_cast<const B *>(scene.getSceneData()->aggregate.get());
+        if (!b) return 0;
+        const auto &flat = X::flat(b);
+        const auto &pr = X::prims(b);
+        for (size_t i = 0; nodes && i < flat.size(); i++) {
+            const BvhNode<D> &n = flat[i];
+            float f[6] = {n.box.pMin[0], n.box.pMin[1], D == 3 ? n.box.pMin[D - 1] : 0.0f,
+                          n.box.pMax[0], n.box.pMax[1], D == 3 ? n.box.pMax[D - 1] : 0.0f};
+            unsigned char *d = (unsigned char *)nodes + i * 32;
+            std::memcpy(d, f, 24);
+            uint32_t np = (uint32_t)n.nReferences;
+            uint32_t off = (uint32_t)(n.nReferences > 0 ? n.referenceOffset : n.secondChildOffset);
+            std::memcpy(d + 24, &np, 4);
+            std::memcpy(d + 28, &off, 4);
+        }
+        for (size_t k = 0; refs && k < pr.size(); k++) refs[k] = pr[k]->getIndex();
+        return (int)flat.size();
+    };
+    if (r->dim == 3) return run(r->s3, std::integral_constant<size_t, 3>());
+    return run(r->s2, std::integral_constant<size_t, 2>());
+}
+
+// closest points and first hits on any scene, with the interaction's objectIndex
+int ref_closest_points_objects(void *h, const float *spheres, int n, int recordNormal, void *out, int *object) {
+    RefScene *r = (RefScene *)h;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        const Aggregate<D> *agg = scene.getSceneData()->aggregate.get();
+        parallelFor(n, [&](int q) {
+            BoundingSphere<D> s(vecOf<D>(spheres + 4 * q), spheres[4 * q + 3]);
+            Interaction<D> i;
+            int nv = 0;
+            agg->findClosestPointFromNode(s, i, 0, agg->getIndex(), nv, recordNormal != 0);
+            writeInteraction<D>(i, (unsigned char *)out + 40 * (size_t)q);
+            object[q] = i.primitiveIndex < 0 ? -1 : i.objectIndex;
+        });
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return 0;
+}
+
+int ref_intersect_rays_objects(void *h, const float *rays, int n, int occl, void *out, int *hit, int *object) {
+    RefScene *r = (RefScene *)h;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        const Aggregate<D> *agg = scene.getSceneData()->aggregate.get();
+        parallelFor(n, [&](int q) {
+            const float *rr = rays + 10 * q;
+            Ray<D> ray(vecOf<D>(rr), vecOf<D>(rr + 3), rr[9]);
+            Interaction<D> i;
+            bool hh = agg->intersect(ray, i, occl != 0);
+            writeInteraction<D>(i, (unsigned char *)out + 40 * (size_t)q);
+            hit[q] = hh ? 1 : 0;
+            object[q] = hh ? i.objectIndex : -1;
         });
     };
     if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());

@@ -31,10 +31,15 @@ def _load():
         _lib.ref_scene_create.restype = P
         _lib.ref_scene_create.argtypes = [i, P, i, P, i, i, i]
         _lib.ref_scene_destroy.argtypes = [P]
+        _lib.ref_scene_create_multi.restype = P
+        _lib.ref_scene_create_multi.argtypes = [i, i, P, P, P, P, P, P, i]
         for name, args in {"ref_export": [P, P, P, P, P], "ref_closest_points": [P, P, i, i, P, P],
                            "ref_intersect_rays": [P, P, i, i, P, P], "ref_silhouettes": [P, P, P, i, f, f, P],
                            "ref_sphere_sample": [P, P, P, i, P, P], "ref_update_and_refit": [P, P, i],
-                           "ref_contains": [P, P, i, P], "ref_line_of_sight": [P, P, P, i, P]}.items():
+                           "ref_contains": [P, P, i, P], "ref_line_of_sight": [P, P, P, i, P],
+                           "ref_closest_points_objects": [P, P, i, i, P, P],
+                           "ref_intersect_rays_objects": [P, P, i, i, P, P, P],
+                           "ref_export_top": [P, P, P]}.items():
             fn = getattr(_lib, name)
             fn.restype = i
             fn.argtypes = args
@@ -128,3 +133,54 @@ class RefScene:
     def update_and_refit(self, positions):
         pos = np.ascontiguousarray(positions, np.float32)
         _load().ref_update_and_refit(self._h, _p(pos), len(pos))
+
+
+class RefMultiScene(RefScene):
+    """The reference Scene<DIM> with several objects and instance transforms
+    (setObjectCount / setObjectInstanceTransforms), built with vectorize=False.
+    objects: list of (positions, indices); transforms: per object a list of
+    (DIM+1)x(DIM+1) matrices (empty: one untransformed instance)."""
+
+    def __init__(self, dim, objects, transforms, aggregate_type=3):
+        self.dim = dim
+        self.silhouettes = False
+        self._pos = [np.ascontiguousarray(p, np.float32) for p, _ in objects]
+        self._idx = [np.ascontiguousarray(f, np.int32) for _, f in objects]
+        k = len(objects)
+        pp = (C.c_void_p * k)(*[a.ctypes.data for a in self._pos])
+        ip = (C.c_void_p * k)(*[a.ctypes.data for a in self._idx])
+        nv = np.array([len(a) for a in self._pos], np.int32)
+        npr = np.array([len(a) for a in self._idx], np.int32)
+        nt = np.array([len(t) for t in transforms], np.int32)
+        self._transforms = [list(t) for t in transforms]
+        mats = [np.asarray(m, np.float32).reshape(dim + 1, dim + 1) for t in transforms for m in t]
+        self._tm = np.ascontiguousarray(np.concatenate([m.reshape(-1) for m in mats]) if mats
+                                        else np.zeros(1, np.float32))
+        self._h = _load().ref_scene_create_multi(dim, k, C.cast(pp, C.c_void_p), _p(nv), C.cast(ip, C.c_void_p),
+                                                 _p(npr), _p(nt), _p(self._tm), int(aggregate_type))
+
+    def closest_points_objects(self, spheres, record_normals=False):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        obj = np.zeros(len(spheres), np.int32)
+        _load().ref_closest_points_objects(self._h, _p(self._sph(spheres)), len(spheres), int(record_normals),
+                                           _p(out), _p(obj))
+        return out, obj
+
+    def intersect_rays_objects(self, rays, occlusion=False):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(rays), R.INTERACTION)
+        hit = np.zeros(len(rays), np.int32)
+        obj = np.zeros(len(rays), np.int32)
+        r = np.ascontiguousarray(rays).view(np.float32)
+        _load().ref_intersect_rays_objects(self._h, _p(r), len(rays), int(occlusion), _p(out), _p(hit), _p(obj))
+        return out, hit.astype(bool), obj
+
+    def export_top(self):
+        """(nodes, aggregate index per leaf reference) of the top-level tree."""
+        from fcpw_gb300 import records as R
+        n = _load().ref_export_top(self._h, None, None)
+        nodes = np.zeros(n, R.BVH_NODE)
+        refs = np.zeros(sum(len(t) or 1 for t in self._transforms), np.int32)
+        _load().ref_export_top(self._h, _p(nodes), _p(refs))
+        return nodes, refs

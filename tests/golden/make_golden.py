@@ -3,14 +3,16 @@
 Run where the reference checkout exists (default /root/reference, override with
 FCPW_REFERENCE_ROOT):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names]
 
 Each fixture holds a small seeded scene, the reference's flattened BVH
 (reference Scene<DIM>::build with vectorize=false, read in the GPU interop
 layouts) and the reference CPU query results on seeded queries: closest points
 (infinite and finite radius, with normals), rays (first hit and occlusion),
 closest silhouette points, sphere sampling and a refit after moving the
-vertices. The reference is compiled from its own headers against the Eigen API
+vertices; the instanced fixtures hold scenes of several objects with
+instance transforms, the reference's top-level tree and its answers with the
+object of every result. The reference is compiled from its own headers against the Eigen API
 shim in oracle/compat (oracle/build.py).
 """
 from __future__ import annotations
@@ -26,7 +28,7 @@ sys.path.insert(0, str(ROOT))
 
 from fcpw_gb300 import records as R  # noqa: E402
 from fcpw_gb300 import workloads as W  # noqa: E402
-from oracle.reference import RefScene, available  # noqa: E402
+from oracle.reference import RefMultiScene, RefScene, available  # noqa: E402
 
 SEED = 777
 
@@ -86,18 +88,96 @@ def make(name, dim, verts, idx, aggregate, silhouettes, box, n=1500):
     print(f"{name}: {len(nodes)} nodes, {len(prims)} primitives, {0 if sils is None else len(sils)} silhouettes")
 
 
-def main():
+def affine(dim, rng):
+    """Seeded (dim+1)x(dim+1) affine map: a rotation, a uniform scale in
+    [0.3, 1.2] and a translation in [-4, 4]^dim."""
+    m = np.eye(dim + 1)
+    if dim == 3:
+        a = rng.normal(size=3)
+        a /= np.linalg.norm(a)
+        ang = rng.uniform(0, 2 * np.pi)
+        k = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+        rot = np.eye(3) * np.cos(ang) + np.sin(ang) * k + (1 - np.cos(ang)) * np.outer(a, a)
+    else:
+        ang = rng.uniform(0, 2 * np.pi)
+        rot = np.array([[np.cos(ang), -np.sin(ang)], [np.sin(ang), np.cos(ang)]])
+    m[:dim, :dim] = rot * rng.uniform(0.3, 1.2)
+    m[:dim, dim] = rng.uniform(-4, 4, dim)
+    return m.astype(np.float32)
+
+
+def make_instanced(name, dim, objects, n_transforms, aggregate, box, seed, n=2000):
+    """A scene of several objects with instance transforms (Scene::setObjectCount,
+    setObjectInstanceTransforms): the reference's top-level tree (leaf
+    references as instance numbers: objects in turn, an object without
+    transforms one instance, an object's transforms in turn) and its answers
+    with the object index of every result."""
+    rng = np.random.default_rng(seed)
+    transforms = [[affine(dim, rng) for _ in range(k)] for k in n_transforms]
+    ref = RefMultiScene(dim, objects, transforms, aggregate)
+    top_nodes, agg_refs = ref.export_top()
+    agg_to_inst, inst, nxt = {}, 0, len(objects)
+    for k, ts in enumerate(transforms):
+        if not ts:
+            agg_to_inst[k] = inst
+            inst += 1
+        for _ in ts:
+            agg_to_inst[nxt] = inst
+            nxt += 1
+            inst += 1
+    top_refs = np.array([agg_to_inst[int(a)] for a in agg_refs] if len(top_nodes) else [], np.uint32)
+    out = {"dim": dim, "aggregate": aggregate, "n_objects": len(objects),
+           "n_transforms": np.array(n_transforms, np.int32),
+           "transforms": np.array([m for ts in transforms for m in ts], np.float32).reshape(-1, dim + 1, dim + 1),
+           "top_nodes": top_nodes, "top_refs": top_refs}
+    for k, (v, f) in enumerate(objects):
+        out[f"obj{k}_positions"] = v
+        out[f"obj{k}_indices"] = f
+    lo, hi = box
+    pts = _queries(dim, n, lo, hi, seed + 1)
+    res, obj = ref.closest_points_objects(R.make_spheres(pts, R.FLT_MAX), record_normals=True)
+    r2 = (W.rng(seed + 2).uniform(0, 1, n) * 0.5).astype(np.float32)
+    res2, obj2 = ref.closest_points_objects(R.make_spheres(pts, r2), record_normals=False)
+    o = _queries(dim, n, lo, hi, seed + 3)
+    d = W.uniform_directions(n, dim, seed + 4)
+    rays = R.make_rays(o, d, R.FLT_MAX)
+    ro, rh, robj = ref.intersect_rays_objects(rays)
+    _, oh, _ = ref.intersect_rays_objects(rays, occlusion=True)
+    out.update(cp_points=pts, cp_out=res, cp_object=obj, cpr_r2=r2, cpr_out=res2, cpr_object=obj2,
+               ray_o=o, ray_d=d, ray_out=ro, ray_hit=rh, ray_object=robj, occ_hit=oh)
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(f"{name}: {len(objects)} objects, {inst} instances, {len(top_nodes)} top-level nodes")
+
+
+def main(names=()):
     if not available():
         raise SystemExit("the reference checkout is required to regenerate the golden fixtures")
+    want = lambda n: not names or n in names  # noqa: E731
     v, f = W.perturbed_sphere(8, SEED)
-    make("sphere3d_sah", 3, v, f, 3, False, (-1.5, 1.5))
-    make("sphere3d_overlap_sah", 3, v, f, 2, False, (-1.5, 1.5))
+    if want("sphere3d_sah"):
+        make("sphere3d_sah", 3, v, f, 3, False, (-1.5, 1.5))
+    if want("sphere3d_overlap_sah"):
+        make("sphere3d_overlap_sah", 3, v, f, 2, False, (-1.5, 1.5))
     vt, ft = W.torus(32, 16, SEED + 10)
-    make("torus3d_snch", 3, vt, ft, 3, True, (-2.0, 2.0))
+    if want("torus3d_snch"):
+        make("torus3d_snch", 3, vt, ft, 3, True, (-2.0, 2.0))
     vs, sg = W.star_polylines(9, 32, SEED + 11)
-    make("stars2d_snch", 2, vs, sg, 3, True, (-3.0, 3.0))
-    make("stars2d_bvh", 2, vs, sg, 1, False, (-3.0, 3.0))
+    if want("stars2d_snch"):
+        make("stars2d_snch", 2, vs, sg, 3, True, (-3.0, 3.0))
+    if want("stars2d_bvh"):
+        make("stars2d_bvh", 2, vs, sg, 1, False, (-3.0, 3.0))
+    vs2, fs2 = W.torus(16, 8, SEED + 13)
+    if want("instanced3d"):
+        make_instanced("instanced3d", 3, [(vt, ft), (v, f), (vs2, fs2)], [13, 0, 7], 3, (-5.0, 5.0), SEED + 20)
+    if want("instanced3d_single"):
+        make_instanced("instanced3d_single", 3, [(vt, ft)], [1], 3, (-5.0, 5.0), SEED + 30)
+    if want("multi3d_plain"):
+        make_instanced("multi3d_plain", 3, [(vt, ft), (v, f)], [0, 0], 2, (-2.5, 2.5), SEED + 40)
+    s0, g0 = W.star_polylines(2, 64, SEED + 14)
+    s1, g1 = W.star_polylines(1, 40, SEED + 15)
+    if want("instanced2d"):
+        make_instanced("instanced2d", 2, [(s0, g0), (s1, g1)], [9, 6], 3, (-5.0, 5.0), SEED + 50)
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -10,7 +10,9 @@ from fcpw_gb300 import records as R
 from helpers import build_scene
 from oracle import oracle as O
 
-GOLDEN = sorted((Path(__file__).resolve().parent / "golden").glob("*.npz"))
+# single-tree fixtures (the instanced ones are covered by test_*_instanced.py)
+GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz")
+                if not p.name.startswith(("instanced", "multi")))
 
 
 def load(p):

@@ -13,7 +13,9 @@ from helpers import compare_closest, distance_tolerance
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN = sorted((Path(__file__).resolve().parent / "golden").glob("*.npz"))
+# single-tree fixtures (the instanced ones are covered by test_*_instanced.py)
+GOLDEN = sorted(p for p in (Path(__file__).resolve().parent / "golden").glob("*.npz")
+                if not p.name.startswith(("instanced", "multi")))
 
 
 def bvh_type(fx):

@@ -1,0 +1,244 @@
+"""Scenes of several objects and instances on the GPU: closest points and
+rays through the C ABI against the reference's own answers
+(tests/golden/instanced*.npz) and, on a larger seeded scene, against the
+oracle's restatement of the reference's instanced traversal; the regular and
+the _instanced entry points agree; single-tree operations refuse such a
+scene."""
+import numpy as np
+import pytest
+
+import fcpw_gb300 as F
+from fcpw_gb300 import records as R
+from fcpw_gb300 import workloads as W
+from helpers import distance_tolerance
+from oracle import oracle as O
+from test_cpu_instanced import NAMES, load, oracle_inputs, scene_of
+
+pytestmark = pytest.mark.gpu
+
+
+def world_prims(s):
+    """Per instance, its object's primitives mapped to world space (FP64 map, FP32 records)."""
+    inst = s.instances
+    _, _, mats = inst.export()
+    dim = s.DIM
+    out = []
+    for i, k in enumerate(inst.instance_objects):
+        v = s.positions(int(k)).astype(np.float64)
+        f = s.indices(int(k))
+        if inst.transformed[i]:
+            t = mats[i, :12].reshape(3, 4).astype(np.float64)
+            v = v @ t[:dim, :dim].T + t[:dim, 3]
+        v = v.astype(np.float32)
+        p = np.zeros(len(f), R.TRIANGLE if dim == 3 else R.LINE_SEGMENT)
+        for j, c in enumerate(("pa", "pb", "pc")[:dim]):
+            p[c][:, :dim] = v[f[:, j]]
+        p["index"] = np.arange(len(f))
+        out.append(p)
+    return out
+
+
+def compare_instanced(s, pts, got, got_inst, ref, ref_obj, what):
+    """Found flags equal, distances within the parity tolerance of helpers.py,
+    and (object, primitive) equal unless tied in FP64: the reference reports
+    the object only, so its candidate's FP64 distance is the minimum over
+    that object's instances."""
+    dim = s.DIM
+    inst = s.instances
+    fg = got_inst != R.UINT_MAX
+    fr = np.asarray(ref_obj) >= 0
+    assert np.array_equal(fg, fr), f"{what}: found/not-found differs for {np.count_nonzero(fg != fr)} queries"
+    m = np.nonzero(fr)[0]
+    tol = distance_tolerance(pts[m], ref["p"][m][:, :dim], ref["d"][m])
+    dd = np.abs(got["d"][m].astype(np.float64) - ref["d"][m].astype(np.float64))
+    assert (dd <= tol).all(), f"{what}: worst |dd| {dd.max():.3e}"
+    gobj = inst.instance_objects[got_inst[m]].astype(np.int64)
+    mism = (gobj != ref_obj[m]) | (got["index"][m] != ref["index"][m])
+    if mism.any():
+        wp = world_prims(s)
+        for j in np.nonzero(mism)[0]:
+            q = m[j]
+            x = pts[q:q + 1]
+            dg = O.prim_distance_f64(dim, wp[got_inst[q]], [got["index"][q]], x)[0]
+            dr = min(O.prim_distance_f64(dim, wp[i], [ref["index"][q]], x)[0]
+                     for i in np.nonzero(inst.instance_objects == ref_obj[q])[0])
+            assert abs(dg - dr) <= 2 * tol[j], f"{what}: query {q} is not a tie"
+    return int(mism.sum())
+
+
+def gpu_of(s, **cfg):
+    g = F.GPUScene3D() if s.DIM == 3 else F.GPUScene2D()
+    if cfg:
+        g.set_traversal(**cfg)
+    g.transfer_to_gpu(s)
+    return g
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("bits", [32, 8])
+def test_closest_points_match_reference(name, bits):
+    gd = load(name)
+    s = scene_of(gd)
+    g = gpu_of(s, branching=4, bits=bits)
+    pts = gd["cp_points"]
+    for r2, key, normals in ((R.FLT_MAX, "cp", True), (gd["cpr_r2"], "cpr", False)):
+        out = F.GPUInteractionList()
+        which = g.find_closest_points_instanced(pts, np.broadcast_to(np.float32(r2), (len(pts),)).copy(), out,
+                                                normals)
+        got = out.array()
+        ref = gd[f"{key}_out"]
+        compare_instanced(s, pts, got, which, ref, gd[f"{key}_object"], f"{name} {key} bits {bits}")
+        if normals:
+            same = (got["index"] == ref["index"]) & (which != R.UINT_MAX)
+            assert np.allclose(got["n"][same], ref["n"][same], atol=1e-5)
+    assert g.check_errors() == 0
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_rays_match_reference(name):
+    gd = load(name)
+    s = scene_of(gd)
+    g = gpu_of(s, branching=4, bits=32)
+    o, d = gd["ray_o"], gd["ray_d"]
+    tmax = np.full(len(o), R.FLT_MAX, np.float32)
+    out = F.GPUInteractionList()
+    which = g.intersect_rays_instanced(o, d, tmax, out)
+    got = out.array()
+    hit = which != R.UINT_MAX
+    ref, rhit = gd["ray_out"], gd["ray_hit"]
+    assert (hit != rhit).sum() <= max(2, int(1e-4 * len(o)))
+    both = hit & rhit
+    assert np.all(np.abs(got["d"][both] - ref["d"][both]) <= 1e-5 * np.maximum(ref["d"][both], 1.0))
+    gobj = s.instances.instance_objects[which[both]].astype(np.int64)
+    same = (got["index"][both] == ref["index"][both]) & (gobj == gd["ray_object"][both])
+    assert same.mean() > 0.999
+    out2 = F.GPUInteractionList()
+    occ = g.intersect_rays_instanced(o, d, tmax, out2, True) != R.UINT_MAX
+    assert (occ != gd["occ_hit"]).sum() <= max(2, int(1e-4 * len(o)))
+
+
+def random_affines(n, rng, spread=6.0):
+    out = []
+    for _ in range(n):
+        a = rng.normal(size=3)
+        a /= np.linalg.norm(a)
+        ang = rng.uniform(0, 2 * np.pi)
+        k = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+        rot = np.eye(3) * np.cos(ang) + np.sin(ang) * k + (1 - np.cos(ang)) * np.outer(a, a)
+        m = np.eye(4)
+        m[:3, :3] = rot * rng.uniform(0.2, 0.9)
+        m[:3, 3] = rng.uniform(-spread, spread, 3)
+        out.append(m.astype(np.float32))
+    return out
+
+
+@pytest.fixture(scope="module")
+def many_instances():
+    rng = np.random.default_rng(2024)
+    v0, f0 = W.torus(96, 48, W.SEED_BASE + 110)
+    v1, f1 = W.perturbed_sphere(12, W.SEED_BASE + 111)
+    s = F.Scene3D()
+    s.set_object_count(3)
+    objs = [(v0, f0), (v1, f1), ((v1 * 0.5 + 3.0).astype(np.float32), f1)]
+    for k, (v, f) in enumerate(objs):
+        s.set_object_vertices(v, k)
+        s.set_object_triangles(f, k)
+    s.set_object_instance_transforms(random_affines(40, rng), 0)
+    s.set_object_instance_transforms(random_affines(25, rng), 1)
+    s.build(F.AggregateType.Bvh_SurfaceArea, False)
+    pts = W.uniform_points(60000, 3, -7, 7, 112)
+    inst, tn, tr, mats, ob = oracle_inputs(s)
+    ref, ref_inst = O.instanced_closest_points(3, tn, tr, mats, inst.instance_objects, inst.transformed, ob,
+                                               R.make_spheres(pts, R.FLT_MAX), False)
+    ref_obj = np.where(ref_inst != R.UINT_MAX,
+                       inst.instance_objects[np.minimum(ref_inst, len(inst) - 1)].astype(np.int64), -1)
+    return s, pts, ref, ref_obj
+
+
+@pytest.mark.parametrize("cfg", [dict(bits=32), dict(bits=16, leaf_size=8), dict(bits=8, sort_queries=False)])
+def test_many_instances_match_oracle(many_instances, cfg):
+    s, pts, ref, ref_obj = many_instances
+    g = gpu_of(s, branching=4, **cfg)
+    out = F.GPUInteractionList()
+    which = g.find_closest_points_instanced(pts, np.full(len(pts), R.FLT_MAX, np.float32), out)
+    compare_instanced(s, pts, out.array(), which, ref, ref_obj, f"66 instances {cfg}")
+    assert g.check_errors() == 0
+
+
+def test_entry_points_agree_and_repeat(many_instances):
+    """The regular host and device entry points give the _instanced answers,
+    and a second call (sorted and unsorted) repeats them byte for byte."""
+    import torch
+    s, pts, _, _ = many_instances
+    pts = pts[:20000]
+    r2 = np.full(len(pts), R.FLT_MAX, np.float32)
+    g = gpu_of(s, branching=4, bits=32)
+    out = F.GPUInteractionList()
+    which = g.find_closest_points_instanced(pts, r2, out)
+    first = out.array().tobytes()
+    out2 = F.GPUInteractionList()
+    assert g.find_closest_points_instanced(pts, r2, out2).tobytes() == which.tobytes()
+    assert out2.array().tobytes() == first
+    plain = F.GPUInteractionList()
+    g.find_closest_points(pts, r2, plain)
+    assert plain.array().tobytes() == first
+    sph = torch.zeros((len(pts), 4), dtype=torch.float32, device="cuda")
+    sph[:, :3] = torch.from_numpy(pts).cuda()
+    sph[:, 3] = float(R.FLT_MAX)
+    res = g.find_closest_points_tensor(sph)
+    torch.cuda.synchronize()
+    assert res.raw.cpu().numpy().view(R.INTERACTION).reshape(-1).tobytes() == first
+
+
+def test_layouts_agree(many_instances):
+    """Records of every box precision and leaf size, compared with the float
+    layout: the answers are the same primitives; where records differ, the
+    message says in which fields."""
+    s, pts, _, _ = many_instances
+    pts = pts[:20000]
+    r2 = np.full(len(pts), R.FLT_MAX, np.float32)
+    base = None
+    report = []
+    for cfg in [dict(bits=32), dict(bits=8), dict(bits=16, leaf_size=6), dict(bits=32, sort_queries=False)]:
+        g = gpu_of(s, branching=4, **cfg)
+        out = F.GPUInteractionList()
+        which = g.find_closest_points_instanced(pts, r2, out)
+        rec = out.array()
+        if base is None:
+            base = (rec, which)
+            continue
+        diff = rec.tobytes() != base[0].tobytes() or which.tobytes() != base[1].tobytes()
+        if diff:
+            fields = {f: int(np.count_nonzero((rec[f] != base[0][f]).reshape(len(rec), -1).any(1)))
+                      for f in ("p", "n", "uv", "d", "index")}
+            fields["instance"] = int(np.count_nonzero(which != base[1]))
+            k = int(np.nonzero((which != base[1]) | (rec["d"] != base[0]["d"]))[0][:1].tolist()[0]) \
+                if (fields["instance"] or fields["d"]) else -1
+            sample = (f" first: query {k}, d {rec['d'][k]!r} vs {base[0]['d'][k]!r}, instance {which[k]} vs "
+                      f"{base[1][k]}, index {rec['index'][k]} vs {base[0]['index'][k]}") if k >= 0 else ""
+            report.append(f"{cfg}: {fields}{sample}")
+    assert not report, "; ".join(report)
+
+
+def test_single_tree_operations_refuse_instanced_scene():
+    gd = load("instanced3d")
+    s = scene_of(gd)
+    g = gpu_of(s)
+    pts = gd["cp_points"][:100]
+    with pytest.raises(F.FcpwError):
+        g.refit_arrays()
+    with pytest.raises(F.FcpwError):
+        g.find_closest_silhouette_points(pts, np.full(100, R.FLT_MAX, np.float32), np.zeros(100, np.uint32),
+                                         F.GPUInteractionList())
+    with pytest.raises(F.FcpwError):
+        g.contains(pts)
+    # a single-tree transfer replaces the instanced scene
+    one = F.Scene3D()
+    one.set_object_count(1)
+    one.set_object_vertices(gd["obj0_positions"], 0)
+    one.set_object_triangles(gd["obj0_indices"], 0)
+    one.build(F.AggregateType.Bvh_SurfaceArea, False)
+    g.transfer_to_gpu(one)
+    out = F.GPUInteractionList()
+    g.find_closest_points(pts, np.full(100, R.FLT_MAX, np.float32), out)
+    assert (out.array()["index"] != R.UINT_MAX).all()
