@@ -240,31 +240,39 @@ template<> struct Count<true> {
     FCPWGB_D unsigned long long get() const { return v; }
 };
 
+// Rounding band of a distance. The band, 8 units of 2^-24 times
+// (|c|_inf + d), bounds the FP32 error of a point-primitive or point-box
+// distance with coordinates of magnitude |c| + d. Boxes are visited while
+// their distance is within the winner's distance plus the band (in every
+// mode): a box holding a primitive at exactly the winner's distance can then
+// not be pruned by rounding, which at query coordinates much larger than the
+// box padding (FLT_EPSILON) would otherwise happen, and exact ties resolve
+// by the rule of beatsWinner whatever the visiting order.
+//
 // Near ties of the precise mode. The FP32 traversal picks its winner with the
 // reference's rounding, but a primitive whose FP32 distance lies within the
-// rounding band of the winner's may be the closer one in exact arithmetic.
-// So the precise mode prunes boxes against the winner's distance plus that
-// band, keeps the best primitive within the band other than the winner (the
-// runner-up), and refines both in FP64 at the end. The band, 8 units of
-// 2^-24 times (|c|_inf + d), bounds the FP32 error of a point-primitive
-// distance with coordinates of magnitude |c| + d. Without it, near-tied
-// segments of a polyline gave 7.5e-7 relative error on 1024 2D samples.
+// band of the winner's may be the closer one in exact arithmetic. So the
+// precise mode also keeps the best primitive within the band other than the
+// winner (the runner-up) and refines both in FP64 at the end. Without it,
+// near-tied segments of a polyline gave 7.5e-7 relative error on 1024 2D
+// samples.
 constexpr float kBandEps = 8.0f * 5.9604645e-8f;
-template<bool TRACK> struct NearTie {  // off: no state
-    FCPWGB_D float prune(float r2, float3) const { return r2; }
-    FCPWGB_D float pruneHit(float d, float3) const { return d * d; }
+FCPWGB_D float tieBand(float3 c, float d) { return kBandEps * (fmax3(fabsf(c.x), fabsf(c.y), fabsf(c.z)) + d); }
+FCPWGB_D float bandRadius2(float d, float3 c) {
+    float t = d + tieBand(c, d);
+    return t * t;
+}
+template<bool TRACK> struct NearTie {  // off: no runner-up state, the same visiting radius
+    FCPWGB_D float prune(float r2, float3 c) const { return bandRadius2(sqrtf(r2), c); }
+    FCPWGB_D float pruneHit(float d, float3 c) const { return bandRadius2(d, c); }
     FCPWGB_D void replaced(float, uint32_t) {}
     FCPWGB_D void offer(float, uint32_t) {}
 };
-FCPWGB_D float tieBand(float3 c, float d) { return kBandEps * (fmax3(fabsf(c.x), fabsf(c.y), fabsf(c.z)) + d); }
 template<> struct NearTie<true> {  // two registers; the band is recomputed from the query when needed
     float d2nd = kFltMax;
     uint32_t sel2nd = kUintMax;
-    FCPWGB_D float pruneHit(float d, float3 c) const {
-        float t = d + tieBand(c, d);
-        return t * t;
-    }
-    FCPWGB_D float prune(float r2, float3 c) const { return pruneHit(sqrtf(r2), c); }
+    FCPWGB_D float pruneHit(float d, float3 c) const { return bandRadius2(d, c); }
+    FCPWGB_D float prune(float r2, float3 c) const { return bandRadius2(sqrtf(r2), c); }
     // the previous winner becomes the runner-up when a primitive beats it
     FCPWGB_D void replaced(float d, uint32_t sel) {
         d2nd = d;
@@ -283,13 +291,12 @@ template<> struct NearTie<true> {  // two registers; the band is recomputed from
 // Whether a tested primitive (distance d, leaf position sel) becomes the
 // winner: before the first hit when d*d <= r2 (the caller's radius, or a
 // child's far distance); after it (r2 is then the winner's d*d) on a smaller
-// distance, or on an equal one with an earlier leaf position. Boxes hold
-// their primitives with a margin (vertices widened by FLT_EPSILON, outward
-// quantisation) and visits are inclusive (d2Min <= r2), so every primitive at
-// the winner's distance is visited and an exact tie resolves to the same
-// primitive in any visiting order: the result depends neither on the order
-// of the queries, nor on which queries share a warp, nor on the wide layout.
-// The runner-up of NearTie is ranked the same way.
+// distance, or on an equal one with an earlier leaf position. Boxes are
+// visited within the winner's distance plus the rounding band (NearTie), so
+// every primitive at the winner's distance is tested and an exact tie
+// resolves to the same primitive in any visiting order: the result depends
+// neither on the order of the queries, nor on which queries share a warp,
+// nor on the wide layout. The runner-up of NearTie is ranked the same way.
 FCPWGB_D bool beatsWinner(bool found, float d, float r2, float bestD, uint32_t sel, uint32_t selected) {
     return found ? (d < bestD || (d == bestD && sel < selected)) : d * d <= r2;
 }

@@ -228,12 +228,16 @@ def test_warp_cooperative_results_repeat_exactly(torus):
 
 
 @pytest.mark.parametrize("precise", [False, True])
-def test_every_wide_layout_and_schedule_agrees_exactly(torus, precise):
+@pytest.mark.parametrize("scale", [1.0, 25.0])
+def test_every_wide_layout_and_schedule_agrees_exactly(torus, precise, scale):
     """The winner (and in precise mode the runner-up) is the first primitive
     in leaf order among those at the smallest distance, which every layout
-    and schedule visits: results are byte-identical across all of them."""
+    and schedule visits (boxes are visited within the winner's distance plus
+    the rounding band): results are byte-identical across all of them, also
+    for queries far from the mesh (scale 25), where box distances round
+    coarser than the box padding."""
     s, g, pts, ref, prims = torus
-    sub = pts[:40000]
+    sub = (pts[:40000] * np.float32(scale)).astype(np.float32)
     outs = {}
     for cfg in [dict(branching=4, bits=32, packet=True), dict(branching=4, bits=32, persistent=False),
                 dict(branching=4, bits=32, persistent=True), dict(branching=2, bits=16),
