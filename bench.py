@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven scenes measurement")
     ap.add_argument("--suite", action="store_true",
                     help="instead of the headline line, one line per other configuration of the scope")
-    ap.add_argument("--only", default="", help="with --suite: comma-separated subset of c1,rays,c3,sil3d,inside")
+    ap.add_argument("--only", default="", help="with --suite: comma-separated subset of c1,rays,c3,sil3d,inside,instanced,build")
     return ap.parse_args()
 
 
@@ -458,6 +458,95 @@ def run_suite(args):
         lines.append({"config": "line of sight, torus 1,048,576 triangles, 4,194,304 point pairs", "queries": n,
                       "gpu": {"queries_per_s": n / (los_ms / 1e3), "ms": los_ms}, "visible_fraction": visible,
                       "cpu_baseline": cpu_los})
+
+    # several objects with instance transforms: 64 rotated and scaled copies of a 65,536-triangle torus,
+    # 64 of a 20,480-triangle sphere and one untransformed sphere, 4,194,304 queries in [-8, 8]^3
+    if want("instanced"):
+        rng = np.random.default_rng(W.SEED_BASE + 5005)
+
+        def affines(k):
+            out_m = []
+            for _ in range(k):
+                a = rng.normal(size=3)
+                a /= np.linalg.norm(a)
+                ang = rng.uniform(0, 2 * np.pi)
+                kk = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+                rot = np.eye(3) * np.cos(ang) + np.sin(ang) * kk + (1 - np.cos(ang)) * np.outer(a, a)
+                m = np.eye(4)
+                m[:3, :3] = rot * rng.uniform(0.3, 1.0)
+                m[:3, 3] = rng.uniform(-7.0, 7.0, 3)
+                out_m.append(m.astype(np.float32))
+            return out_m
+
+        vt, ft = W.torus(256, 128, W.SEED_BASE + 5006)
+        vs, fs = W.perturbed_sphere(32, W.SEED_BASE + 5007)
+        s = F.Scene3D()
+        s.set_object_count(3)
+        for k, (v, f) in enumerate([(vt, ft), (vs, fs), (vs, fs)]):
+            s.set_object_vertices(v, k)
+            s.set_object_triangles(f, k)
+        s.set_object_instance_transforms(affines(64), 0)
+        s.set_object_instance_transforms(affines(64), 1)
+        s.build(F.AggregateType.Bvh_SurfaceArea, False)
+        n = N_QUERIES
+        pts = W.uniform_points(n, 3, -8.0, 8.0, W.SEED_BASE + 5008)
+        sph = sph_tensor(pts)
+        out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+        inst_out = torch.empty(n, dtype=torch.int32, device=dev)
+        g = F.GPUScene3D("", False, device=0)
+        g.transfer_to_gpu(s)
+
+        def inst_run():
+            check(L.fcpwgb_find_closest_points_instanced_device(g.handle, sph.data_ptr(), out.data_ptr(),
+                                                                inst_out.data_ptr(), n, 0, sp))
+
+        table = {}
+        for bits in (32, 16, 8):
+            g.set_traversal(4, bits, sort_queries=True)
+            table[bits] = timed(inst_run)
+        best_bits = min(table, key=table.get)
+        inst = s.instances
+        top_nodes, top_refs, mats = inst.export()
+        objs = [o.export()[:2] for o in inst.objects]
+        cpu = cpu_rate(lambda m: O.instanced_closest_points(3, top_nodes, top_refs, mats, inst.instance_objects,
+                                                            inst.transformed, objs,
+                                                            R.make_spheres(pts[:m], R.FLT_MAX), nthreads=threads),
+                       n)
+        world_tris = 64 * len(ft) + 65 * len(fs)
+        lines.append({"config": f"instanced: 129 instances of 3 objects ({world_tris:,} triangles in world space), "
+                                f"{n:,} closest-point queries", "queries": n, "instances": len(inst),
+                      "gpu": {"queries_per_s": n / (table[best_bits] / 1e3), "ms": table[best_bits],
+                              "variant": {"branching": 4, "bits": best_bits, "sort_queries": True}},
+                      "ms_by_bits": {str(b): round(t, 3) for b, t in table.items()}, "cpu_baseline": cpu})
+        del g, s
+
+    # scene setup on the 1M-triangle torus: the host SAH build (the reference's algorithm) and its
+    # transfer against the GPU build with its transfer
+    if want("build"):
+        v, f, _ = make_workload(0, 1)
+        t0 = time.perf_counter()
+        s, _ = build_scene(v, f)
+        t_host = time.perf_counter() - t0
+        g = F.GPUScene3D("", False, device=0)
+        t0 = time.perf_counter()
+        g.transfer_to_gpu(s)
+        torch.cuda.synchronize()
+        t_transfer = time.perf_counter() - t0
+        vd, fd = torch.from_numpy(v).to(dev), torch.from_numpy(f).to(dev)
+        gb = F.GPUScene3D("", False, device=0)
+        gb.build_on_gpu(vd, fd)
+        runs = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            gb.build_on_gpu(vd, fd)
+            torch.cuda.synchronize()
+            runs.append(time.perf_counter() - t0)
+        lines.append({"config": f"scene setup, torus {len(f):,} triangles", "host_sah_build_s": t_host,
+                      "host_transfer_s": t_transfer, "gpu_build_and_transfer_s": min(runs),
+                      "speedup": (t_host + t_transfer) / min(runs), "host_tree_nodes": g.info()["n_nodes"],
+                      "gpu_tree_nodes": gb.info()["n_nodes"]})
+        del g, gb, s
 
     for line in lines:
         print(json.dumps(line), flush=True)

@@ -199,8 +199,20 @@ def _instanced_args(top_nodes, top_refs, mats, inst_object, inst_transformed, ob
             np.ascontiguousarray(inst_transformed, np.uint32), np_, pp_)
 
 
+def _chunked(n, nthreads, call):
+    """Runs call(begin, end) over nthreads slices of [0, n) (the C calls release the GIL)."""
+    k = max(1, min(threads(nthreads), n // 1024 or 1))
+    bounds = [(n * t // k, n * (t + 1) // k) for t in range(k)]
+    if k == 1:
+        call(0, n)
+        return
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(k) as ex:
+        list(ex.map(lambda b: call(*b), bounds))
+
+
 def instanced_closest_points(dim, top_nodes, top_refs, mats, inst_object, inst_transformed, objects, spheres,
-                             record_normals=False):
+                             record_normals=False, nthreads=None):
     """Closest points on a scene of several objects / instances (the
     reference's top-level walk with TransformedAggregate leaves). objects:
     per object (nodes, primitives) in the interop layouts; mats: (n, 24) as
@@ -211,14 +223,20 @@ def instanced_closest_points(dim, top_nodes, top_refs, mats, inst_object, inst_t
     out = R.default_interactions(len(spheres))
     inst = np.zeros(len(spheres), np.uint32)
     sp = np.ascontiguousarray(spheres)
-    _load().oracle_instanced_closest_points(dim, _p(tn), _p(tr), len(io), _p(m), _p(io), _p(it),
-                                            C.cast(np_, C.c_void_p), C.cast(pp_, C.c_void_p), _p(sp), len(sp),
-                                            int(record_normals), _p(out), _p(inst))
+
+    def call(b, e):
+        _load().oracle_instanced_closest_points(dim, _p(tn), _p(tr), len(io), _p(m), _p(io), _p(it),
+                                                C.cast(np_, C.c_void_p), C.cast(pp_, C.c_void_p),
+                                                sp.ctypes.data + b * sp.itemsize, e - b, int(record_normals),
+                                                out.ctypes.data + b * out.itemsize, inst.ctypes.data + 4 * b)
+
+    _chunked(len(sp), nthreads, call)
     del keep
     return out, inst
 
 
-def instanced_rays(dim, top_nodes, top_refs, mats, inst_object, inst_transformed, objects, rays, occlusion=False):
+def instanced_rays(dim, top_nodes, top_refs, mats, inst_object, inst_transformed, objects, rays, occlusion=False,
+                   nthreads=None):
     """Ray queries on a scene of several objects / instances. Returns
     (interactions, hit, instance)."""
     R = _records()
@@ -228,9 +246,14 @@ def instanced_rays(dim, top_nodes, top_refs, mats, inst_object, inst_transformed
     hit = np.zeros(len(rays), np.int32)
     inst = np.zeros(len(rays), np.uint32)
     rr = np.ascontiguousarray(rays)
-    _load().oracle_instanced_rays(dim, _p(tn), _p(tr), len(io), _p(m), _p(io), _p(it), C.cast(np_, C.c_void_p),
-                                  C.cast(pp_, C.c_void_p), _p(rr), len(rr), int(occlusion), _p(out), _p(hit),
-                                  _p(inst))
+
+    def call(b, e):
+        _load().oracle_instanced_rays(dim, _p(tn), _p(tr), len(io), _p(m), _p(io), _p(it), C.cast(np_, C.c_void_p),
+                                      C.cast(pp_, C.c_void_p), rr.ctypes.data + b * rr.itemsize, e - b,
+                                      int(occlusion), out.ctypes.data + b * out.itemsize, hit.ctypes.data + 4 * b,
+                                      inst.ctypes.data + 4 * b)
+
+    _chunked(len(rr), nthreads, call)
     del keep
     return out, hit.astype(bool), inst
 
