@@ -33,6 +33,8 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_transfer": (c_int, [P, c_int, P, c_uint32, P, c_uint32, P, c_uint32, P, c_uint32]),
     "fcpwgb_gpu_scene_transfer_cpu_bvh": (c_int, [P, P]),
     "fcpwgb_gpu_scene_build": (c_int, [P, P, c_uint32, P, c_uint32, c_uint32]),
+    "fcpwgb_gpu_scene_build_sah": (c_int, [P, P, c_uint32, P, c_uint32, c_int]),
+    "fcpwgb_gpu_scene_build_sah_device": (c_int, [P, P, c_uint32, P, c_uint32, c_int, P]),
     "fcpwgb_cpu_instances_build": (c_int, [c_int, c_int, P, c_uint32, P, P, P, c_uint32, P]),
     "fcpwgb_cpu_instances_destroy": (None, [P]),
     "fcpwgb_cpu_instances_export": (c_int, [P, P, P, P, P]),

@@ -443,12 +443,15 @@ extern "C" int fcpwgb_gpu_scene_transfer_cpu_bvh(fcpwgb_gpu_scene *s, const fcpw
 // Builds the tree on the device (k_build.cu), reads the interop arrays back
 // and hands them to the validating transfer, so the scene is set up exactly
 // as for a host-built tree.
+// sahHeuristic >= 0: the reference's binned SAH build with that heuristic
+// (k_sah_build.cu) instead of the linear BVH
 static int gpuBuild(fcpwgb_gpu_scene *s, const float *positions, uint32_t nVertices, const int32_t *indices,
-                    uint32_t nPrims, uint32_t maxLeaf, cudaStream_t st) {
+                    uint32_t nPrims, uint32_t maxLeaf, cudaStream_t st, int sahHeuristic = -1) {
     const int dim = s->dim;
     if (!positions || !indices || nPrims == 0 || nVertices == 0)
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "non-empty positions and indices are required");
-    if (maxLeaf == 0 || maxLeaf > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "max_leaf_size must be 1..15");
+    if (sahHeuristic < 0 && (maxLeaf == 0 || maxLeaf > 15))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "max_leaf_size must be 1..15");
     if (nPrims >= (1u << 27)) return setError(FCPWGB_ERR_UNSUPPORTED, "too many primitives for the GPU build");
     const size_t recBytes = dim == 3 ? sizeof(fcpwgb_triangle) : sizeof(fcpwgb_line_segment);
     DeviceBuffer scratch, nodes, prims, verts, counters;
@@ -465,6 +468,24 @@ static int gpuBuild(fcpwgb_gpu_scene *s, const float *positions, uint32_t nVerti
     FCPWGB_CUDA(cudaStreamSynchronize(st));
     if (host[8]) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "vertex index out of range");
     FCPWGB_CUDA(cudaMemsetAsync(cnt + 9, 0, sizeof(uint32_t), st));
+    if (sahHeuristic >= 0) {
+        DeviceBuffer sNodes, sPrims, sVerts;
+        uint32_t nNodes = 0;
+        if ((rc = buildSahTree(dim, sahHeuristic, positions, indices, nPrims, cnt + 9, st, sNodes, sPrims, sVerts,
+                               nNodes)))
+            return rc;
+        FCPWGB_CUDA(cudaMemcpyAsync(host, cnt, 16 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        FCPWGB_CUDA(cudaStreamSynchronize(st));
+        if (host[9]) return setError(FCPWGB_ERR_TRAVERSAL, "GPU build: a subtree stack overflowed");
+        std::vector<unsigned char> hN((size_t)nNodes * sizeof(fcpwgb_bvh_node)), hP((size_t)nPrims * recBytes);
+        std::vector<int32_t> hV((size_t)nPrims * dim);
+        FCPWGB_CUDA(cudaMemcpyAsync(hN.data(), sNodes.ptr, hN.size(), cudaMemcpyDeviceToHost, st));
+        FCPWGB_CUDA(cudaMemcpyAsync(hP.data(), sPrims.ptr, hP.size(), cudaMemcpyDeviceToHost, st));
+        FCPWGB_CUDA(cudaMemcpyAsync(hV.data(), sVerts.ptr, hV.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        FCPWGB_CUDA(cudaStreamSynchronize(st));
+        return fcpwgb_gpu_scene_transfer(s, dim == 3 ? FCPWGB_TRIANGLE_BVH : FCPWGB_LINE_SEGMENT_BVH, hN.data(),
+                                         nNodes, hP.data(), nPrims, nullptr, 0, hV.data(), nVertices);
+    }
     FCPWGB_CUDA(launchBuildLbvh(positions, indices, dim, nPrims, maxLeaf, (uint32_t *)scratch.ptr,
                                 (unsigned char *)nodes.ptr, (unsigned char *)prims.ptr, (int32_t *)verts.ptr, cnt,
                                 cnt + 9, s->smCount(), st));
@@ -492,6 +513,48 @@ extern "C" int fcpwgb_gpu_scene_build_device(fcpwgb_gpu_scene *s, const float *p
     int rc = s->activate();
     if (rc) return rc;
     return gpuBuild(s, positions, n_vertices, indices, n_primitives, max_leaf_size, s->pick(stream));
+}
+
+static int sahHeuristicOf(int aggregateType) {
+    switch (aggregateType) {
+        case FCPWGB_AGGREGATE_BVH_LONGEST_AXIS: return 0;
+        case FCPWGB_AGGREGATE_BVH_SURFACE_AREA: return 1;
+        case FCPWGB_AGGREGATE_BVH_OVERLAP_SURFACE: return 2;
+        case FCPWGB_AGGREGATE_BVH_VOLUME: return 3;
+        case FCPWGB_AGGREGATE_BVH_OVERLAP_VOLUME: return 4;
+        default: return -1;
+    }
+}
+
+extern "C" int fcpwgb_gpu_scene_build_sah_device(fcpwgb_gpu_scene *s, const float *positions, uint32_t n_vertices,
+                                                 const int32_t *indices, uint32_t n_primitives, int aggregate_type,
+                                                 void *stream) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    int h = sahHeuristicOf(aggregate_type);
+    if (h < 0) return setError(FCPWGB_ERR_UNSUPPORTED, "the SAH build needs a BVH aggregate type (Bvh_*)");
+    int rc = s->activate();
+    if (rc) return rc;
+    return gpuBuild(s, positions, n_vertices, indices, n_primitives, 4, s->pick(stream), h);
+}
+
+extern "C" int fcpwgb_gpu_scene_build_sah(fcpwgb_gpu_scene *s, const float *positions, uint32_t n_vertices,
+                                          const int32_t *indices, uint32_t n_primitives, int aggregate_type) {
+    if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
+    int h = sahHeuristicOf(aggregate_type);
+    if (h < 0) return setError(FCPWGB_ERR_UNSUPPORTED, "the SAH build needs a BVH aggregate type (Bvh_*)");
+    int rc = s->activate();
+    if (rc) return rc;
+    if (!positions || !indices || n_primitives == 0 || n_vertices == 0)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "non-empty positions and indices are required");
+    for (uint64_t k = 0; k < (uint64_t)n_primitives * s->dim; k++)
+        if (indices[k] < 0 || (uint32_t)indices[k] >= n_vertices)
+            return setError(FCPWGB_ERR_INVALID_ARGUMENT, "vertex index out of range");
+    DeviceBuffer pos, idx;
+    if ((rc = pos.upload(positions, (size_t)n_vertices * s->dim * sizeof(float), s->stream))) return rc;
+    if ((rc = idx.upload(indices, (size_t)n_primitives * s->dim * sizeof(int32_t), s->stream))) return rc;
+    rc = gpuBuild(s, (const float *)pos.ptr, n_vertices, (const int32_t *)idx.ptr, n_primitives, 4, s->stream, h);
+    cudaStreamSynchronize(s->stream);
+    return rc;
 }
 
 extern "C" int fcpwgb_gpu_scene_build(fcpwgb_gpu_scene *s, const float *positions, uint32_t n_vertices,

@@ -120,6 +120,13 @@ cudaError_t launchSortBatchQueries(int dim, const BatchSceneGrid *grids, const u
                                    uint32_t *tileSums, DevSphere *sorted, uint32_t *perm, uint32_t *roots,
                                    cudaStream_t s);
 
+// the reference's binned SAH tree built on the device (k_sah_build.cu); heuristic
+// 0..4 = longest axis, surface area, overlap surface area, volume, overlap volume
+struct DeviceBuffer;
+int buildSahTree(int dim, int heuristic, const float *positions, const int32_t *indices, uint32_t n,
+                 uint32_t *errorWord, cudaStream_t st, DeviceBuffer &nodesOut, DeviceBuffer &primsOut,
+                 DeviceBuffer &vertsOut, uint32_t &nNodes);
+
 // GPU BVH construction (k_build.cu)
 size_t lbvhScratchWords(uint32_t n);
 cudaError_t launchCheckIndices(const int32_t *indices, size_t nIdx, uint32_t nVertices, uint32_t *bad, int numSMs,

@@ -258,12 +258,18 @@ class _GPUScene:
         self._n_nodes = info["n_nodes"]
         self._snch = info["bvh_type"] in (R.LINE_SEGMENT_SNCH, R.TRIANGLE_SNCH)
 
-    def build_on_gpu(self, positions, indices, max_leaf_size: int = 4) -> None:
-        """Builds the tree on the device and sets the scene up from it
-        (fcpwgb_gpu_scene_build): positions (V, DIM) float32, indices (P, DIM)
-        int32, as numpy arrays or contiguous CUDA tensors (built on the current
-        torch stream). A linear BVH: distances agree with the host SAH build,
-        the primitive chosen on an exact tie may differ. No silhouettes."""
+    def build_on_gpu(self, positions, indices, max_leaf_size: int = 4, method: str = "lbvh",
+                     aggregate_type: int = 3) -> None:
+        """Builds the tree on the device and sets the scene up from it:
+        positions (V, DIM) float32, indices (P, DIM) int32, as numpy arrays or
+        contiguous CUDA tensors (built on the current torch stream). method
+        "lbvh" (fcpwgb_gpu_scene_build): a linear BVH, distances agree with
+        the host SAH build, the primitive chosen on an exact tie may differ;
+        "sah" (fcpwgb_gpu_scene_build_sah): the reference's binned SAH tree
+        for aggregate_type (a Bvh_* AggregateType), node for node the tree
+        Scene.build makes. No silhouettes."""
+        if method not in ("lbvh", "sah"):
+            raise ValueError("method must be 'lbvh' or 'sah'")
         try:
             import torch
             on_device = isinstance(positions, torch.Tensor) and positions.is_cuda
@@ -277,16 +283,26 @@ class _GPUScene:
                     or indices.shape[1] != self.DIM:
                 raise ValueError(f"positions and indices must have {self.DIM} columns")
             stream = torch.cuda.current_stream(positions.device).cuda_stream
-            check(lib().fcpwgb_gpu_scene_build_device(self._h, positions.data_ptr(), positions.shape[0],
-                                                      indices.data_ptr(), indices.shape[0], int(max_leaf_size),
-                                                      C.c_void_p(stream)))
+            if method == "sah":
+                check(lib().fcpwgb_gpu_scene_build_sah_device(self._h, positions.data_ptr(), positions.shape[0],
+                                                              indices.data_ptr(), indices.shape[0],
+                                                              int(aggregate_type), C.c_void_p(stream)))
+            else:
+                check(lib().fcpwgb_gpu_scene_build_device(self._h, positions.data_ptr(), positions.shape[0],
+                                                          indices.data_ptr(), indices.shape[0], int(max_leaf_size),
+                                                          C.c_void_p(stream)))
             n_vertices = positions.shape[0]
         else:
             pos = np.ascontiguousarray(positions, np.float32)
             idx = np.ascontiguousarray(indices, np.int32)
             if pos.ndim != 2 or pos.shape[1] != self.DIM or idx.ndim != 2 or idx.shape[1] != self.DIM:
                 raise ValueError(f"positions and indices must have {self.DIM} columns")
-            check(lib().fcpwgb_gpu_scene_build(self._h, ptr(pos), len(pos), ptr(idx), len(idx), int(max_leaf_size)))
+            if method == "sah":
+                check(lib().fcpwgb_gpu_scene_build_sah(self._h, ptr(pos), len(pos), ptr(idx), len(idx),
+                                                       int(aggregate_type)))
+            else:
+                check(lib().fcpwgb_gpu_scene_build(self._h, ptr(pos), len(pos), ptr(idx), len(idx),
+                                                   int(max_leaf_size)))
             n_vertices = len(pos)
         self._cpu_bvh = None
         self._n_vertices = int(n_vertices)

@@ -149,3 +149,47 @@ def test_bad_input_is_refused():
     # the scene stays usable after a refused build
     g.build_on_gpu(v, f)
     assert g.info()["n_primitives"] == len(f)
+
+
+# ------------------------------------------------------------- the reference's SAH tree on the device
+@pytest.mark.parametrize("dim,aggregate,size", [(3, 3, "large"), (3, 3, "small"), (3, 2, "large"), (3, 5, "large"),
+                                                (3, 1, "large"), (3, 4, "large"), (2, 3, "large")])
+def test_device_sah_tree_equals_host_build(dim, aggregate, size):
+    """fcpwgb_gpu_scene_build_sah builds the host builder's tree (which is the
+    reference's, tests/test_golden_cpu.py) byte for byte: nodes and the
+    primitive order, for every heuristic, with large nodes split level by
+    level on the whole GPU and small subtrees by one thread each."""
+    from helpers import build_scene
+    if dim == 3:
+        v, f = (W.torus(192, 96, W.SEED_BASE + 120) if size == "large" else W.torus(12, 8, W.SEED_BASE + 121))
+    else:
+        v, f = W.star_polylines(48, 128, W.SEED_BASE + 122)
+    s = build_scene(dim, v, f, aggregate=aggregate)
+    nodes, prims, _ = s.cpu_bvh.export()
+    g = _scene(dim)
+    g.build_on_gpu(v, f, method="sah", aggregate_type=aggregate)
+    got = g.export_nodes()
+    assert len(got) == len(nodes)
+    diff = np.nonzero((got.view(np.uint8).reshape(len(got), -1) != nodes.view(np.uint8).reshape(len(nodes), -1))
+                      .any(1))[0]
+    assert len(diff) == 0, f"{len(diff)} nodes differ, first {diff[:3]}: {got[diff[:1]]} vs {nodes[diff[:1]]}"
+    lo, hi = (-2.0, 2.0) if dim == 3 else (-3.0, 3.0)
+    pts = W.uniform_points(20000, dim, lo, hi, 123)
+    g.set_traversal(0)
+    host = _scene(dim)
+    host.transfer_to_gpu(s)
+    host.set_traversal(0)
+    assert _run(g, pts).tobytes() == _run(host, pts).tobytes()
+
+
+def test_device_sah_tree_edge_cases():
+    from helpers import build_scene
+    v, f = W.torus(8, 4, W.SEED_BASE + 124)
+    for sub in (f[:1], f[:5], np.repeat(f[:2], 900, axis=0), np.concatenate([f] * 20)):
+        s = build_scene(3, v, sub)
+        nodes, _, _ = s.cpu_bvh.export()
+        g = F.GPUScene3D()
+        g.build_on_gpu(v, sub, method="sah")
+        assert g.export_nodes().tobytes() == nodes.tobytes(), f"{len(sub)} primitives"
+    with pytest.raises(F.FcpwError):
+        g.build_on_gpu(v, f, method="sah", aggregate_type=0)       # Baseline has no tree
