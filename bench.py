@@ -533,20 +533,29 @@ def run_suite(args):
         torch.cuda.synchronize()
         t_transfer = time.perf_counter() - t0
         vd, fd = torch.from_numpy(v).to(dev), torch.from_numpy(f).to(dev)
-        gb = F.GPUScene3D("", False, device=0)
-        gb.build_on_gpu(vd, fd)
-        runs = []
-        for _ in range(3):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            gb.build_on_gpu(vd, fd)
-            torch.cuda.synchronize()
-            runs.append(time.perf_counter() - t0)
+
+        def gpu_build(method):
+            gb = F.GPUScene3D("", False, device=0)
+            gb.build_on_gpu(vd, fd, method=method)
+            runs = []
+            for _ in range(3):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                gb.build_on_gpu(vd, fd, method=method)
+                torch.cuda.synchronize()
+                runs.append(time.perf_counter() - t0)
+            return gb, min(runs)
+
+        gl, t_lbvh = gpu_build("lbvh")
+        gs, t_sah = gpu_build("sah")
+        same = bool(np.array_equal(gs.export_nodes().view(np.uint8), g.export_nodes().view(np.uint8)))
         lines.append({"config": f"scene setup, torus {len(f):,} triangles", "host_sah_build_s": t_host,
-                      "host_transfer_s": t_transfer, "gpu_build_and_transfer_s": min(runs),
-                      "speedup": (t_host + t_transfer) / min(runs), "host_tree_nodes": g.info()["n_nodes"],
-                      "gpu_tree_nodes": gb.info()["n_nodes"]})
-        del g, gb, s
+                      "host_transfer_s": t_transfer,
+                      "gpu_sah_build_and_transfer_s": t_sah, "gpu_sah_tree_equals_host": same,
+                      "speedup_sah": (t_host + t_transfer) / t_sah,
+                      "gpu_lbvh_build_and_transfer_s": t_lbvh, "speedup_lbvh": (t_host + t_transfer) / t_lbvh,
+                      "host_tree_nodes": g.info()["n_nodes"], "lbvh_tree_nodes": gl.info()["n_nodes"]})
+        del g, gl, gs, s
 
     for line in lines:
         print(json.dumps(line), flush=True)

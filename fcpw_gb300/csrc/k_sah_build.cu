@@ -35,7 +35,7 @@ namespace {
 constexpr int kNB = 8;                // buckets (bvh.h:77 default)
 constexpr int kLeafRefs = 4;          // leaf size (fcpw.inl:813)
 constexpr uint32_t kCutDepth = 62;    // FCPW_BVH_MAX_DEPTH - 2 (bvh.inl:170)
-constexpr uint32_t kSmall = 512;      // subtrees of at most this many references: one thread each
+constexpr uint32_t kSmall = 64;       // subtrees of at most this many references: one thread each
 constexpr uint32_t kChunk = 2048;     // references per block in the level passes
 constexpr uint32_t kLB = 256;         // threads per block in the level passes
 constexpr int kSeqStack = 130;

@@ -251,6 +251,17 @@ int fcpwgb_intersect_rays_instanced_device(fcpwgb_gpu_scene *scene, const fcpwgb
  * is ready. */
 int fcpwgb_gpu_scene_build(fcpwgb_gpu_scene *scene, const float *positions, uint32_t n_vertices,
                            const int32_t *indices, uint32_t n_primitives, uint32_t max_leaf_size);
+/* Scene::build(aggregate_type, vectorize=false) + transferToGPU (fcpw.h:95,
+ * fcpw_gpu.h:21) with the reference's binned SAH build (bvh.inl:1-234: 8
+ * buckets, leaf <= 4, depth cut at 62; aggregate_type one of the Bvh_* types)
+ * run on the device: the tree and the primitive order equal the host build's
+ * (fcpwgb_cpu_bvh_build, and so the reference's) byte for byte. BVH only, no
+ * silhouettes. Same arrays, streams and return as fcpwgb_gpu_scene_build. */
+int fcpwgb_gpu_scene_build_sah(fcpwgb_gpu_scene *scene, const float *positions, uint32_t n_vertices,
+                               const int32_t *indices, uint32_t n_primitives, int aggregate_type);
+int fcpwgb_gpu_scene_build_sah_device(fcpwgb_gpu_scene *scene, const float *positions, uint32_t n_vertices,
+                                      const int32_t *indices, uint32_t n_primitives, int aggregate_type,
+                                      void *stream);
 int fcpwgb_gpu_scene_build_device(fcpwgb_gpu_scene *scene, const float *positions, uint32_t n_vertices,
                                   const int32_t *indices, uint32_t n_primitives, uint32_t max_leaf_size,
                                   void *stream);
