@@ -31,9 +31,9 @@ __global__ void __launch_bounds__(kCheckThreads) kBruteF64(const unsigned char *
             w.pb = t.pb;
             w.pc = t.pc;
             w.index = t.index;
-            d = w.refine(c, p);
+            d = w.refine64(c, p);
         } else {
-            d = Seg24Prim::load(prims, k).refine(c, p);
+            d = Seg24Prim::load(prims, k).refine64(c, p);
         }
         best = fmin(best, d);
     }

@@ -5,10 +5,18 @@
 
 #include <type_traits>
 
+#include "ds_float.cuh"
 #include "kernels.h"
 #include "wide_common.cuh"
 
 namespace fcpwgb {
+
+// Bounds of the double-single refinement (refine below): conditioning limit
+// (2^-46 x 2^10 = 2^-36 relative error at most, far below the 1e-6 that the
+// precise mode promises) and the ranges of the offset scale, the edges and
+// the normal within which squares and products of pairs stay normal floats.
+constexpr float kDsCond = 1024.0f;
+constexpr float kDsMinScale = 0x1p-28f, kDsMaxScale = 0x1p28f, kDsMinEdge = 0x1p-30f, kDsMinNormal = 0x1p-40f;
 
 // 48 B triangle record of the wide kernels: (pa, index), (pb, 0), (pc, 0)
 struct Tri48Prim {
@@ -33,7 +41,7 @@ struct Tri48Prim {
     }
     // FP64 distance and closest point, vertices taken relative to the query
     // (not inlined: its FP64 registers stay out of the traversal loop)
-    __device__ __noinline__ double refine(float3 x, float3 &pOut) const {
+    __device__ __noinline__ double refine64(float3 x, float3 &pOut) const {
         double ax = (double)pa.x - x.x, ay = (double)pa.y - x.y, az = (double)pa.z - x.z;
         double bx = (double)pb.x - x.x, by = (double)pb.y - x.y, bz = (double)pb.z - x.z;
         double cx = (double)pc.x - x.x, cy = (double)pc.y - x.y, cz = (double)pc.z - x.z;
@@ -65,6 +73,68 @@ struct Tri48Prim {
         pOut = make_float3((float)(x.x + px), (float)(x.y + py), (float)(x.z + pz));
         return sqrt(px * px + py * py + pz * pz);
     }
+    // The same distance and closest point in double-single arithmetic
+    // (ds_float.cuh), which runs on the FP32 pipes. The vertex offsets
+    // from the query and the edges are exact pairs (TwoSum), so the error
+    // grows only with the conditioning of the projection,
+    // cond = s |ab| |ac| / (|n| d), s the largest vertex offset, n the
+    // face normal and d the FP32 distance found by the traversal: about
+    // 2^-46 cond relative. Where the FP32 estimate of cond is above
+    // kDsCond, or s, an edge or |n| lies outside the range where pair
+    // products stay normal floats, refine64 computes it in FP64 instead.
+    __device__ __noinline__ DS refine(float3 x, float dApprox, float3 &pOut) const {
+        const float3 eab = pb - pa, eac = pc - pa, ebc = pc - pb;
+        const float s = fmaxf(fmaxf(fmaxf(fabsf(pa.x - x.x), fabsf(pa.y - x.y)), fmaxf(fabsf(pa.z - x.z),
+                                    fabsf(pb.x - x.x))),
+                              fmaxf(fmaxf(fabsf(pb.y - x.y), fabsf(pb.z - x.z)),
+                                    fmaxf(fmaxf(fabsf(pc.x - x.x), fabsf(pc.y - x.y)), fabsf(pc.z - x.z))));
+        const float lab = len3(eab), lac = len3(eac), ln = len3(cross3(eab, eac));
+        const bool ok = s >= kDsMinScale && s <= kDsMaxScale && fminf(fminf(lab, lac), len3(ebc)) >= kDsMinEdge &&
+                        ln >= kDsMinNormal && s * lab * lac <= kDsCond * ln * dApprox;
+        if (!ok) return dsFromDouble(refine64(x, pOut));
+        const DS ax = twoSum(pa.x, -x.x), ay = twoSum(pa.y, -x.y), az = twoSum(pa.z, -x.z);
+        const DS bx = twoSum(pb.x, -x.x), by = twoSum(pb.y, -x.y), bz = twoSum(pb.z, -x.z);
+        const DS cx = twoSum(pc.x, -x.x), cy = twoSum(pc.y, -x.y), cz = twoSum(pc.z, -x.z);
+        const DS abx = twoSum(pb.x, -pa.x), aby = twoSum(pb.y, -pa.y), abz = twoSum(pb.z, -pa.z);
+        const DS acx = twoSum(pc.x, -pa.x), acy = twoSum(pc.y, -pa.y), acz = twoSum(pc.z, -pa.z);
+        const DS d1 = dsNeg(dsDot3(abx, aby, abz, ax, ay, az)), d2 = dsNeg(dsDot3(acx, acy, acz, ax, ay, az));
+        const DS d3 = dsNeg(dsDot3(abx, aby, abz, bx, by, bz)), d4 = dsNeg(dsDot3(acx, acy, acz, bx, by, bz));
+        const DS d5 = dsNeg(dsDot3(abx, aby, abz, cx, cy, cz)), d6 = dsNeg(dsDot3(acx, acy, acz, cx, cy, cz));
+        DS px, py, pz;
+        if (d1.hi <= 0.0f && d2.hi <= 0.0f) {
+            px = ax; py = ay; pz = az;
+        } else if (d3.hi >= 0.0f && dsSub(d4, d3).hi <= 0.0f) {
+            px = bx; py = by; pz = bz;
+        } else if (d6.hi >= 0.0f && dsSub(d5, d6).hi <= 0.0f) {
+            px = cx; py = cy; pz = cz;
+        } else {
+            const DS vc = dsSub(dsMul(d1, d4), dsMul(d3, d2));
+            const DS vb = dsSub(dsMul(d5, d2), dsMul(d1, d6));
+            const DS va = dsSub(dsMul(d3, d6), dsMul(d5, d4));
+            const DS e43 = dsSub(d4, d3), e56 = dsSub(d5, d6);
+            if (vc.hi <= 0.0f && d1.hi >= 0.0f && d3.hi <= 0.0f) {
+                const DS v = dsDiv(d1, dsSub(d1, d3));
+                px = dsAdd(ax, dsMul(abx, v)); py = dsAdd(ay, dsMul(aby, v)); pz = dsAdd(az, dsMul(abz, v));
+            } else if (vb.hi <= 0.0f && d2.hi >= 0.0f && d6.hi <= 0.0f) {
+                const DS w = dsDiv(d2, dsSub(d2, d6));
+                px = dsAdd(ax, dsMul(acx, w)); py = dsAdd(ay, dsMul(acy, w)); pz = dsAdd(az, dsMul(acz, w));
+            } else if (va.hi <= 0.0f && e43.hi >= 0.0f && e56.hi >= 0.0f) {
+                const DS w = dsDiv(e43, dsAdd(e43, e56));
+                px = dsAdd(bx, dsMul(twoSum(pc.x, -pb.x), w));
+                py = dsAdd(by, dsMul(twoSum(pc.y, -pb.y), w));
+                pz = dsAdd(bz, dsMul(twoSum(pc.z, -pb.z), w));
+            } else {
+                // face region: project the query (the origin) onto the plane
+                const DS nx = dsSub(dsMul(aby, acz), dsMul(abz, acy));
+                const DS ny = dsSub(dsMul(abz, acx), dsMul(abx, acz));
+                const DS nz = dsSub(dsMul(abx, acy), dsMul(aby, acx));
+                const DS t = dsDiv(dsDot3(ax, ay, az, nx, ny, nz), dsDot3(nx, ny, nz, nx, ny, nz));
+                px = dsMul(nx, t); py = dsMul(ny, t); pz = dsMul(nz, t);
+            }
+        }
+        pOut = make_float3(dsAdd(dsOf(x.x), px).hi, dsAdd(dsOf(x.y), py).hi, dsAdd(dsOf(x.z), pz).hi);
+        return dsSqrt(dsDot3(px, py, pz, px, py, pz));
+    }
 };
 
 // 2D segments keep the 24 B record (SegPrim) and gain an FP64 refinement
@@ -75,7 +145,7 @@ struct Seg24Prim : SegPrim {
         s.pa = b.pa; s.pb = b.pb; s.index = b.index;
         return s;
     }
-    __device__ __noinline__ double refine(float3 x, float3 &pOut) const {
+    __device__ __noinline__ double refine64(float3 x, float3 &pOut) const {
         double ax = (double)pa.x - x.x, ay = (double)pa.y - x.y;
         double ux = (double)pb.x - pa.x, uy = (double)pb.y - pa.y;
         double c1 = -(ux * ax + uy * ay), c2 = ux * ux + uy * uy, px, py;
@@ -84,6 +154,28 @@ struct Seg24Prim : SegPrim {
         else { double t = c1 / c2; px = ax + ux * t; py = ay + uy * t; }
         pOut = make_float3((float)(x.x + px), (float)(x.y + py), 0.0f);
         return sqrt(px * px + py * py);
+    }
+    // double-single counterpart (see Tri48Prim::refine); a segment's
+    // projection has cond = s / d
+    __device__ __noinline__ DS refine(float3 x, float dApprox, float3 &pOut) const {
+        const float s = fmaxf(fmaxf(fabsf(pa.x - x.x), fabsf(pa.y - x.y)), fmaxf(fabsf(pb.x - x.x), fabsf(pb.y - x.y)));
+        const bool ok = s >= kDsMinScale && s <= kDsMaxScale && len3(pb - pa) >= kDsMinEdge &&
+                        s <= kDsCond * dApprox;
+        if (!ok) return dsFromDouble(refine64(x, pOut));
+        const DS ax = twoSum(pa.x, -x.x), ay = twoSum(pa.y, -x.y);
+        const DS ux = twoSum(pb.x, -pa.x), uy = twoSum(pb.y, -pa.y);
+        const DS c1 = dsNeg(dsAdd(dsMul(ux, ax), dsMul(uy, ay))), c2 = dsAdd(dsMul(ux, ux), dsMul(uy, uy));
+        DS px, py;
+        if (c1.hi <= 0.0f) {
+            px = ax; py = ay;
+        } else if (dsSub(c2, c1).hi <= 0.0f) {
+            px = dsAdd(ax, ux); py = dsAdd(ay, uy);
+        } else {
+            const DS t = dsDiv(c1, c2);
+            px = dsAdd(ax, dsMul(ux, t)); py = dsAdd(ay, dsMul(uy, t));
+        }
+        pOut = make_float3(dsAdd(dsOf(x.x), px).hi, dsAdd(dsOf(x.y), py).hi, 0.0f);
+        return dsSqrt(dsAdd(dsMul(px, px), dsMul(py, py)));
     }
 };
 
@@ -253,7 +345,8 @@ template<> struct Count<true> {
 // reference's rounding, but a primitive whose FP32 distance lies within the
 // band of the winner's may be the closer one in exact arithmetic. So the
 // precise mode also keeps the best primitive within the band other than the
-// winner (the runner-up) and refines both in FP64 at the end. Without it,
+// winner (the runner-up) and refines both at the end (Tri48Prim::refine:
+// double-single arithmetic, FP64 where ill-conditioned). Without it,
 // near-tied segments of a polyline gave 7.5e-7 relative error on 1024 2D
 // samples.
 constexpr float kBandEps = 8.0f * 5.9604645e-8f;
@@ -405,8 +498,9 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
     return found;
 }
 
-// Final record of query i: FP64 distance of the winning primitive (PRECISE;
-// with a runner-up within the rounding band, the closer of the two in FP64),
+// Final record of query i: the refined distance of the winning primitive
+// (PRECISE: double-single, FP64 where ill-conditioned; with a runner-up
+// within the rounding band, the closer of the two),
 // its face normal (recordNormal), written to the caller's slot.
 template<class Prim, bool PRECISE>
 FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_t *__restrict__ perm,
@@ -416,13 +510,13 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
         Prim prim = Prim::load(prims, selected);
         if constexpr (PRECISE) {
             float3 p;
-            double d = prim.refine(c, p);
+            DS d = prim.refine(c, best.d, p);
             if (tie.sel2nd != kUintMax && tie.d2nd <= best.d + tieBand(c, best.d) &&
                 tie.d2nd * tie.d2nd <= r2User) {
                 Prim q = Prim::load(prims, tie.sel2nd);
                 float3 p2;
-                double d2 = q.refine(c, p2);
-                if (d2 < d) {
+                DS d2 = q.refine(c, tie.d2nd, p2);
+                if (dsLess(d2, d)) {
                     float3 pt;
                     float2 uv;
                     q.closestPoint(c, pt, uv);
@@ -433,7 +527,7 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
                     prim = q;
                 }
             }
-            best.d = (float)d;
+            best.d = d.hi;
             best.p = p;
         }
         if (recordNormal) best.n = prim.normal();
