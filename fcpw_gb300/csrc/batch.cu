@@ -31,7 +31,7 @@ struct BatchScene {
 };
 
 struct GraphKey {
-    const void *spheres, *out, *nodes, *prims, *cells, *perm, *sorted, *roots, *grids, *offsets;
+    const void *spheres, *out, *nodes, *prims, *cells, *perm, *sorted, *roots, *grids, *offsets, *sel;
     uint32_t n, recordNormal, branching, bits, persistent, precise, sort, packet, leaf, shortStack;
     bool operator==(const GraphKey &o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
@@ -59,6 +59,7 @@ struct fcpwgb_gpu_batch {
     std::vector<BatchSceneGrid> grids;
     uint32_t nCells = 0;
     DeviceBuffer gridBuf, offsetBuf, cells, tileSums, perm, sorted, rootBuf, counter, errorWord;
+    DeviceBuffer refineSel;  // precise mode: winner and runner-up leaf positions per sorted query
     DeviceBuffer qIn, qOut;
 
     cudaGraphExec_t exec = nullptr;
@@ -198,6 +199,7 @@ int ensureLayout(fcpwgb_gpu_batch *b, const uint32_t *offsets, uint32_t nOffsets
     if ((rc = b->tileSums.ensure((size_t)batchScanTiles((uint32_t)cellBase) * sizeof(uint32_t) + 16))) return rc;
     if ((rc = b->perm.ensure((size_t)std::max(n, 1u) * sizeof(uint32_t)))) return rc;
     if ((rc = b->sorted.ensure((size_t)std::max(n, 1u) * sizeof(DevSphere)))) return rc;
+    if ((rc = b->refineSel.ensure((size_t)std::max(n, 1u) * sizeof(uint2)))) return rc;
     if ((rc = b->rootBuf.ensure((size_t)std::max(n, 1u) * sizeof(uint32_t)))) return rc;
     cudaError_t e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return cudaFail(e, "layout upload");
@@ -228,6 +230,7 @@ int enqueue(fcpwgb_gpu_batch *b, const DevSphere *spheres, DevInteraction *out, 
     l.spheres = (const DevSphere *)b->sorted.ptr;
     l.perm = (const uint32_t *)b->perm.ptr;
     l.roots = (const uint32_t *)b->rootBuf.ptr;
+    l.sel = (uint2 *)b->refineSel.ptr;
     uint32_t blocks = (n + 127) / 128;
     l.packet = b->cfg.packet;
     l.shortStack = b->cfg.shortStack;
@@ -261,7 +264,7 @@ int runDevice(fcpwgb_gpu_batch *b, const DevSphere *spheres, const uint32_t *off
     std::memset(&k, 0, sizeof(k));
     k.spheres = spheres; k.out = out; k.nodes = b->nodes.ptr; k.prims = b->prims.ptr; k.cells = b->cells.ptr;
     k.perm = b->perm.ptr; k.sorted = b->sorted.ptr; k.roots = b->rootBuf.ptr; k.grids = b->gridBuf.ptr;
-    k.offsets = b->offsetBuf.ptr; k.n = n; k.recordNormal = (uint32_t)recordNormal;
+    k.offsets = b->offsetBuf.ptr; k.sel = b->refineSel.ptr; k.n = n; k.recordNormal = (uint32_t)recordNormal;
     k.branching = (uint32_t)b->cfg.branching; k.bits = (uint32_t)b->cfg.bits;
     k.persistent = (uint32_t)b->cfg.persistent; k.precise = (uint32_t)b->cfg.precise;
     k.sort = (uint32_t)b->cfg.sortQueries;

@@ -82,7 +82,7 @@ struct Tri48Prim {
     // 2^-46 cond relative. Where the FP32 estimate of cond is above
     // kDsCond, or s, an edge or |n| lies outside the range where pair
     // products stay normal floats, refine64 computes it in FP64 instead.
-    __device__ __noinline__ DS refine(float3 x, float dApprox, float3 &pOut) const {
+    FCPWGB_D DS refine(float3 x, float dApprox, float3 &pOut) const {
         const float3 eab = pb - pa, eac = pc - pa, ebc = pc - pb;
         const float s = fmaxf(fmaxf(fmaxf(fabsf(pa.x - x.x), fabsf(pa.y - x.y)), fmaxf(fabsf(pa.z - x.z),
                                     fabsf(pb.x - x.x))),
@@ -157,7 +157,7 @@ struct Seg24Prim : SegPrim {
     }
     // double-single counterpart (see Tri48Prim::refine); a segment's
     // projection has cond = s / d
-    __device__ __noinline__ DS refine(float3 x, float dApprox, float3 &pOut) const {
+    FCPWGB_D DS refine(float3 x, float dApprox, float3 &pOut) const {
         const float s = fmaxf(fmaxf(fabsf(pa.x - x.x), fabsf(pa.y - x.y)), fmaxf(fabsf(pb.x - x.x), fabsf(pb.y - x.y)));
         const bool ok = s >= kDsMinScale && s <= kDsMaxScale && len3(pb - pa) >= kDsMinEdge &&
                         s <= kDsCond * dApprox;
@@ -498,38 +498,62 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
     return found;
 }
 
-// Final record of query i: the refined distance of the winning primitive
-// (PRECISE: double-single, FP64 where ill-conditioned; with a runner-up
-// within the rounding band, the closer of the two),
-// its face normal (recordNormal), written to the caller's slot.
+// Final step of query i. Without PRECISE: the FP32 record of the winner,
+// with its face normal (recordNormal), to the caller's slot. With PRECISE:
+// only the leaf positions of the winner and of the runner-up within the
+// rounding band and the caller's radius (kUintMax: none) to sel[i]; the
+// refinement pass (kRefineClosest) then writes the record. Keeping the
+// refinement out of the traversal kernels keeps its registers out of their
+// loops: inside them it cost 10-18% of the traversal time in spills.
 template<class Prim, bool PRECISE>
 FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_t *__restrict__ perm,
-                          DevInteraction *__restrict__ out, uint32_t i, float3 c, float r2User, bool found,
-                          uint32_t selected, int recordNormal, DevInteraction &best, const NearTie<PRECISE> &tie) {
-    if (found) {
-        Prim prim = Prim::load(prims, selected);
-        if constexpr (PRECISE) {
-            float3 p;
-            DS d = prim.refine(c, best.d, p);
-            if (tie.sel2nd != kUintMax && tie.d2nd <= best.d + tieBand(c, best.d) &&
-                tie.d2nd * tie.d2nd <= r2User) {
-                Prim q = Prim::load(prims, tie.sel2nd);
-                float3 p2;
-                DS d2 = q.refine(c, tie.d2nd, p2);
-                if (dsLess(d2, d)) {
-                    float3 pt;
-                    float2 uv;
-                    q.closestPoint(c, pt, uv);
-                    d = d2;
-                    p = p2;
-                    best.uv = uv;
-                    best.index = q.index;
-                    prim = q;
-                }
+                          DevInteraction *__restrict__ out, uint2 *__restrict__ sel, uint32_t i, float3 c,
+                          float r2User, bool found, uint32_t selected, int recordNormal, DevInteraction &best,
+                          const NearTie<PRECISE> &tie) {
+    if constexpr (PRECISE) {
+        const bool second = found && tie.sel2nd != kUintMax && tie.d2nd <= best.d + tieBand(c, best.d) &&
+                            tie.d2nd * tie.d2nd <= r2User;
+        sel[i] = make_uint2(found ? selected : kUintMax, second ? tie.sel2nd : kUintMax);
+    } else {
+        if (found && recordNormal) best.n = Prim::load(prims, selected).normal();
+        out[perm ? __ldg(perm + i) : i] = best;
+    }
+}
+
+// Record of sorted query i from the leaf positions of finishQuery<PRECISE>:
+// the FP32 closest point of the winner for uv, the refined distance and
+// point (Prim::refine), the runner-up's when it is closer after refinement,
+// and the face normal of the one kept (recordNormal); written to the
+// caller's slot. Without a winner, the default record.
+template<class Prim>
+FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphere *__restrict__ spheres,
+                          const uint32_t *__restrict__ perm, const uint2 *__restrict__ sel,
+                          DevInteraction *__restrict__ out, uint32_t i, int recordNormal) {
+    const uint2 s = __ldg(sel + i);
+    DevInteraction best = defaultInteraction();
+    if (s.x != kUintMax) {
+        const float4 s4 = ldg4(spheres + i);
+        const float3 c = make_float3(s4.x, s4.y, s4.z);
+        Prim prim = Prim::load(prims, s.x);
+        float3 pt, p;
+        float2 uv;
+        DS d = prim.refine(c, prim.closestPoint(c, pt, uv), p);
+        if (s.y != kUintMax) {
+            const Prim q = Prim::load(prims, s.y);
+            float3 pt2, p2;
+            float2 uv2;
+            const DS d2 = q.refine(c, q.closestPoint(c, pt2, uv2), p2);
+            if (dsLess(d2, d)) {
+                d = d2;
+                p = p2;
+                uv = uv2;
+                prim = q;
             }
-            best.d = d.hi;
-            best.p = p;
         }
+        best.p = p;
+        best.uv = uv;
+        best.d = d.hi;
+        best.index = prim.index;
         if (recordNormal) best.n = prim.normal();
     }
     out[perm ? __ldg(perm + i) : i] = best;
@@ -552,7 +576,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                                                                 const DevSphere *__restrict__ spheres,
                                                                 const uint32_t *__restrict__ perm,
                                                                 const uint32_t *__restrict__ roots,
-                                                                DevInteraction *__restrict__ out, uint32_t n,
+                                                                DevInteraction *__restrict__ out,
+                                                                uint2 *__restrict__ sel, uint32_t n,
                                                                 int recordNormal, uint32_t *counter,
                                                                 uint32_t *errorWord, unsigned long long *stats) {
     __shared__ uint32_t sRef[SHORT > 0 ? SHORT * kWideBlock : 1];
@@ -572,7 +597,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
             NearTie<PRECISE> tie;
             bool found = wideClosest<W, BITS, Prim, PRECISE, STATS, SHORT>(nodes, prims, root, c, s4.w, false, best, selected, tie,
                                                              st, errorWord, tExp, tTests);
-            finishQuery<Prim, PRECISE>(prims, perm, out, i, c, s4.w, found, selected, recordNormal, best, tie);
+            finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, s4.w, found, selected, recordNormal, best, tie);
         }
     } else {
         const uint32_t lane = threadIdx.x & 31u;
@@ -613,7 +638,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                                                             st, errorWord, tExp, tTests);
                 seed = found ? selected : kUintMax;
                 seedRoot = root;
-                finishQuery<Prim, PRECISE>(prims, perm, out, i, c, s4.w, found, selected, recordNormal, best, tie);
+                finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, s4.w, found, selected, recordNormal, best, tie);
             }
         }
     }
@@ -640,7 +665,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                                                                       const DevSphere *__restrict__ spheres,
                                                                       const uint32_t *__restrict__ perm,
                                                                       const uint32_t *__restrict__ roots,
-                                                                      DevInteraction *__restrict__ out, uint32_t n,
+                                                                      DevInteraction *__restrict__ out,
+                                                                      uint2 *__restrict__ sel, uint32_t n,
                                                                       int recordNormal, uint32_t *errorWord,
                                                                       unsigned long long *stats) {
     constexpr uint32_t kSlotMask = W - 1;
@@ -794,7 +820,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
             if (!next) break;
         }
     }
-    if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, i, c, r2User, found, selected, recordNormal, best, tie);
+    if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, r2User, found, selected, recordNormal, best, tie);
     if (STATS && stats) {
         if (lane == 0) {
             atomicAdd(stats + 3, tVisits.get());
@@ -956,33 +982,40 @@ cudaError_t launchWideClosestKernel(const WideLaunch &l, cudaStream_t s) {
     dim3 g(l.grid), b(kWideBlock);
     if (l.packet)
         kWidePacketClosestPoint<W, B, Prim, PRECISE, STATS><<<g, b, 0, s>>>(
-            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.errorWord, l.stats);
+            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.errorWord, l.stats);
     else if (l.counter) {
         if (l.shortStack)
             kWideClosestPoint<W, B, Prim, PRECISE, true, STATS, kShortStack><<<g, b, 0, s>>>(
-                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.counter, l.errorWord,
                 l.stats);
         else
             kWideClosestPoint<W, B, Prim, PRECISE, true, STATS, 0><<<g, b, 0, s>>>(
-                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.counter, l.errorWord,
                 l.stats);
     } else {
         if (l.shortStack)
             kWideClosestPoint<W, B, Prim, PRECISE, false, STATS, kShortStack><<<g, b, 0, s>>>(
-                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.counter, l.errorWord,
                 l.stats);
         else
             kWideClosestPoint<W, B, Prim, PRECISE, false, STATS, 0><<<g, b, 0, s>>>(
-                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.n, l.recordNormal, l.counter, l.errorWord,
+                l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.counter, l.errorWord,
                 l.stats);
     }
     return cudaGetLastError();
 }
+// Precise mode: the traversal writes leaf positions to l.sel, then the
+// refinement pass (launchRefineClosest) writes the records.
 template<int W, int B, class Prim>
 cudaError_t launchWideClosestPrim(bool precise, const WideLaunch &l, cudaStream_t s) {
-    if (precise)
-        return l.stats ? launchWideClosestKernel<W, B, Prim, true, true>(l, s)
-                       : launchWideClosestKernel<W, B, Prim, true, false>(l, s);
+    if (precise) {
+        if (!l.sel) return cudaErrorInvalidValue;
+        cudaError_t e = l.stats ? launchWideClosestKernel<W, B, Prim, true, true>(l, s)
+                                : launchWideClosestKernel<W, B, Prim, true, false>(l, s);
+        if (e != cudaSuccess) return e;
+        return launchRefineClosest(std::is_same<Prim, Tri48Prim>::value ? 3 : 2, l.prims, l.spheres, l.perm, l.sel,
+                                   l.out, l.n, l.recordNormal, s);
+    }
     return l.stats ? launchWideClosestKernel<W, B, Prim, false, true>(l, s)
                    : launchWideClosestKernel<W, B, Prim, false, false>(l, s);
 }

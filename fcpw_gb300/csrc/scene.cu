@@ -106,6 +106,10 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
         l.spheres = (const DevSphere *)sortSpheres.ptr;
         l.perm = (const uint32_t *)sortPerm.ptr;
     }
+    if (c.precise) {
+        if ((rc = refineSel.ensure((size_t)n * sizeof(uint2)))) return rc;
+        l.sel = (uint2 *)refineSel.ptr;
+    }
     uint32_t blocks = (n + 127) / 128;
     l.packet = c.packet;
     l.shortStack = c.shortStack;

@@ -76,8 +76,9 @@ struct GpuScene {
     WideConfig wideConfig;
     WideTree wide;
     DeviceBuffer wideNodes, wideChildBinary, widePrims;
-    // scratch of the fast path: query sort cells / permutation / sorted copy, work counter
-    DeviceBuffer sortCells, sortPerm, sortSpheres, sortRays, workCounter;
+    // scratch of the fast path: query sort cells / permutation / sorted copy, work counter,
+    // precise mode's winner and runner-up leaf positions
+    DeviceBuffer sortCells, sortPerm, sortSpheres, sortRays, workCounter, refineSel;
     int numSMs = 0;
 
     // optional event timing of traversal launches
