@@ -90,9 +90,6 @@ FCPWGB_D DS dsDot3(DS ax, DS ay, DS az, DS bx, DS by, DS bz) {
     return dsAdd(dsAdd(dsMul(ax, bx), dsMul(ay, by)), dsMul(az, bz));
 }
 
-// a < b for normalised pairs
-FCPWGB_D bool dsLess(DS a, DS b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
-
 // the pair nearest to an FP64 value
 FCPWGB_D DS dsFromDouble(double d) {
     float hi = (float)d;

@@ -16,6 +16,9 @@ namespace fcpwgb {
 // precise mode promises) and the ranges of the offset scale, the edges and
 // the normal within which squares and products of pairs stay normal floats.
 constexpr float kDsCond = 1024.0f;
+// relative margin by which a refined runner-up must beat the refined winner
+// (above the refinement's rounding, far below the 1e-6 accuracy promised)
+constexpr float kRefineTie = 0x1p-28f;
 constexpr float kDsMinScale = 0x1p-28f, kDsMaxScale = 0x1p28f, kDsMinEdge = 0x1p-30f, kDsMinNormal = 0x1p-40f;
 
 // 48 B triangle record of the wide kernels: (pa, index), (pb, 0), (pc, 0)
@@ -359,7 +362,7 @@ template<bool TRACK> struct NearTie {  // off: no runner-up state, the same visi
     FCPWGB_D float prune(float r2, float3 c) const { return bandRadius2(sqrtf(r2), c); }
     FCPWGB_D float pruneHit(float d, float3 c) const { return bandRadius2(d, c); }
     FCPWGB_D void replaced(float, uint32_t) {}
-    FCPWGB_D void offer(float, uint32_t) {}
+    FCPWGB_D void offer(float, uint32_t, uint32_t) {}
 };
 template<> struct NearTie<true> {  // two registers; the band is recomputed from the query when needed
     float d2nd = kFltMax;
@@ -372,9 +375,11 @@ template<> struct NearTie<true> {  // two registers; the band is recomputed from
         sel2nd = sel;
     }
     // a primitive that did not beat the winner (the caller's radius is checked
-    // at the end); ranked like the winner, by distance and then leaf position
-    FCPWGB_D void offer(float d, uint32_t sel) {
-        if (d < d2nd || (d == d2nd && sel < sel2nd)) {
+    // at the end); ranked like the winner, by distance and then leaf position.
+    // The winner itself is not its own runner-up: the persistent schedule
+    // tests its seed before the walk and meets it again in its leaf.
+    FCPWGB_D void offer(float d, uint32_t sel, uint32_t winner) {
+        if (sel != winner && (d < d2nd || (d == d2nd && sel < sel2nd))) {
             d2nd = d;
             sel2nd = sel;
         }
@@ -480,7 +485,7 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
                     selected = off + p;
                     found = true;
                 } else {
-                    tie.offer(d, off + p);
+                    tie.offer(d, off + p, selected);
                 }
             }
         }
@@ -543,7 +548,12 @@ FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphe
             float3 pt2, p2;
             float2 uv2;
             const DS d2 = q.refine(c, q.closestPoint(c, pt2, uv2), p2);
-            if (dsLess(d2, d)) {
+            // the runner-up replaces the winner only when closer by more than
+            // the refinement's own rounding: an exact tie (two faces sharing
+            // the closest edge, whose formulas round differently) stays with
+            // the winner, the earlier leaf position, so that every layout and
+            // schedule returns the same record
+            if (dsSub(d, d2).hi > kRefineTie * d.hi) {
                 d = d2;
                 p = p2;
                 uv = uv2;
@@ -790,7 +800,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                             selected = off + p;
                             found = true;
                         } else {
-                            tie.offer(d, off + p);
+                            tie.offer(d, off + p, selected);
                         }
                     }
                 }
