@@ -821,12 +821,13 @@ def run_ours(args):
                                        for c, t in table]},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 40},
             # per timed step: the query-bound reduction, histogram, three scan kernels and the scatter of
-            # the spatial sort (when on), then the traversal kernel
-            "gpu_launches": args.steps * (7 if best.get("sort_queries", True) else 1),
+            # the spatial sort (when on), then the traversal kernel and the precise mode's refinement pass
+            "gpu_launches": args.steps * ((7 if best.get("sort_queries", True) else 1) + 1),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": f"hbm_gbs ({peak_kind})",
-                         "kernel": "kWidePacketClosestPoint" if best.get("packet") else "kWideClosestPoint",
-                         "kernel_ms": kms,
+                         "kernel": ("kWidePacketClosestPoint" if best.get("packet") else "kWideClosestPoint")
+                         + " + kRefineClosest",
+                         "kernel_ms": kms,  # CUDA events around both kernels of the precise launch
                          "algorithmic_bytes_per_launch": fast_stats["bytes"], "per_query": fast_stats["per_query"]},
             "clocks": clocks, "accuracy": accuracy,
         }
