@@ -59,7 +59,7 @@ struct fcpwgb_gpu_batch {
     std::vector<BatchSceneGrid> grids;
     uint32_t nCells = 0;
     DeviceBuffer gridBuf, offsetBuf, cells, tileSums, perm, sorted, rootBuf, counter, errorWord;
-    DeviceBuffer refineSel;  // precise mode: winner and runner-up leaf positions per sorted query
+    DeviceBuffer refineSel;  // precise mode on triangles: winner and runner-up leaf positions per sorted query
     DeviceBuffer qIn, qOut;
 
     cudaGraphExec_t exec = nullptr;
@@ -199,7 +199,7 @@ int ensureLayout(fcpwgb_gpu_batch *b, const uint32_t *offsets, uint32_t nOffsets
     if ((rc = b->tileSums.ensure((size_t)batchScanTiles((uint32_t)cellBase) * sizeof(uint32_t) + 16))) return rc;
     if ((rc = b->perm.ensure((size_t)std::max(n, 1u) * sizeof(uint32_t)))) return rc;
     if ((rc = b->sorted.ensure((size_t)std::max(n, 1u) * sizeof(DevSphere)))) return rc;
-    if ((rc = b->refineSel.ensure((size_t)std::max(n, 1u) * sizeof(uint2)))) return rc;
+    if (b->dim == 3 && (rc = b->refineSel.ensure((size_t)std::max(n, 1u) * sizeof(uint2)))) return rc;
     if ((rc = b->rootBuf.ensure((size_t)std::max(n, 1u) * sizeof(uint32_t)))) return rc;
     cudaError_t e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) return cudaFail(e, "layout upload");

@@ -1,10 +1,10 @@
-// Precise mode's refinement pass. The traversal kernels leave, per sorted
-// query, the leaf positions of the winner and of the runner-up within the
-// rounding band; this pass computes their distances in double-single
-// arithmetic (FP64 where ill-conditioned, Tri48Prim::refine), keeps the
-// closer one and writes the record to the caller's slot. One thread per
-// query in sorted order, so neighbouring threads read neighbouring
-// primitives.
+// Precise mode's refinement pass on triangles. The traversal kernels leave,
+// per sorted query, the leaf positions of the winner and of the runner-up
+// within the rounding band; this pass computes their distances in
+// double-single arithmetic (FP64 where ill-conditioned, Tri48Prim::refine),
+// keeps the closer one and writes the record to the caller's slot. One
+// thread per query in sorted order, so neighbouring threads read
+// neighbouring primitives. (Segments refine inside the traversal kernels.)
 #include "k_wide.cuh"
 
 namespace fcpwgb {
@@ -26,14 +26,11 @@ __global__ void __launch_bounds__(kRefineBlock) kRefineClosest(const unsigned ch
 
 }  // namespace
 
-cudaError_t launchRefineClosest(int dim, const unsigned char *prims, const DevSphere *spheres, const uint32_t *perm,
-                                const uint2 *sel, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t s) {
+cudaError_t launchRefineTriangles(const unsigned char *prims, const DevSphere *spheres, const uint32_t *perm,
+                                  const uint2 *sel, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const uint32_t g = (n + kRefineBlock - 1) / kRefineBlock;
-    if (dim == 3)
-        kRefineClosest<Tri48Prim><<<g, kRefineBlock, 0, s>>>(prims, spheres, perm, sel, out, n, recordNormal);
-    else
-        kRefineClosest<Seg24Prim><<<g, kRefineBlock, 0, s>>>(prims, spheres, perm, sel, out, n, recordNormal);
+    kRefineClosest<Tri48Prim><<<g, kRefineBlock, 0, s>>>(prims, spheres, perm, sel, out, n, recordNormal);
     return cudaGetLastError();
 }
 

@@ -23,6 +23,10 @@ constexpr float kDsMinScale = 0x1p-28f, kDsMaxScale = 0x1p28f, kDsMinEdge = 0x1p
 
 // 48 B triangle record of the wide kernels: (pa, index), (pb, 0), (pc, 0)
 struct Tri48Prim {
+    // precise mode refines in a second pass (kRefineClosest): inlined at the
+    // end of the traversal, the triangle refinement made the traversal loop
+    // spill
+    static constexpr bool kRefinePass = true;
     float3 pa, pb, pc;
     uint32_t index;
     FCPWGB_D static Tri48Prim load(const unsigned char *prims, uint32_t k) {
@@ -140,8 +144,12 @@ struct Tri48Prim {
     }
 };
 
-// 2D segments keep the 24 B record (SegPrim) and gain an FP64 refinement
+// 2D segments keep the 24 B record (SegPrim) and gain the refinement
 struct Seg24Prim : SegPrim {
+    // precise mode refines at the end of the traversal: the segment
+    // refinement is small enough (no spills), and a second pass over all
+    // records would cost more than it does
+    static constexpr bool kRefinePass = false;
     FCPWGB_D static Seg24Prim load(const unsigned char *prims, uint32_t k) {
         Seg24Prim s;
         SegPrim b = SegPrim::load(prims, k);
@@ -159,8 +167,9 @@ struct Seg24Prim : SegPrim {
         return sqrt(px * px + py * py);
     }
     // double-single counterpart (see Tri48Prim::refine); a segment's
-    // projection has cond = s / d
-    FCPWGB_D DS refine(float3 x, float dApprox, float3 &pOut) const {
+    // projection has cond = s / d (not inlined: it runs inside the traversal
+    // kernels, whose loops keep their registers)
+    __device__ __noinline__ DS refine(float3 x, float dApprox, float3 &pOut) const {
         const float s = fmaxf(fmaxf(fabsf(pa.x - x.x), fabsf(pa.y - x.y)), fmaxf(fabsf(pb.x - x.x), fabsf(pb.y - x.y)));
         const bool ok = s >= kDsMinScale && s <= kDsMaxScale && len3(pb - pa) >= kDsMinEdge &&
                         s <= kDsCond * dApprox;
@@ -503,13 +512,46 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
     return found;
 }
 
+// Precise record of a query from the traversal's winner (leaf position
+// `first`; best holds its FP32 distance, uv and index) and runner-up within
+// the rounding band and the caller's radius (`second`, FP32 distance
+// dSecond; kUintMax: none): both refined (Prim::refine), the runner-up's
+// record when it is closer by more than the refinement's own rounding (an
+// exact tie -- two faces sharing the closest edge, whose formulas round
+// differently -- stays with the winner, the earlier leaf position, so every
+// layout and schedule returns the same record), and the face normal of the
+// one kept (recordNormal).
+template<class Prim>
+FCPWGB_D void refineRecord(const unsigned char *__restrict__ prims, float3 c, uint32_t first, uint32_t second,
+                           float dSecond, int recordNormal, DevInteraction &best) {
+    Prim prim = Prim::load(prims, first);
+    float3 p;
+    DS d = prim.refine(c, best.d, p);
+    if (second != kUintMax) {
+        const Prim q = Prim::load(prims, second);
+        float3 p2;
+        const DS d2 = q.refine(c, dSecond, p2);
+        if (dsSub(d, d2).hi > kRefineTie * d.hi) {
+            float3 pt;
+            float2 uv;
+            q.closestPoint(c, pt, uv);
+            d = d2;
+            p = p2;
+            best.uv = uv;
+            best.index = q.index;
+            prim = q;
+        }
+    }
+    best.d = d.hi;
+    best.p = p;
+    if (recordNormal) best.n = prim.normal();
+}
+
 // Final step of query i. Without PRECISE: the FP32 record of the winner,
-// with its face normal (recordNormal), to the caller's slot. With PRECISE:
-// only the leaf positions of the winner and of the runner-up within the
-// rounding band and the caller's radius (kUintMax: none) to sel[i]; the
-// refinement pass (kRefineClosest) then writes the record. Keeping the
-// refinement out of the traversal kernels keeps its registers out of their
-// loops: inside them it cost 10-18% of the traversal time in spills.
+// with its face normal (recordNormal), to the caller's slot. With PRECISE
+// and Prim::kRefinePass: only the leaf positions of the winner and of the
+// runner-up to sel[i]; the refinement pass (kRefineClosest) then writes the
+// record. With PRECISE otherwise: the refined record (refineRecord).
 template<class Prim, bool PRECISE>
 FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_t *__restrict__ perm,
                           DevInteraction *__restrict__ out, uint2 *__restrict__ sel, uint32_t i, float3 c,
@@ -518,18 +560,23 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
     if constexpr (PRECISE) {
         const bool second = found && tie.sel2nd != kUintMax && tie.d2nd <= best.d + tieBand(c, best.d) &&
                             tie.d2nd * tie.d2nd <= r2User;
-        sel[i] = make_uint2(found ? selected : kUintMax, second ? tie.sel2nd : kUintMax);
+        if constexpr (Prim::kRefinePass) {
+            sel[i] = make_uint2(found ? selected : kUintMax, second ? tie.sel2nd : kUintMax);
+            return;
+        } else {
+            if (found) refineRecord<Prim>(prims, c, selected, second ? tie.sel2nd : kUintMax, tie.d2nd, recordNormal,
+                                          best);
+        }
     } else {
         if (found && recordNormal) best.n = Prim::load(prims, selected).normal();
-        out[perm ? __ldg(perm + i) : i] = best;
     }
+    out[perm ? __ldg(perm + i) : i] = best;
 }
 
-// Record of sorted query i from the leaf positions of finishQuery<PRECISE>:
-// the FP32 closest point of the winner for uv, the refined distance and
-// point (Prim::refine), the runner-up's when it is closer after refinement,
-// and the face normal of the one kept (recordNormal); written to the
-// caller's slot. Without a winner, the default record.
+// The refinement pass's work for sorted query i: the FP32 record of the
+// winner recorded in sel[i] (closest point for uv, distance, index), the
+// runner-up's FP32 distance, then refineRecord; written to the caller's
+// slot. Without a winner, the default record.
 template<class Prim>
 FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphere *__restrict__ spheres,
                           const uint32_t *__restrict__ perm, const uint2 *__restrict__ sel,
@@ -539,32 +586,16 @@ FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphe
     if (s.x != kUintMax) {
         const float4 s4 = ldg4(spheres + i);
         const float3 c = make_float3(s4.x, s4.y, s4.z);
-        Prim prim = Prim::load(prims, s.x);
-        float3 pt, p;
-        float2 uv;
-        DS d = prim.refine(c, prim.closestPoint(c, pt, uv), p);
-        if (s.y != kUintMax) {
-            const Prim q = Prim::load(prims, s.y);
-            float3 pt2, p2;
-            float2 uv2;
-            const DS d2 = q.refine(c, q.closestPoint(c, pt2, uv2), p2);
-            // the runner-up replaces the winner only when closer by more than
-            // the refinement's own rounding: an exact tie (two faces sharing
-            // the closest edge, whose formulas round differently) stays with
-            // the winner, the earlier leaf position, so that every layout and
-            // schedule returns the same record
-            if (dsSub(d, d2).hi > kRefineTie * d.hi) {
-                d = d2;
-                p = p2;
-                uv = uv2;
-                prim = q;
-            }
-        }
-        best.p = p;
-        best.uv = uv;
-        best.d = d.hi;
+        const Prim prim = Prim::load(prims, s.x);
+        float3 pt;
+        best.d = prim.closestPoint(c, pt, best.uv);
         best.index = prim.index;
-        if (recordNormal) best.n = prim.normal();
+        float dSecond = kFltMax;
+        if (s.y != kUintMax) {
+            float2 uv2;
+            dSecond = Prim::load(prims, s.y).closestPoint(c, pt, uv2);
+        }
+        refineRecord<Prim>(prims, c, s.x, s.y, dSecond, recordNormal, best);
     }
     out[perm ? __ldg(perm + i) : i] = best;
 }
@@ -1014,17 +1045,16 @@ cudaError_t launchWideClosestKernel(const WideLaunch &l, cudaStream_t s) {
     }
     return cudaGetLastError();
 }
-// Precise mode: the traversal writes leaf positions to l.sel, then the
-// refinement pass (launchRefineClosest) writes the records.
+// Precise mode on triangles: the traversal writes leaf positions to l.sel,
+// then the refinement pass (launchRefineTriangles) writes the records.
 template<int W, int B, class Prim>
 cudaError_t launchWideClosestPrim(bool precise, const WideLaunch &l, cudaStream_t s) {
     if (precise) {
-        if (!l.sel) return cudaErrorInvalidValue;
+        if (Prim::kRefinePass && !l.sel) return cudaErrorInvalidValue;
         cudaError_t e = l.stats ? launchWideClosestKernel<W, B, Prim, true, true>(l, s)
                                 : launchWideClosestKernel<W, B, Prim, true, false>(l, s);
-        if (e != cudaSuccess) return e;
-        return launchRefineClosest(std::is_same<Prim, Tri48Prim>::value ? 3 : 2, l.prims, l.spheres, l.perm, l.sel,
-                                   l.out, l.n, l.recordNormal, s);
+        if (e != cudaSuccess || !Prim::kRefinePass) return e;
+        return launchRefineTriangles(l.prims, l.spheres, l.perm, l.sel, l.out, l.n, l.recordNormal, s);
     }
     return l.stats ? launchWideClosestKernel<W, B, Prim, false, true>(l, s)
                    : launchWideClosestKernel<W, B, Prim, false, false>(l, s);

@@ -53,7 +53,7 @@ struct WideLaunch {
     const uint32_t *perm = nullptr;        // sorted position -> caller query index, or NULL
     const uint32_t *roots = nullptr;       // root record of every (sorted) query in a forest, or NULL (root 0)
     DevInteraction *out = nullptr;
-    uint2 *sel = nullptr;                  // precise mode: per (sorted) query, winner and runner-up leaf positions
+    uint2 *sel = nullptr;                  // precise mode on triangles: per (sorted) query, winner and runner-up leaf positions
     uint32_t n = 0;
     int recordNormal = 0;
     uint32_t *counter = nullptr;           // work counter (zero on entry) for persistent blocks, or NULL
@@ -64,10 +64,11 @@ struct WideLaunch {
     uint32_t grid = 0;
 };
 template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
-// precise mode's second pass: one thread per (sorted) query refines the winner
-// and runner-up of sel[i] and writes the record to out[perm[i]] (out[i])
-cudaError_t launchRefineClosest(int dim, const unsigned char *prims, const DevSphere *spheres, const uint32_t *perm,
-                                const uint2 *sel, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t s);
+// precise mode's second pass on triangles (48 B records): one thread per
+// (sorted) query refines the winner and runner-up of sel[i] and writes the
+// record to out[perm[i]] (out[i])
+cudaError_t launchRefineTriangles(const unsigned char *prims, const DevSphere *spheres, const uint32_t *perm,
+                                  const uint2 *sel, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t s);
 // dispatch over W = 2, 4, 8
 cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
 // rays on the wide trees (one thread per ray)

@@ -106,7 +106,7 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
         l.spheres = (const DevSphere *)sortSpheres.ptr;
         l.perm = (const uint32_t *)sortPerm.ptr;
     }
-    if (c.precise) {
+    if (c.precise && dim == 3) {
         if ((rc = refineSel.ensure((size_t)n * sizeof(uint2)))) return rc;
         l.sel = (uint2 *)refineSel.ptr;
     }
