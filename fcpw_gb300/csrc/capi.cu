@@ -734,6 +734,11 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
         q = (const DevSphere *)s->sortSpheres.ptr;
         perm = (const uint32_t *)s->sortPerm.ptr;
     }
+    if (s->useWideSilhouettes(sq_min_r)) {
+        rc = s->wideSilhouettes(q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st);
+        if (rc != FCPWGB_ERR_UNSUPPORTED) return rc;
+        // the tree does not collapse into the configured layout: the binary kernel answers
+    }
     FCPWGB_CUDA(launchSilhouetteBinary(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st));
     return FCPWGB_OK;
 }

@@ -1,0 +1,150 @@
+"""Closest silhouette points on the wide trees of SNCH scenes
+(k_wide_sil.cu): against the reference's own answers (tests/golden), against
+the oracle's restatement of the reference traversal (bvh.inl:1435-1596) on
+larger seeded scenes, the same records for every branching factor and query
+order, refits, and the cases that stay on the binary kernel."""
+import numpy as np
+import pytest
+
+import fcpw_gb300 as F
+from fcpw_gb300 import records as R
+from fcpw_gb300 import workloads as W
+from helpers import build_scene, distance_tolerance
+from oracle import oracle as O
+from test_gpu_golden import GOLDEN, bvh_type
+
+pytestmark = pytest.mark.gpu
+
+
+def run(g, pts, flip, r2=None, sq_min_r=0.0):
+    out = F.GPUInteractionList()
+    r2 = np.full(len(pts), R.FLT_MAX, np.float32) if r2 is None else r2
+    g.find_closest_silhouette_points(pts, r2, flip, out, sq_min_r, 1e-3)
+    return out.array()
+
+
+def compare(dim, pts, got, ref, what):
+    """Found flags agree up to grazing cases, distances within the
+    silhouette tests' precision (1e-3, tests/aggregate_tests.cpp:610) plus
+    the rounding floor of helpers.py, and the same silhouette almost always."""
+    fg, fr = got["index"] != R.UINT_MAX, ref["index"] != R.UINT_MAX
+    assert (fg != fr).sum() <= max(2, int(1e-4 * len(pts))), f"{what}: found flags differ"
+    both = fg & fr
+    tol = distance_tolerance(pts[both], ref["p"][both][:, :dim], ref["d"][both])
+    dd = np.abs(got["d"][both].astype(np.float64) - ref["d"][both])
+    assert np.all(dd <= 1e-3 * ref["d"][both] + tol), f"{what}: worst |dd| {dd.max():.3e}"
+    assert (got["index"][both] == ref["index"][both]).mean() > 0.995, what
+
+
+@pytest.fixture(scope="module", params=[2, 3], ids=["2d", "3d"])
+def scene(request):
+    dim = request.param
+    if dim == 2:
+        v, idx = W.star_polylines(64, 128, W.SEED_BASE + 3)
+        pts = W.uniform_points(50000, 2, -3, 3, 91)
+    else:
+        v, idx = W.torus(64, 32, W.SEED_BASE + 2)
+        pts = W.uniform_points(30000, 3, -2, 2, 92)
+    s = build_scene(dim, v, idx, silhouettes=True)
+    g = F.GPUScene3D() if dim == 3 else F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    flip = (W.rng(93).uniform(0, 1, len(pts)) < 0.5).astype(np.uint32)
+    nodes, _, sils = s.cpu_bvh.export()
+    ref = O.silhouettes_bvh(dim, nodes, sils, R.make_spheres(pts, R.FLT_MAX), flip)
+    return dim, s, g, pts, flip, ref
+
+
+@pytest.mark.parametrize("branching", [2, 4, 8])
+def test_wide_silhouettes_match_oracle(scene, branching):
+    dim, s, g, pts, flip, ref = scene
+    g.set_traversal(branching, 32, sort_queries=True)
+    got = run(g, pts, flip)
+    g.set_traversal(0)
+    compare(dim, pts, got, ref, f"{dim}D W={branching}")
+    assert g.check_errors() == 0
+
+
+def test_wide_silhouette_layouts_agree(scene):
+    """Exact distance ties go to the earlier silhouette reference, so every
+    branching factor, the query order and the schedule flags (which the
+    silhouette packets ignore) give byte-identical records."""
+    dim, s, g, pts, flip, ref = scene
+    outs = {}
+    for cfg in [dict(branching=4, bits=32), dict(branching=2, bits=32), dict(branching=8, bits=32),
+                dict(branching=4, bits=32, sort_queries=False), dict(branching=4, bits=32, packet=True),
+                dict(branching=4, bits=32, persistent=False)]:
+        g.set_traversal(**cfg)
+        outs[str(cfg)] = run(g, pts, flip).tobytes()
+    g.set_traversal(0)
+    first = next(iter(outs.values()))
+    assert [k for k, v in outs.items() if v != first] == []
+
+
+def test_wide_silhouettes_finite_radius(scene):
+    dim, s, g, pts, flip, _ = scene
+    r2 = (0.5 * W.rng(94).uniform(0, 1, len(pts)) ** 2).astype(np.float32)
+    nodes, _, sils = s.cpu_bvh.export()
+    ref = O.silhouettes_bvh(dim, nodes, sils, R.make_spheres(pts, r2), flip)
+    g.set_traversal(4, 32)
+    got = run(g, pts, flip, r2)
+    g.set_traversal(0)
+    compare(dim, pts, got, ref, f"{dim}D finite radius")
+
+
+def test_layouts_outside_the_wide_path_use_the_binary_kernel(scene):
+    """A positive squared minimum radius (early stop in the reference's
+    visiting order), quantised boxes and merged leaves answer with the binary
+    kernel: byte-identical to the binary configuration."""
+    dim, s, g, pts, flip, _ = scene
+    sub, fsub = pts[:20000], flip[:20000]
+    for sq_min_r in (0.0, 0.01):
+        g.set_traversal(0)
+        base = run(g, sub, fsub, sq_min_r=sq_min_r).tobytes()
+        cfgs = [dict(branching=4, bits=8), dict(branching=4, bits=32, leaf_size=8)]
+        if sq_min_r > 0:
+            cfgs.append(dict(branching=4, bits=32))
+        for cfg in cfgs:
+            g.set_traversal(**cfg)
+            assert run(g, sub, fsub, sq_min_r=sq_min_r).tobytes() == base, (sq_min_r, cfg)
+    g.set_traversal(0)
+
+
+def test_wide_silhouettes_after_refit():
+    """Moved vertices, refit on the GPU: the cone records follow the refit
+    binary nodes."""
+    v, sg = W.star_polylines(16, 64, W.SEED_BASE + 7)
+    s = build_scene(2, v, sg, silhouettes=True)
+    g = F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    n = 20000
+    pts = W.uniform_points(n, 2, -3, 3, 95)
+    flip = np.zeros(n, np.uint32)
+    g.set_traversal(4, 32)
+    run(g, pts, flip)  # builds the wide tree and its cones
+    v2 = (v + 0.002 * W.rng(96).normal(size=v.shape)).astype(np.float32)
+    s.update_object_vertices(v2, 0)
+    g.refit(s, True)
+    got = run(g, pts, flip)
+    g.set_traversal(0)
+    nodes, prims, sils = s.cpu_bvh.export()
+    ref = O.silhouettes_bvh(2, O.refit(2, nodes, prims, sils), sils, R.make_spheres(pts, R.FLT_MAX), flip)
+    compare(2, pts, got, ref, "after refit")
+
+
+@pytest.mark.parametrize("path", [p for p in GOLDEN], ids=[p.stem for p in GOLDEN])
+def test_wide_silhouettes_match_reference(path):
+    fx = dict(np.load(path))
+    if "sil_out" not in fx:
+        pytest.skip("fixture without silhouettes")
+    dim = int(fx["dim"])
+    g = F.GPUScene3D() if dim == 3 else F.GPUScene2D()
+    g.transfer_arrays(bvh_type(fx), fx["nodes"], fx["prims"], fx.get("sils"))
+    g.set_traversal(4, 32)
+    pts = fx["sil_points"]
+    got = run(g, pts, fx["sil_flip"])
+    ref = fx["sil_out"]
+    fg, fr = got["index"] != R.UINT_MAX, ref["index"] != R.UINT_MAX
+    assert (fg != fr).sum() <= 1
+    both = fg & fr
+    tol = distance_tolerance(pts[both], ref["p"][both][:, :dim], ref["d"][both])
+    assert np.all(np.abs(got["d"][both] - ref["d"][both]) <= 1e-3 * ref["d"][both] + tol)
