@@ -342,11 +342,11 @@ def run_suite(args):
         gs.set_traversal(0)
         plain = timed(sil_run(gs, sph, flip, out, n))
         variants = {}
-        gs.set_traversal(4, 8, sort_queries=True)  # 8-bit boxes: the binary kernel on spatially sorted queries
-        variants["binary, queries sorted"] = timed(sil_run(gs, sph, flip, out, n))
-        for w in (2, 4, 8):  # wide trees with per-slot cones, warp packets, queries sorted
-            gs.set_traversal(w, 32, sort_queries=True)
-            variants[f"wide{w}_q32_packet, queries sorted"] = timed(sil_run(gs, sph, flip, out, n))
+        # a fast-path configuration: warp packets on the binary SNCH tree (k_sil_packet.cu)
+        for sort in (True, False):
+            gs.set_traversal(4, 32, sort_queries=sort)
+            variants["warp packets, queries sorted" if sort else "warp packets, caller order"] = timed(
+                sil_run(gs, sph, flip, out, n))
         gs.set_traversal(0)
         best = min(variants, key=variants.get)
         fast = variants[best]

@@ -724,8 +724,9 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
     const DevSphere *q = (const DevSphere *)spheres;
     const uint32_t *perm = nullptr;
     if (s->useWide() && s->wideConfig.sortQueries && n >= 4096) {
-        // with a fast-path configuration the queries are sorted spatially first;
-        // each query's traversal, and so its result, is unchanged
+        // with a fast-path configuration the queries are sorted spatially first, so
+        // a warp packet holds neighbouring queries (the packets' answers, like the
+        // binary kernel's, do not depend on the order of the queries)
         if ((rc = s->sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;
         if ((rc = s->sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
         if ((rc = s->sortSpheres.ensure((size_t)n * sizeof(DevSphere)))) return rc;
@@ -734,10 +735,9 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
         q = (const DevSphere *)s->sortSpheres.ptr;
         perm = (const uint32_t *)s->sortPerm.ptr;
     }
-    if (s->useWideSilhouettes(sq_min_r)) {
-        rc = s->wideSilhouettes(q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st);
-        if (rc != FCPWGB_ERR_UNSUPPORTED) return rc;
-        // the tree does not collapse into the configured layout: the binary kernel answers
+    if (s->usePacketSilhouettes(sq_min_r)) {
+        FCPWGB_CUDA(launchSilhouettePacket(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st));
+        return FCPWGB_OK;
     }
     FCPWGB_CUDA(launchSilhouetteBinary(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st));
     return FCPWGB_OK;

@@ -71,26 +71,11 @@ cudaError_t launchRefineTriangles(const unsigned char *prims, const DevSphere *s
                                   const uint2 *sel, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t s);
 // dispatch over W = 2, 4, 8
 cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
-// closest silhouette points on the wide trees of an SNCH scene (k_wide_sil.cu):
-// warp packets over float-box wide records with unmerged leaves, plus one
-// cone record per child slot (wideConeBytes() each, built by launchWideCones
-// from the binary node behind every slot)
-struct WideSilLaunch {
-    const unsigned char *nodes = nullptr;  // wide records, 32-bit boxes
-    const void *cones = nullptr;           // per child slot
-    const unsigned char *sils = nullptr;   // 56 B edges (3D) or 32 B vertices (2D)
-    const DevSphere *spheres = nullptr;    // (sorted when perm is set)
-    const uint32_t *flip = nullptr;        // caller order
-    const uint32_t *perm = nullptr;        // sorted position -> caller query index, or NULL
-    DevInteraction *out = nullptr;
-    uint32_t n = 0;
-    float sqMinR = 0.0f, precision = 1e-3f;
-    uint32_t *errorWord = nullptr;
-};
-size_t wideConeBytes();
-cudaError_t launchWideCones(const int32_t *childBinary, const unsigned char *binNodes, uint32_t nSlots, void *cones,
-                            cudaStream_t s);
-cudaError_t launchWideSilhouette(int W, int dim, const WideSilLaunch &l, cudaStream_t s);
+// closest silhouette points with warp packets on the binary SNCH tree
+// (k_sil_packet.cu): queries sorted when perm is set, flip in caller order
+cudaError_t launchSilhouettePacket(const SceneView &v, const DevSphere *spheres, const uint32_t *flip,
+                                   const uint32_t *perm, DevInteraction *out, uint32_t n, float sqMinR,
+                                   float precision, cudaStream_t s);
 // rays on the wide trees (one thread per ray)
 struct WideRayLaunch {
     const unsigned char *nodes = nullptr;

@@ -62,7 +62,6 @@ int GpuScene::ensureWide(cudaStream_t st) {
         return cudaFail(e, "requantize");
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "wide build");
     wide.valid = true;
-    wide.cones = false;
     wide.branching = c.branching;
     wide.bits = c.bits;
     wide.leafSize = c.leafSize;
@@ -238,49 +237,9 @@ int GpuScene::closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_in
     return 0;
 }
 
-int GpuScene::ensureWideCones(cudaStream_t st) {
-    int rc = ensureWide(st);
-    if (rc) return rc;
-    if (wide.cones) return 0;
-    if ((uint64_t)wide.nNodes * wide.branching >= (1u << 31))
-        return setError(FCPWGB_ERR_UNSUPPORTED, "too many wide nodes for silhouette leaf references");
-    const uint32_t slots = wide.nNodes * (uint32_t)wide.branching;
-    if ((rc = wideCones.ensure((size_t)slots * wideConeBytes()))) return rc;
-    cudaError_t e = launchWideCones((const int32_t *)wideChildBinary.ptr, (const unsigned char *)nodes.ptr, slots,
-                                    wideCones.ptr, st);
-    if (e != cudaSuccess) return cudaFail(e, "wide cones");
-    wide.cones = true;
-    return 0;
-}
-
-int GpuScene::wideSilhouettes(const DevSphere *spheres, const uint32_t *flip, const uint32_t *perm,
-                              DevInteraction *out, uint32_t n, float sqMinR, float precision, cudaStream_t st) {
-    int rc = ensureWideCones(st);
-    if (rc) return rc;
-    WideSilLaunch l;
-    l.nodes = (const unsigned char *)wideNodes.ptr;
-    l.cones = wideCones.ptr;
-    l.sils = (const unsigned char *)sils.ptr;
-    l.spheres = spheres;
-    l.flip = flip;
-    l.perm = perm;
-    l.out = out;
-    l.n = n;
-    l.sqMinR = sqMinR;
-    l.precision = precision;
-    l.errorWord = (uint32_t *)errorWord.ptr;
-    if ((rc = timeStart(st))) return rc;
-    cudaError_t e = launchWideSilhouette(wide.branching, dim, l, st);
-    if (e != cudaSuccess) return cudaFail(e, "wide silhouette launch");
-    return timeEnd(st);
-}
-
 int GpuScene::afterRefit(cudaStream_t st) {
     if (!wide.valid) return 0;
     cudaError_t e;
-    if (wide.cones && (e = launchWideCones((const int32_t *)wideChildBinary.ptr, (const unsigned char *)nodes.ptr,
-                                           wide.nNodes * (uint32_t)wide.branching, wideCones.ptr, st)) != cudaSuccess)
-        return cudaFail(e, "wide cones");
     if (dim == 3 && (e = launchPackTri48((const DevTriangle *)prims.ptr, nPrims, (float4 *)widePrims.ptr, st)) !=
                         cudaSuccess)
         return cudaFail(e, "pack triangles");

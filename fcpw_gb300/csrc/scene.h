@@ -75,7 +75,7 @@ struct GpuScene {
     // derived wide / quantised tree (built on demand, see wide.h)
     WideConfig wideConfig;
     WideTree wide;
-    DeviceBuffer wideNodes, wideChildBinary, widePrims, wideCones;
+    DeviceBuffer wideNodes, wideChildBinary, widePrims;
     // scratch of the fast path: query sort cells / permutation / sorted copy, work counter,
     // precise mode's winner and runner-up leaf positions
     DeviceBuffer sortCells, sortPerm, sortSpheres, sortRays, workCounter, refineSel;
@@ -124,16 +124,10 @@ struct GpuScene {
     // builds (or rebuilds) the wide tree the current config asks for
     int ensureWide(cudaStream_t st);
     bool useWide() const { return wideConfig.branching > 0; }
-    // silhouette queries on the wide tree: an SNCH scene, float boxes, unmerged
-    // leaves, and no positive minimum radius (whose early stop follows the
-    // reference's visiting order)
-    bool useWideSilhouettes(float sqMinR) const {
-        return useWide() && snch && wideConfig.bits == 32 && wideConfig.leafSize == 0 && !(sqMinR > 0.0f);
-    }
-    // builds the wide tree and its per-slot cone records
-    int ensureWideCones(cudaStream_t st);
-    int wideSilhouettes(const DevSphere *spheres, const uint32_t *flip, const uint32_t *perm, DevInteraction *out,
-                        uint32_t n, float sqMinR, float precision, cudaStream_t st);
+    // silhouette queries as warp packets (with a fast-path configuration and no
+    // positive minimum radius, whose early stop follows the reference's
+    // visiting order)
+    bool usePacketSilhouettes(float sqMinR) const { return useWide() && !(sqMinR > 0.0f); }
     int wideRays(const DevRay *rays, DevInteraction *out, uint32_t n, int occl, cudaStream_t st);
     SortLimits sortLimits() const;
     int smCount();  // multiprocessors of the scene's device (queried once)

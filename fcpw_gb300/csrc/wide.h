@@ -63,14 +63,10 @@ bool buildWideTree(int W, int bits, const std::vector<uint32_t> &nPrims, const s
 // what a scene keeps about its derived wide tree (buffers live in the scene)
 struct WideTree {
     bool valid = false;
-    bool cones = false;  // per-slot cone records of an SNCH scene built (silhouette queries)
     int branching = 0, bits = 32, leafSize = 0;
     uint32_t nNodes = 0, depth = 0;
     uint64_t builtFromVersion = 0;
-    void clear() {
-        valid = false;
-        cones = false;
-    }
+    void clear() { valid = false; }
 };
 
 }  // namespace fcpwgb

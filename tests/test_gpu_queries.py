@@ -297,10 +297,12 @@ def test_fp64_brute_force_probe_matches_oracle(sphere20k, stars2d, dim):
     assert np.allclose(d_gpu, d_ref, rtol=1e-12, atol=1e-14)
 
 
-def test_sorted_silhouette_queries_give_identical_results(stars2d):
+def test_fast_path_silhouettes_agree_with_binary_kernel(stars2d):
     """With a fast-path configuration silhouette queries are sorted spatially
-    before the traversal; each query's traversal is unchanged, so the results
-    are bit-identical to the unsorted ones, in the caller's order."""
+    and answered by warp packets (k_sil_packet.cu). The same tests prune the
+    same subtrees, so against the binary kernel (reference order) the found
+    flags are equal and the distances agree to the rounding floor; the
+    silhouette differs only on exact ties."""
     s, g = stars2d
     n = 50000
     pts = W.uniform_points(n, 2, -3, 3, 61)
@@ -313,7 +315,11 @@ def test_sorted_silhouette_queries_give_identical_results(stars2d):
     b = F.GPUInteractionList()
     g.find_closest_silhouette_points(pts, r2, flip, b, 0.0, 1e-3)
     g.set_traversal(0)
-    assert a.array().tobytes() == b.array().tobytes()
+    a, b = a.array(), b.array()
+    fa, fb = a["index"] != R.UINT_MAX, b["index"] != R.UINT_MAX
+    assert np.array_equal(fa, fb)
+    tol = distance_tolerance(pts[fa], a["p"][fa][:, :2], a["d"][fa])
+    assert np.all(np.abs(a["d"][fa].astype(np.float64) - b["d"][fa]) <= tol)
 
 
 @pytest.mark.parametrize("dim", [3, 2])

@@ -1,8 +1,9 @@
-"""Closest silhouette points on the wide trees of SNCH scenes
-(k_wide_sil.cu): against the reference's own answers (tests/golden), against
-the oracle's restatement of the reference traversal (bvh.inl:1435-1596) on
-larger seeded scenes, the same records for every branching factor and query
-order, refits, and the cases that stay on the binary kernel."""
+"""Closest silhouette points with warp packets on the binary SNCH tree
+(k_sil_packet.cu, used with a fast-path configuration): against the
+reference's own answers (tests/golden), against the oracle's restatement of
+the reference traversal (bvh.inl:1435-1596) on larger seeded scenes, the
+same records for every configuration and query order, refits, and the
+positive minimum radius that stays on the binary kernel."""
 import numpy as np
 import pytest
 
@@ -24,16 +25,22 @@ def run(g, pts, flip, r2=None, sq_min_r=0.0):
 
 
 def compare(dim, pts, got, ref, what):
-    """Found flags agree up to grazing cases, distances within the
+    """Found flags agree up to grazing cases and distances within the
     silhouette tests' precision (1e-3, tests/aggregate_tests.cpp:610) plus
-    the rounding floor of helpers.py, and the same silhouette almost always."""
+    the rounding floor of helpers.py. The silhouette may differ on exact
+    ties: in 3D the closest silhouette point is often a vertex shared by
+    several silhouette edges, which the reference resolves by its visiting
+    order and the packets by the earlier reference."""
     fg, fr = got["index"] != R.UINT_MAX, ref["index"] != R.UINT_MAX
     assert (fg != fr).sum() <= max(2, int(1e-4 * len(pts))), f"{what}: found flags differ"
     both = fg & fr
     tol = distance_tolerance(pts[both], ref["p"][both][:, :dim], ref["d"][both])
     dd = np.abs(got["d"][both].astype(np.float64) - ref["d"][both])
     assert np.all(dd <= 1e-3 * ref["d"][both] + tol), f"{what}: worst |dd| {dd.max():.3e}"
-    assert (got["index"][both] == ref["index"][both]).mean() > 0.995, what
+    same = got["index"][both] == ref["index"][both]
+    # a different silhouette is almost always at the same distance (a tie, up to the rounding floor)
+    assert np.count_nonzero(dd[~same] > tol[~same]) <= max(2, int(1e-3 * both.sum())), \
+        f"{what}: different silhouettes that are not ties"
 
 
 @pytest.fixture(scope="module", params=[2, 3], ids=["2d", "3d"])
@@ -54,33 +61,41 @@ def scene(request):
     return dim, s, g, pts, flip, ref
 
 
-@pytest.mark.parametrize("branching", [2, 4, 8])
-def test_wide_silhouettes_match_oracle(scene, branching):
+@pytest.mark.parametrize("sort_queries", [True, False])
+def test_packet_silhouettes_match_oracle(scene, sort_queries):
     dim, s, g, pts, flip, ref = scene
-    g.set_traversal(branching, 32, sort_queries=True)
+    g.set_traversal(4, 32, sort_queries=sort_queries)
     got = run(g, pts, flip)
     g.set_traversal(0)
-    compare(dim, pts, got, ref, f"{dim}D W={branching}")
+    compare(dim, pts, got, ref, f"{dim}D sorted {sort_queries}")
     assert g.check_errors() == 0
 
 
-def test_wide_silhouette_layouts_agree(scene):
-    """Exact distance ties go to the earlier silhouette reference, so every
-    branching factor, the query order and the schedule flags (which the
-    silhouette packets ignore) give byte-identical records."""
+def test_packet_silhouettes_do_not_depend_on_order(scene):
+    """Boxes within the winner's distance plus the rounding band are visited
+    and exact ties go to the earlier silhouette reference, so the records are
+    byte-identical whatever the configuration (the packets walk the binary
+    tree; the wide settings do not apply), the sort, and the order in which
+    the caller lists the queries."""
     dim, s, g, pts, flip, ref = scene
     outs = {}
-    for cfg in [dict(branching=4, bits=32), dict(branching=2, bits=32), dict(branching=8, bits=32),
-                dict(branching=4, bits=32, sort_queries=False), dict(branching=4, bits=32, packet=True),
-                dict(branching=4, bits=32, persistent=False)]:
+    for cfg in [dict(branching=4, bits=32), dict(branching=2, bits=16), dict(branching=8, bits=8),
+                dict(branching=4, bits=32, sort_queries=False), dict(branching=4, bits=32, leaf_size=8),
+                dict(branching=4, bits=32, persistent=False, packet=True)]:
         g.set_traversal(**cfg)
         outs[str(cfg)] = run(g, pts, flip).tobytes()
+    perm = W.rng(97).permutation(len(pts))
+    g.set_traversal(4, 32, sort_queries=False)
+    shuffled = run(g, pts[perm], flip[perm])
     g.set_traversal(0)
     first = next(iter(outs.values()))
     assert [k for k, v in outs.items() if v != first] == []
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(len(perm))
+    assert shuffled[inv].tobytes() == first
 
 
-def test_wide_silhouettes_finite_radius(scene):
+def test_packet_silhouettes_finite_radius(scene):
     dim, s, g, pts, flip, _ = scene
     r2 = (0.5 * W.rng(94).uniform(0, 1, len(pts)) ** 2).astype(np.float32)
     nodes, _, sils = s.cpu_bvh.export()
@@ -91,27 +106,24 @@ def test_wide_silhouettes_finite_radius(scene):
     compare(dim, pts, got, ref, f"{dim}D finite radius")
 
 
-def test_layouts_outside_the_wide_path_use_the_binary_kernel(scene):
-    """A positive squared minimum radius (early stop in the reference's
-    visiting order), quantised boxes and merged leaves answer with the binary
-    kernel: byte-identical to the binary configuration."""
+def test_positive_min_radius_uses_the_binary_kernel(scene):
+    """A positive squared minimum radius stops at the first silhouette found
+    within it, in the reference's visiting order: with a fast-path
+    configuration the binary kernel still answers, byte-identical to the
+    binary configuration (sorting does not change its per-query traversal)."""
     dim, s, g, pts, flip, _ = scene
     sub, fsub = pts[:20000], flip[:20000]
-    for sq_min_r in (0.0, 0.01):
-        g.set_traversal(0)
-        base = run(g, sub, fsub, sq_min_r=sq_min_r).tobytes()
-        cfgs = [dict(branching=4, bits=8), dict(branching=4, bits=32, leaf_size=8)]
-        if sq_min_r > 0:
-            cfgs.append(dict(branching=4, bits=32))
-        for cfg in cfgs:
-            g.set_traversal(**cfg)
-            assert run(g, sub, fsub, sq_min_r=sq_min_r).tobytes() == base, (sq_min_r, cfg)
+    g.set_traversal(0)
+    base = run(g, sub, fsub, sq_min_r=0.01).tobytes()
+    for cfg in [dict(branching=4, bits=32), dict(branching=4, bits=8, sort_queries=False)]:
+        g.set_traversal(**cfg)
+        assert run(g, sub, fsub, sq_min_r=0.01).tobytes() == base, cfg
     g.set_traversal(0)
 
 
-def test_wide_silhouettes_after_refit():
-    """Moved vertices, refit on the GPU: the cone records follow the refit
-    binary nodes."""
+def test_packet_silhouettes_after_refit():
+    """Moved vertices, refit on the GPU: the packets read the refit boxes and
+    cones."""
     v, sg = W.star_polylines(16, 64, W.SEED_BASE + 7)
     s = build_scene(2, v, sg, silhouettes=True)
     g = F.GPUScene2D()
@@ -120,7 +132,7 @@ def test_wide_silhouettes_after_refit():
     pts = W.uniform_points(n, 2, -3, 3, 95)
     flip = np.zeros(n, np.uint32)
     g.set_traversal(4, 32)
-    run(g, pts, flip)  # builds the wide tree and its cones
+    run(g, pts, flip)
     v2 = (v + 0.002 * W.rng(96).normal(size=v.shape)).astype(np.float32)
     s.update_object_vertices(v2, 0)
     g.refit(s, True)
@@ -132,7 +144,7 @@ def test_wide_silhouettes_after_refit():
 
 
 @pytest.mark.parametrize("path", [p for p in GOLDEN], ids=[p.stem for p in GOLDEN])
-def test_wide_silhouettes_match_reference(path):
+def test_packet_silhouettes_match_reference(path):
     fx = dict(np.load(path))
     if "sil_out" not in fx:
         pytest.skip("fixture without silhouettes")
