@@ -14,9 +14,9 @@
 // Equal distances: the reference keeps the later candidate of its own
 // visiting order. Here boxes are visited within the winner's distance plus
 // the rounding band of the closest-point kernels (bandRadius2), so every
-// candidate at the winner's distance is tested, and the earlier silhouette
-// reference wins: the answer does not depend on which queries share a warp
-// or on their order. (A wide collapse of the tree would skip the cone tests
+// candidate at the winner's distance is tested, and the earliest silhouette
+// reference wins (over all listings of the tied silhouettes): the answer
+// does not depend on which queries share a warp or on their order. (A wide collapse of the tree would skip the cone tests
 // of the collapsed binary nodes, whose outcome is not monotone in floating
 // point, so the packets walk the binary nodes.) With a positive squared
 // minimum radius the reference stops at the first silhouette found within
@@ -75,9 +75,14 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
                 const NodeCone cone = loadCone(nodes, cur);
                 for (uint32_t p = 0; p < cone.nSil; p++) {
                     const Sil sil = Sil::load(sils, cone.silOffset + p);
-                    if (act && sil.index != best.index) {
+                    const uint32_t pos = cone.silOffset + p;
+                    if (act && sil.index == best.index) {
+                        // the winner again, listed in another leaf (an edge is listed for both of
+                        // its faces): not tested again, as in the reference, but its earliest
+                        // listing is what a tie compares against
+                        bestPos = min(bestPos, pos);
+                    } else if (act) {
                         DevInteraction cI = defaultInteraction();
-                        const uint32_t pos = cone.silOffset + p;
                         if (sil.closestSilhouettePoint(c, r2, flipNormal, sqMinR, precision, cI) &&
                             (bestPos == kUintMax || cI.d < best.d || (cI.d == best.d && pos < bestPos))) {
                             r2 = fminf(r2, cI.d * cI.d);
