@@ -16,9 +16,10 @@
 // the rounding band of the closest-point kernels (bandRadius2), so every
 // candidate at the winner's distance is tested, and the earliest silhouette
 // reference wins (over all listings of the tied silhouettes): the answer
-// does not depend on which queries share a warp or on their order. (A wide collapse of the tree would skip the cone tests
-// of the collapsed binary nodes, whose outcome is not monotone in floating
-// point, so the packets walk the binary nodes.) With a positive squared
+// does not depend on which queries share a warp or on their order. (A wide
+// collapse of the tree would skip the cone tests of the collapsed binary
+// nodes, whose outcome is not monotone in floating point, so the packets
+// walk the binary nodes.) With a positive squared
 // minimum radius the reference stops at the first silhouette found within
 // it, which depends on its visiting order: that case stays on the binary
 // kernel (k_binary.cu).
