@@ -208,6 +208,17 @@ template<int W, int BITS> struct WideNodeRegs {
     FCPWGB_D uint32_t halfAt(int off) const { return (w[off >> 2] >> (8 * (off & 3))) & 0xffffu; }
     FCPWGB_D uint32_t ref(int c) const { return w[(L::kRefs >> 2) + c]; }
     FCPWGB_D uint32_t cnt(int c) const { return byteAt(L::kCnt + c); }
+    // cnt of a runtime slot (< W) by shifts, without indexing the registers:
+    // the count bytes start on a word, one word for W <= 4, two for W = 8
+    FCPWGB_D uint32_t cntAt(uint32_t slot) const {
+        static_assert((L::kCnt & 3) == 0, "count bytes start on a word");
+        if constexpr (W <= 4) {
+            return (w[L::kCnt >> 2] >> (8u * slot)) & 0xffu;
+        } else {
+            const uint64_t b = (uint64_t)w[L::kCnt >> 2] | ((uint64_t)w[(L::kCnt >> 2) + 1] << 32);
+            return (uint32_t)(b >> (8u * slot)) & 0xffu;
+        }
+    }
     FCPWGB_D float origin(int a) const { return __uint_as_float(w[a]); }
     FCPWGB_D float scale(int a) const { return exp2i((int)byteAt(12 + a) - 127); }
     // bound k = 0..2 lo(x,y,z), 3..5 hi(x,y,z) of child c
@@ -761,36 +772,39 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                         rp2 = tie.prune(r2, c);
                     }
                 }
-                // children needed by any lane, ordered by the first active lane's distances
+                // children needed by any lane (one OR over the warp of each lane's
+                // mask), ordered by the first active lane's distances
+                uint32_t needMask = 0;
+#pragma unroll
+                for (int k = 0; k < W; k++)
+                    needMask |= (act && node.cnt(k) != kWideEmpty && d2Min[k] <= rp2) ? (1u << k) : 0u;
+                const uint32_t anyMask = __reduce_or_sync(0xffffffffu, needMask);
                 const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
                 uint32_t key[W];
-                int nh = 0;
 #pragma unroll
                 for (int k = 0; k < W; k++) {
-                    bool need = act && node.cnt(k) != kWideEmpty && d2Min[k] <= rp2;
-                    bool any = __ballot_sync(0xffffffffu, need) != 0;
-                    float lead = __shfl_sync(0xffffffffu, d2Min[k], leader);
-                    key[k] = any ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
-                    nh += any ? 1 : 0;
+                    const float lead = __shfl_sync(0xffffffffu, d2Min[k], leader);
+                    key[k] = ((anyMask >> k) & 1u) ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
                 }
+                const int nh = __popc(anyMask);
                 sortNetwork<W>(key);
                 if (nh > 0) {
                     if (sp + nh - 1 > kWideStack) {
                         if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
                         break;
                     }
-                    uint32_t refs[W];
-                    childRefs<W, BITS>(node, refs);
-                    // a lane out of this record is out of its children too (NaN is never <= rp2)
-                    float mine[W];
+                    uint32_t rawRefs[W];
 #pragma unroll
-                    for (int s = 0; s < W; s++) mine[s] = act ? d2Min[s] : __int_as_float(0x7fc00000);
+                    for (int s = 0; s < W; s++) rawRefs[s] = node.ref(s);
 #pragma unroll
                     for (int k = W - 1; k >= 0; k--) {
                         if (k < nh) {
                             const uint32_t slot = key[k] & kSlotMask;
-                            uint32_t packed = selectBySlot<W>(refs, slot);
-                            float dl = selectBySlot<W>(mine, slot);
+                            const uint32_t cnt = node.cntAt(slot);
+                            const uint32_t ref = selectBySlot<W>(rawRefs, slot);
+                            const uint32_t packed = cnt == 0 ? ref : packLeaf(ref, cnt);
+                            // a lane out of this record is out of its children too (NaN is never <= rp2)
+                            const float dl = act ? selectBySlot<W>(d2Min, slot) : __int_as_float(0x7fc00000);
                             if (k == 0) {
                                 cur = packed;
                                 act = dl <= rp2;
