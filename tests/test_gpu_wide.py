@@ -6,7 +6,7 @@ import pytest
 import fcpw_gb300 as F
 from fcpw_gb300 import records as R
 from fcpw_gb300 import workloads as W
-from helpers import build_scene, compare_closest, relative_error
+from helpers import build_scene, compare_closest, leaf_positions, relative_error
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -101,6 +101,37 @@ def test_wide_finite_radius_and_normals(torus):
     compare_closest(3, prims, pts, got, ref2, "wide finite radius")
     same = (got["index"] == ref2["index"]) & (ref2["index"] != R.UINT_MAX)
     assert np.allclose(got["n"][same], ref2["n"][same], atol=1e-6)
+
+
+@pytest.mark.parametrize("cfg", [dict(branching=4, bits=32, packet=True), dict(branching=4, bits=8, persistent=False),
+                                 dict(branching=2, bits=16, persistent=True)])
+def test_precise_mode_finite_radius_and_normals(torus, cfg):
+    """Precise mode on triangles writes its records in the refinement pass:
+    the face normal of the primitive it keeps, the caller's radius respected
+    by the winner and the runner-up, and FP64-accurate distances."""
+    s, g, pts, ref, prims = torus
+    sub = pts[:40000]
+    r2 = (0.05 * W.rng(45).uniform(0, 1, len(sub))).astype(np.float32)
+    nodes, _, _ = s.cpu_bvh.export()
+    ref2 = O.closest_points_bvh(3, nodes, prims, R.make_spheres(sub, r2), record_normals=True)
+    g.set_traversal(precise=True, **cfg)
+    out = F.GPUInteractionList()
+    g.find_closest_points(sub, r2, out, True)
+    got = out.array()
+    g.set_traversal(0)
+    compare_closest(3, prims, sub, got, ref2, f"precise finite radius {cfg}")
+    found = got["index"] != R.UINT_MAX
+    assert np.all(got["d"][found].astype(np.float64) ** 2 <= r2[found].astype(np.float64) * (1 + 1e-6))
+    same = (got["index"] == ref2["index"]) & found
+    assert np.allclose(got["n"][same], ref2["n"][same], atol=1e-6)
+    # the normal is the kept primitive's own face normal
+    pos = leaf_positions(prims)[got["index"][found].astype(np.int64)]
+    p = prims[pos]
+    n = np.cross(p["pb"][:, :3].astype(np.float64) - p["pa"][:, :3], p["pc"][:, :3].astype(np.float64) - p["pa"][:, :3])
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    assert np.allclose(got["n"][found], n, atol=1e-5)
+    d64, _ = O.closest_points_brute_f64(3, prims, R.make_spheres(sub[found], R.FLT_MAX))
+    assert relative_error(got["d"][found], d64).max() <= 1e-6
 
 
 def test_wide_after_refit(torus):
