@@ -20,6 +20,7 @@ SIGNATURES = {
     "fcpwgb_last_error": (C.c_char_p, []),
     "fcpwgb_version": (C.c_char_p, []),
     "fcpwgb_device_count": (c_int, []),
+    "fcpwgb_debug_fail_allocations": (c_int, [c_int, c_int]),
     "fcpwgb_cpu_bvh_build": (c_int, [c_int, P, c_uint32, P, c_uint32, c_int, c_int, C.POINTER(c_void_p)]),
     "fcpwgb_cpu_bvh_destroy": (None, [P]),
     "fcpwgb_cpu_bvh_info": (c_int, [P, P]),

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -27,6 +28,22 @@ namespace fcpwgb {
 int setError(int code, const std::string &msg) {
     g_lastError = msg;
     return code;
+}
+namespace {
+std::mutex gInjectMutex;
+int gSkipAllocs = 0, gFailAllocs = 0;
+}
+bool injectedAllocFailure() {
+    std::lock_guard<std::mutex> lock(gInjectMutex);
+    if (gSkipAllocs > 0) {
+        gSkipAllocs--;
+        return false;
+    }
+    if (gFailAllocs > 0) {
+        gFailAllocs--;
+        return true;
+    }
+    return false;
 }
 int cudaFail(cudaError_t e, const char *where) {
     return setError(e == cudaErrorMemoryAllocation ? FCPWGB_ERR_OUT_OF_MEMORY : FCPWGB_ERR_CUDA,
@@ -49,6 +66,14 @@ extern "C" int fcpwgb_device_count(void) {
         return 0;
     }
     return n;
+}
+
+extern "C" int fcpwgb_debug_fail_allocations(int skip, int count) {
+    if (skip < 0 || count < 0) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "negative allocation count");
+    std::lock_guard<std::mutex> lock(fcpwgb::gInjectMutex);
+    fcpwgb::gSkipAllocs = count > 0 ? skip : 0;
+    fcpwgb::gFailAllocs = count;
+    return FCPWGB_OK;
 }
 
 // ----------------------------------------------------------- CPU producer

@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(kWideBlock) kInstancedClosestPoint(
     if (q >= n) return;
     float4 s4 = ldg4(spheres + q);
     const float3 c = make_float3(s4.x, s4.y, s4.z);
-    float r2 = s4.w;
+    float r2 = queryRadius2(c, s4.w);
     DevInteraction best = defaultInteraction();
     uint32_t bestInst = kUintMax;
     if (nInstances == 1) {

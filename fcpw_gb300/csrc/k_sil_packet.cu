@@ -19,10 +19,10 @@
 // does not depend on which queries share a warp or on their order. (A wide
 // collapse of the tree would skip the cone tests of the collapsed binary
 // nodes, whose outcome is not monotone in floating point, so the packets
-// walk the binary nodes.) With a positive squared
-// minimum radius the reference stops at the first silhouette found within
-// it, which depends on its visiting order: that case stays on the binary
-// kernel (k_binary.cu).
+// walk the binary nodes.) With a positive squared minimum radius the
+// reference stops at the first silhouette found within it, which depends on
+// its visiting order: that case stays on the binary kernel (k_binary.cu). A
+// query whose centre is not finite gets the default record.
 #include "k_wide.cuh"
 #include "silhouette.cuh"
 
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
     if (valid) {
         const float4 s4 = ldg4(spheres + i);
         c = make_float3(s4.x, s4.y, s4.z);
-        r2 = s4.w;
+        r2 = queryRadius2(c, s4.w);
         flipNormal = __ldg(flip + slot) != 0;
     }
     DevInteraction best = defaultInteraction();

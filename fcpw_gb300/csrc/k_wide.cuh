@@ -267,6 +267,13 @@ FCPWGB_D float childD2Max(const WideNodeRegs<W, BITS> &node, float3 c, int k) {
 }
 
 constexpr uint32_t kLeafBit = 0x80000000u;
+
+// the search radius of a query: empty (-1) when its centre is not finite,
+// since the box distances drop NaN operands (max.f32) and would admit every
+// box; such a query gets the default record without walking the tree
+FCPWGB_D float queryRadius2(float3 c, float r2) {
+    return isfinite(c.x) && isfinite(c.y) && isfinite(c.z) ? r2 : -1.0f;
+}
 FCPWGB_D uint32_t packLeaf(uint32_t off, uint32_t cnt) { return kLeafBit | (cnt << 27) | off; }
 
 // a[slot] for a register array and a runtime slot < W: a binary tree of
@@ -647,9 +654,10 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
             uint32_t selected = kUintMax;
             uint32_t root = roots ? __ldg(roots + i) : 0u;
             NearTie<PRECISE> tie;
-            bool found = wideClosest<W, BITS, Prim, PRECISE, STATS, SHORT>(nodes, prims, root, c, s4.w, false, best, selected, tie,
+            const float r2 = queryRadius2(c, s4.w);
+            bool found = wideClosest<W, BITS, Prim, PRECISE, STATS, SHORT>(nodes, prims, root, c, r2, false, best, selected, tie,
                                                              st, errorWord, tExp, tTests);
-            finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, s4.w, found, selected, recordNormal, best, tie);
+            finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, r2, found, selected, recordNormal, best, tie);
         }
     } else {
         const uint32_t lane = threadIdx.x & 31u;
@@ -664,7 +672,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
             for (uint32_t i = b + lane; i < e; i += 32) {
                 float4 s4 = ldg4(spheres + i);
                 float3 c = make_float3(s4.x, s4.y, s4.z);
-                float r2 = s4.w;
+                float r2 = queryRadius2(c, s4.w);
+                const float r2User = r2;
                 DevInteraction best = defaultInteraction();
                 uint32_t selected = kUintMax;
                 uint32_t root = roots ? __ldg(roots + i) : 0u;
@@ -690,7 +699,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                                                             st, errorWord, tExp, tTests);
                 seed = found ? selected : kUintMax;
                 seedRoot = root;
-                finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, s4.w, found, selected, recordNormal, best, tie);
+                finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, r2User, found, selected, recordNormal, best, tie);
             }
         }
     }
@@ -736,7 +745,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
     if (valid) {
         float4 s4 = ldg4(spheres + i);
         c = make_float3(s4.x, s4.y, s4.z);
-        r2 = s4.w;
+        r2 = queryRadius2(c, s4.w);
         root = roots ? __ldg(roots + i) : 0u;
     }
     DevInteraction best = defaultInteraction();

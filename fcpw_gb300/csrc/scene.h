@@ -17,6 +17,8 @@ namespace fcpwgb {
 
 int setError(int code, const std::string &msg);
 int cudaFail(cudaError_t e, const char *where);
+// consumes one injected allocation failure (fcpwgb_debug_fail_allocations)
+bool injectedAllocFailure();
 
 // Grow-only device allocation owned by a scene.
 struct DeviceBuffer {
@@ -33,6 +35,8 @@ struct DeviceBuffer {
     }
     int ensure(size_t n) {
         if (n <= bytes) return 0;
+        if (injectedAllocFailure())
+            return setError(FCPWGB_ERR_OUT_OF_MEMORY, "cudaMalloc: injected allocation failure");
         release();
         cudaError_t e = cudaMalloc(&ptr, n);
         if (e != cudaSuccess) {

@@ -95,6 +95,13 @@ const char *fcpwgb_last_error(void);
 const char *fcpwgb_version(void);
 /* number of CUDA devices visible (0 when none); never fails */
 int fcpwgb_device_count(void);
+/* Testing aid, injected on the host: after the next `skip` growths of a
+ * device buffer succeed, the `count` growths after them fail with
+ * FCPWGB_ERR_OUT_OF_MEMORY without calling the allocator, leaving the buffer
+ * as it was ((0, 0) clears the injection). No device call is made or
+ * faulted. The reference has no counterpart (its allocation failures exit
+ * the process, slang_rhi_utils.h:51-59). */
+int fcpwgb_debug_fail_allocations(int skip, int count);
 
 /* ------------------------------------------------ CPU-side BVH producer
  * Builds the binary SAH BVH on the host exactly as the reference's
