@@ -270,9 +270,12 @@ constexpr uint32_t kLeafBit = 0x80000000u;
 
 // the search radius of a query: empty (-1) when its centre is not finite,
 // since the box distances drop NaN operands (max.f32) and would admit every
-// box; such a query gets the default record without walking the tree
+// box, or when the radius itself is NaN, which the first shrink to a child's
+// far distance (fminf drops NaN) would turn finite; such a query gets the
+// default record without walking the tree, as in the reference, whose root
+// test d2Min <= r2 fails for a NaN radius
 FCPWGB_D float queryRadius2(float3 c, float r2) {
-    return isfinite(c.x) && isfinite(c.y) && isfinite(c.z) ? r2 : -1.0f;
+    return isfinite(c.x) && isfinite(c.y) && isfinite(c.z) && r2 == r2 ? r2 : -1.0f;
 }
 FCPWGB_D uint32_t packLeaf(uint32_t off, uint32_t cnt) { return kLeafBit | (cnt << 27) | off; }
 
