@@ -13,8 +13,10 @@ namespace {
 
 constexpr int kRefineBlock = 256;
 
+// 3 blocks per SM (80 registers; the few spilled bytes sit around the FP64
+// fallback call): 0.05 ms faster on 4M queries than 2 blocks at 97 registers
 template<class Prim>
-__global__ void __launch_bounds__(kRefineBlock) kRefineClosest(const unsigned char *__restrict__ prims,
+__global__ void __launch_bounds__(kRefineBlock, 3) kRefineClosest(const unsigned char *__restrict__ prims,
                                                                const DevSphere *__restrict__ spheres,
                                                                const uint32_t *__restrict__ perm,
                                                                const uint2 *__restrict__ sel,
