@@ -1,7 +1,7 @@
 // Spatial reordering of query batches and record packing for the wide kernels.
 //
-// Queries (sphere centres, ray origins) are bucketed by a Morton-ordered cell of a 2^18-cell grid (64^3 in
-// 3D, 512^2 in 2D) and counting-sorted (histogram, exclusive scan, scatter).
+// Queries (sphere centres, ray origins) are bucketed by a Morton-ordered cell of a 128^3 grid in 3D (1024^2 in
+// 2D) and counting-sorted (histogram, exclusive scan, scatter).
 // The grid spans the bounding box of the batch's own query centres, clipped
 // to limits around the scene, so that cells are neither empty nor crowded
 // whatever the query distribution. Threads of a warp then traverse
@@ -18,15 +18,15 @@
 
 namespace fcpwgb {
 
-FCPWGB_D uint32_t spread3(uint32_t v) {  // 6 bits -> every third bit
-    v &= 0x3fu;
+FCPWGB_D uint32_t spread3(uint32_t v) {  // up to 8 bits -> every third bit
+    v &= 0xffu;
     v = (v | (v << 8)) & 0x0300f00fu;
     v = (v | (v << 4)) & 0x030c30c3u;
     v = (v | (v << 2)) & 0x09249249u;
     return v;
 }
-FCPWGB_D uint32_t spread2(uint32_t v) {  // 9 bits -> every second bit
-    v &= 0x1ffu;
+FCPWGB_D uint32_t spread2(uint32_t v) {  // up to 16 bits -> every second bit
+    v &= 0xffffu;
     v = (v | (v << 8)) & 0x00ff00ffu;
     v = (v | (v << 4)) & 0x0f0f0f0fu;
     v = (v | (v << 2)) & 0x33333333u;
@@ -47,7 +47,7 @@ struct CellGrid {
 
 // qb: ordered-int min[3], max[3] of the query centres
 FCPWGB_D CellGrid cellGrid(const SortLimits &lim, const int *qb) {
-    const float cells = lim.dim == 3 ? 64.0f : 512.0f;
+    const float cells = lim.dim == 3 ? 128.0f : 1024.0f;
     float lo[3] = {lim.lo.x, lim.lo.y, lim.lo.z}, hi[3] = {lim.hi.x, lim.hi.y, lim.hi.z}, inv[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -69,14 +69,14 @@ FCPWGB_D CellGrid cellGrid(const SortLimits &lim, const int *qb) {
 FCPWGB_D uint32_t cellOf(int dim, const CellGrid &g, float3 c) {
     if (dim == 3) {
         float fx = (c.x - g.lo.x) * g.inv.x, fy = (c.y - g.lo.y) * g.inv.y, fz = (c.z - g.lo.z) * g.inv.z;
-        uint32_t ix = (uint32_t)fminf(fmaxf(fx, 0.0f), 63.0f);
-        uint32_t iy = (uint32_t)fminf(fmaxf(fy, 0.0f), 63.0f);
-        uint32_t iz = (uint32_t)fminf(fmaxf(fz, 0.0f), 63.0f);
+        uint32_t ix = (uint32_t)fminf(fmaxf(fx, 0.0f), 127.0f);
+        uint32_t iy = (uint32_t)fminf(fmaxf(fy, 0.0f), 127.0f);
+        uint32_t iz = (uint32_t)fminf(fmaxf(fz, 0.0f), 127.0f);
         return spread3(ix) | (spread3(iy) << 1) | (spread3(iz) << 2);
     }
     float fx = (c.x - g.lo.x) * g.inv.x, fy = (c.y - g.lo.y) * g.inv.y;
-    uint32_t ix = (uint32_t)fminf(fmaxf(fx, 0.0f), 511.0f);
-    uint32_t iy = (uint32_t)fminf(fmaxf(fy, 0.0f), 511.0f);
+    uint32_t ix = (uint32_t)fminf(fmaxf(fx, 0.0f), 1023.0f);
+    uint32_t iy = (uint32_t)fminf(fmaxf(fy, 0.0f), 1023.0f);
     return spread2(ix) | (spread2(iy) << 1);
 }
 
