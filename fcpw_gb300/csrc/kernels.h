@@ -95,7 +95,7 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
                                               uint32_t *errorWord, cudaStream_t s);
 
 // query reordering and record packing (k_sort.cu)
-constexpr uint32_t kSortCellBits = 21;  // 2^21 cells: 128^3 in 3D, 1024^2 (2^20) in 2D
+constexpr uint32_t kSortCellBits = 21;  // up to 2^21 cells: 128^3 in 3D (512^2 in 2D)
 constexpr uint32_t kSortCells = 1u << kSortCellBits;
 // the sort grid spans the query bounds clipped to [lo, hi]
 struct SortLimits { float3 lo; float3 hi; int dim; };
