@@ -156,8 +156,12 @@ int ensureForest(fcpwgb_gpu_batch *b) {
     return FCPWGB_OK;
 }
 
-// per-scene sort grids sized by the scene's query count (about 16 queries a
-// cell), over the scene box grown by its largest extent on every side
+// per-scene sort grids sized by the scene's query count (about 2 queries a
+// cell of the grid, which spans the scene box grown by its largest extent on
+// every side, so a few more per cell where the queries are), at most 2^8
+// cells per axis in 3D and 2^12 in 2D; fine cells keep the queries of a warp
+// packet close together. The density halves until the cells of all scenes
+// fit kMaxBatchCells.
 int ensureLayout(fcpwgb_gpu_batch *b, const uint32_t *offsets, uint32_t nOffsets) {
     const uint32_t nS = (uint32_t)b->scenes.size();
     if (!offsets || nOffsets != nS + 1)
@@ -171,12 +175,23 @@ int ensureLayout(fcpwgb_gpu_batch *b, const uint32_t *offsets, uint32_t nOffsets
             return setError(FCPWGB_ERR_INVALID_ARGUMENT, "query_offsets must be non-decreasing");
     const uint32_t n = offsets[nS];
     std::vector<BatchSceneGrid> grids(nS);
+    const int maxBits = b->dim == 3 ? 8 : 12;
+    std::vector<int> bits(nS);
     uint64_t cellBase = 0;
-    const int maxBits = b->dim == 3 ? 6 : 9;
+    for (uint64_t per = 2;; per *= 2) {
+        cellBase = 0;
+        for (uint32_t s = 0; s < nS; s++) {
+            const uint64_t nq = offsets[s + 1] - offsets[s];
+            int k = 0;
+            while (k < maxBits && (per << (b->dim * (k + 1))) <= nq) k++;
+            bits[s] = k;
+            cellBase += (uint64_t)1 << (b->dim * k);
+        }
+        if (cellBase <= kMaxBatchCells || per > (1ull << 32)) break;  // one cell a scene: checked below
+    }
+    cellBase = 0;
     for (uint32_t s = 0; s < nS; s++) {
-        uint32_t nq = offsets[s + 1] - offsets[s];
-        int bitsPerAxis = 0;
-        while (bitsPerAxis < maxBits && ((uint64_t)16 << (b->dim * (bitsPerAxis + 1))) <= nq) bitsPerAxis++;
+        const int bitsPerAxis = bits[s];
         const float *bx = b->scenes[s].box;
         float ext = 1e-6f;
         for (int a = 0; a < b->dim; a++) ext = std::max(ext, bx[3 + a] - bx[a]);
