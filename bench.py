@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven scenes measurement")
     ap.add_argument("--suite", action="store_true",
                     help="instead of the headline line, one line per other configuration of the scope")
-    ap.add_argument("--only", default="", help="with --suite: comma-separated subset of c1,rays,c3,sil3d,inside,instanced,build")
+    ap.add_argument("--only", default="",
+                    help="with --suite: comma-separated subset of c1,rays,c3,sil3d,inside,instanced,build,batch")
     return ap.parse_args()
 
 
@@ -564,6 +565,10 @@ def run_suite(args):
                       "gpu_lbvh_build_and_transfer_s": t_lbvh, "speedup_lbvh": (t_host + t_transfer) / t_lbvh,
                       "host_tree_nodes": g.info()["n_nodes"], "lbvh_tree_nodes": gl.info()["n_nodes"]})
         del g, gl, gs, s
+
+    # the 512-mesh batch alone (also part of the headline line)
+    if want("batch") and only is not None:
+        lines.append({"config": "batched uneven scenes", **batched_scenes_bench(0)})
 
     for line in lines:
         print(json.dumps(line), flush=True)
