@@ -91,6 +91,24 @@ FCPWGB_D float3 recordPosition(const DevRay *q, uint32_t i) {  // 40 B records: 
     float2 a = ldg2(p), b = ldg2(p + 8);
     return make_float3(a.x, a.y, b.x);
 }
+// the sort cell of a record: a sphere by its centre; a ray by the octant of
+// its direction first (the rays of a warp then share their near-child
+// order), then the Morton cell of its origin on a grid half as fine per axis
+// (64^3 in 3D, 256^2 in 2D), so that both fit the cells of a sphere grid
+FCPWGB_D uint32_t recordCell(int dim, const CellGrid &g, const DevSphere *q, uint32_t i) {
+    return cellOf(dim, g, recordPosition(q, i));
+}
+FCPWGB_D uint32_t recordCell(int dim, const CellGrid &g, const DevRay *q, uint32_t i) {
+    const unsigned char *p = reinterpret_cast<const unsigned char *>(q + i);
+    const float2 a = ldg2(p), b = ldg2(p + 8), c = ldg2(p + 16);  // (o.x, o.y), (o.z, d.x), (d.y, d.z)
+    const uint32_t oct = (b.y < 0.0f ? 1u : 0u) | (c.x < 0.0f ? 2u : 0u) | (dim == 3 && c.y < 0.0f ? 4u : 0u);
+    if (dim == 3) {
+        const uint32_t m = cellOf(3, g, make_float3(a.x, a.y, b.x));  // 21 bits: x, y, z interleaved
+        return (oct << 18) | (m >> 3);                                 // drop each axis's lowest bit
+    }
+    const uint32_t m = cellOf(2, g, make_float3(a.x, a.y, 0.0f));     // 18 bits
+    return (oct << 16) | (m >> 2);
+}
 FCPWGB_D void copyRecord(const DevSphere *q, uint32_t i, DevSphere *dst, uint32_t j) {
     reinterpret_cast<float4 *>(dst)[j] = ldg4(q + i);
 }
@@ -163,7 +181,7 @@ __global__ void kCellHistogram(SortLimits lim, const int *qb, const Rec *__restr
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     CellGrid g = cellGrid(lim, qb);
-    atomicAdd(cells + cellOf(lim.dim, g, recordPosition(q, i)), 1u);
+    atomicAdd(cells + recordCell(lim.dim, g, q, i), 1u);
 }
 
 template<class Rec>
@@ -172,7 +190,7 @@ __global__ void kScatterQueries(SortLimits lim, const int *qb, const Rec *__rest
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     CellGrid g = cellGrid(lim, qb);
-    uint32_t pos = atomicAdd(cells + cellOf(lim.dim, g, recordPosition(q, i)), 1u);
+    uint32_t pos = atomicAdd(cells + recordCell(lim.dim, g, q, i), 1u);
     copyRecord(q, i, sorted, pos);
     perm[pos] = i;
 }
