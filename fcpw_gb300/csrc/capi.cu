@@ -1061,8 +1061,7 @@ extern "C" int fcpwgb_contains_device(fcpwgb_gpu_scene *s, const fcpwgb_float3 *
     int rc = requireTree(s);
     if (rc) return rc;
     if (n > 0 && (!points || !result)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL point or result array");
-    FCPWGB_CUDA(launchContains(s->view(), (const float *)points, n, result, s->pick(stream)));
-    return FCPWGB_OK;
+    return s->containsPoints((const float *)points, n, result, s->pick(stream));
 }
 
 extern "C" int fcpwgb_contains(fcpwgb_gpu_scene *s, const fcpwgb_float3 *points, uint32_t n, uint32_t *result) {
@@ -1073,7 +1072,7 @@ extern "C" int fcpwgb_contains(fcpwgb_gpu_scene *s, const fcpwgb_float3 *points,
     HostQuery h{s};
     size_t ob = (size_t)n * sizeof(uint32_t);
     if ((rc = h.begin(points, (size_t)n * 12, nullptr, 0, ob))) return rc;
-    FCPWGB_CUDA(launchContains(s->view(), (const float *)s->qIn0.ptr, n, (uint32_t *)s->qOut.ptr, s->stream));
+    if ((rc = s->containsPoints((const float *)s->qIn0.ptr, n, (uint32_t *)s->qOut.ptr, s->stream))) return rc;
     return h.finish(result, ob);
 }
 

@@ -175,22 +175,34 @@ FCPWGB_D int hitCount(const unsigned char *__restrict__ nodes, const unsigned ch
     return count;
 }
 
+// point q at points[stride * q] (3 floats, or the first 3 of a 16 B record);
+// with perm non-NULL the points are in sorted order and the answer goes to
+// the caller's slot perm[q]
 template<int DIM, int NODE_STRIDE>
 __global__ void __launch_bounds__(128) kContains(const unsigned char *__restrict__ nodes,
                                                  const unsigned char *__restrict__ prims,
-                                                 const float *__restrict__ points, uint32_t n, uint32_t *out,
+                                                 const float *__restrict__ points, uint32_t stride,
+                                                 const uint32_t *__restrict__ perm, uint32_t n, uint32_t *out,
                                                  uint32_t *errorWord) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    float3 x = make_float3(points[3 * q], points[3 * q + 1], DIM == 3 ? points[3 * q + 2] : 0.0f);
+    const float *pq = points + (size_t)stride * q;
+    float3 x = make_float3(pq[0], pq[1], DIM == 3 ? pq[2] : 0.0f);
+    const uint32_t slot = perm ? __ldg(perm + q) : q;
     int h1 = hitCount<DIM, NODE_STRIDE>(nodes, prims, xray(DIM, x, make_float3(1.0f, 0.0f, 0.0f), kFltMax));
     int h2 = hitCount<DIM, NODE_STRIDE>(nodes, prims, xray(DIM, x, make_float3(0.0f, 1.0f, 0.0f), kFltMax));
     if (h1 < 0 || h2 < 0) {
         atomicOr(errorWord, kErrStepBudget);
-        out[q] = 2u;
+        out[slot] = 2u;
         return;
     }
-    out[q] = (h1 % 2 == 1 && h2 % 2 == 1) ? 1u : 0u;
+    out[slot] = (h1 % 2 == 1 && h2 % 2 == 1) ? 1u : 0u;
+}
+
+// points (3 floats each) as 16 B sphere records, the input of the query sort
+__global__ void kPackPoints(const float *__restrict__ points, uint32_t n, float4 *__restrict__ out) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_float4(points[3 * i], points[3 * i + 1], points[3 * i + 2], 0.0f);
 }
 
 template<int DIM, int NODE_STRIDE>
@@ -261,16 +273,23 @@ __global__ void __launch_bounds__(128) kLineOfSight(const unsigned char *__restr
 
 }  // namespace
 
-cudaError_t launchContains(const SceneView &v, const float *points, uint32_t n, uint32_t *out, cudaStream_t s) {
+cudaError_t launchContains(const SceneView &v, const float *points, uint32_t stride, const uint32_t *perm,
+                           uint32_t n, uint32_t *out, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     dim3 g((n + 127) / 128), b(128);
     if (v.dim == 3) {
-        if (v.snch) kContains<3, 64><<<g, b, 0, s>>>(v.nodes, v.prims, points, n, out, v.errorWord);
-        else kContains<3, 32><<<g, b, 0, s>>>(v.nodes, v.prims, points, n, out, v.errorWord);
+        if (v.snch) kContains<3, 64><<<g, b, 0, s>>>(v.nodes, v.prims, points, stride, perm, n, out, v.errorWord);
+        else kContains<3, 32><<<g, b, 0, s>>>(v.nodes, v.prims, points, stride, perm, n, out, v.errorWord);
     } else {
-        if (v.snch) kContains<2, 64><<<g, b, 0, s>>>(v.nodes, v.prims, points, n, out, v.errorWord);
-        else kContains<2, 32><<<g, b, 0, s>>>(v.nodes, v.prims, points, n, out, v.errorWord);
+        if (v.snch) kContains<2, 64><<<g, b, 0, s>>>(v.nodes, v.prims, points, stride, perm, n, out, v.errorWord);
+        else kContains<2, 32><<<g, b, 0, s>>>(v.nodes, v.prims, points, stride, perm, n, out, v.errorWord);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launchPackPoints(const float *points, uint32_t n, DevSphere *out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    kPackPoints<<<(n + 255) / 256, 256, 0, s>>>(points, n, reinterpret_cast<float4 *>(out));
     return cudaGetLastError();
 }
 

@@ -37,7 +37,10 @@ cudaError_t launchFillDefault(DevInteraction *out, uint32_t n, cudaStream_t s);
 
 // Scene::contains and hasLineOfSight with the reference CPU arithmetic (k_inside.cu);
 // points are 3 floats each, results 0 / 1 (contains: 2 when a ray had too many hits)
-cudaError_t launchContains(const SceneView &v, const float *points, uint32_t n, uint32_t *out, cudaStream_t s);
+// points at points[stride * q]; perm non-NULL: points in sorted order, answers to out[perm[q]]
+cudaError_t launchContains(const SceneView &v, const float *points, uint32_t stride, const uint32_t *perm,
+                           uint32_t n, uint32_t *out, cudaStream_t s);
+cudaError_t launchPackPoints(const float *points, uint32_t n, DevSphere *out, cudaStream_t s);
 cudaError_t launchLineOfSight(const SceneView &v, const float *a, const float *b, uint32_t n, uint32_t *out,
                               cudaStream_t s);
 

@@ -237,6 +237,31 @@ int GpuScene::closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_in
     return 0;
 }
 
+int GpuScene::containsPoints(const float *points, uint32_t n, uint32_t *result, cudaStream_t st) {
+    cudaError_t e;
+    if (useWide() && wideConfig.sortQueries && n >= 4096) {
+        // the rays of contains go along +x and +y from every point: sorted points
+        // walk the tree alike; each point's answer is unchanged
+        int rc;
+        if ((rc = packedPoints.ensure((size_t)n * sizeof(DevSphere))) ||
+            (rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords)) ||
+            (rc = sortPerm.ensure((size_t)n * sizeof(uint32_t))) ||
+            (rc = sortSpheres.ensure((size_t)n * sizeof(DevSphere))))
+            return rc;
+        if ((e = launchPackPoints(points, n, (DevSphere *)packedPoints.ptr, st)) != cudaSuccess)
+            return cudaFail(e, "pack points");
+        if ((e = launchSortQueries(sortLimits(), (const DevSphere *)packedPoints.ptr, n, (uint32_t *)sortCells.ptr,
+                                   (DevSphere *)sortSpheres.ptr, (uint32_t *)sortPerm.ptr, smCount(), st)) != cudaSuccess)
+            return cudaFail(e, "sort points");
+        if ((e = launchContains(view(), (const float *)sortSpheres.ptr, 4, (const uint32_t *)sortPerm.ptr, n, result,
+                                st)) != cudaSuccess)
+            return cudaFail(e, "contains");
+        return 0;
+    }
+    if ((e = launchContains(view(), points, 3, nullptr, n, result, st)) != cudaSuccess) return cudaFail(e, "contains");
+    return 0;
+}
+
 int GpuScene::afterRefit(cudaStream_t st) {
     if (!wide.valid) return 0;
     cudaError_t e;

@@ -82,7 +82,7 @@ struct GpuScene {
     DeviceBuffer wideNodes, wideChildBinary, widePrims;
     // scratch of the fast path: query sort cells / permutation / sorted copy, work counter,
     // precise mode's winner and runner-up leaf positions
-    DeviceBuffer sortCells, sortPerm, sortSpheres, sortRays, workCounter, refineSel;
+    DeviceBuffer sortCells, sortPerm, sortSpheres, sortRays, workCounter, refineSel, packedPoints;
     int numSMs = 0;
 
     // optional event timing of traversal launches
@@ -121,6 +121,8 @@ struct GpuScene {
     int closestPointsStats(const DevSphere *spheres, DevInteraction *out, uint32_t n, unsigned long long *stats,
                            cudaStream_t st);
     int rays(const DevRay *rays, DevInteraction *out, uint32_t n, int occl, cudaStream_t st);
+    // contains: points sorted spatially first with a fast-path configuration
+    int containsPoints(const float *points, uint32_t n, uint32_t *result, cudaStream_t st);
     int closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_interaction *out, uint32_t n,
                           int recordNormal);
     // keeps derived trees in step after the binary tree was refit on stream st

@@ -353,4 +353,12 @@ def test_contains_and_line_of_sight_match_oracle(dim):
     torch.cuda.synchronize()
     assert np.array_equal(t_in.cpu().numpy().astype(np.uint32), inside)
     assert np.array_equal(t_los.cpu().numpy().astype(np.uint32), los)
+    # with a fast-path configuration the points are sorted spatially first:
+    # the same answers, in the caller's order, from the host and device entries
+    g.set_traversal(4, 32, sort_queries=True)
+    assert np.array_equal(g.contains(a), inside)
+    t_in2 = g.contains_tensor(pa)
+    torch.cuda.synchronize()
+    assert np.array_equal(t_in2.cpu().numpy().astype(np.uint32), inside)
+    g.set_traversal(0)
     assert g.check_errors() == 0
