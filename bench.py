@@ -774,7 +774,7 @@ def run_ours(args):
     plain_ms, plain_kms = timed(max(3, args.steps // 4), 2)
     plain_stats = traversal_stats(32, 40, 16)
 
-    # 2) fast path: wide tree with quantised child boxes, queries sorted, persistent blocks, FP64 final distance
+    # 2) fast path: wide tree with quantised child boxes, queries sorted, persistent blocks, refined final distance
     sample = spheres[: min(n, 1 << 20)]
     if args.variant == "auto":
         best, table = autotune_closest_points(gpu, sample)

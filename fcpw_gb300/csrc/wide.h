@@ -26,7 +26,7 @@ struct WideConfig {
     int blockSize = 128; // threads per block
     int sortQueries = 1; // reorder queries by spatial cell before traversal
     int persistent = 1;  // persistent blocks fetching query chunks from a work counter
-    int precise = 1;     // recompute the winning primitive's distance in FP64
+    int precise = 1;     // refine the winning primitive's distance to within 1e-6 of FP64
     int packet = 0;      // traverse the 32 queries of a warp as one packet
     int leafSize = 0;    // > 0: binary subtrees of at most this many primitives collapse into one leaf
     int shortStack = 16; // traversal stack entries per thread in shared memory (thread schedules): 0 or 16

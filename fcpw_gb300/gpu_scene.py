@@ -207,8 +207,11 @@ class _GPUScene:
         """Selects the closest point traversal (see fcpwgb_traversal_config):
         branching 0 is the reference-order binary traversal; 2/4/8 use a wide
         tree with 32-, 16- or 8-bit child boxes; packet walks the queries of a
-        warp together; leaf_size merges small subtrees into wide leaves;
-        short_stack (0 or 16) is the per-thread stack depth kept in shared memory."""
+        warp together; precise refines distances to within 1e-6 of FP64;
+        leaf_size merges small subtrees into wide leaves; short_stack (0 or 16)
+        is the per-thread stack depth kept in shared memory. With branching
+        > 0, silhouette queries use warp packets and contains and rays are
+        sorted spatially (sort_queries)."""
         from ._lib import TraversalConfig
         cfg = TraversalConfig(int(branching), int(bits), 128, int(bool(sort_queries)), int(bool(persistent)),
                               int(bool(precise)), int(bool(packet)), int(leaf_size), int(short_stack))

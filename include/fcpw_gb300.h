@@ -305,7 +305,11 @@ int fcpwgb_gpu_scene_update_vertices_device_static(fcpwgb_gpu_scene *scene, cons
  * are stored in 32-bit floats or conservatively quantised to 16 or 8 bits;
  * sort_queries reorders each batch spatially before traversal, persistent
  * runs one resident block set that fetches query chunks from a counter, and
- * precise recomputes the winning primitive's distance and point in FP64;
+ * precise recomputes the winning primitive's distance and point (and the
+ * runner-up's within the FP32 rounding band) to within 1e-6 of FP64:
+ * double-single arithmetic, FP64 where the projection is ill-conditioned;
+ * for triangles in a second kernel after the traversal, for segments at its
+ * end;
  * packet traverses the 32 (sorted) queries of a warp together, one record
  * load per warp and step, each query pruning with its own radius (persistent
  * is then ignored); leaf_size > 0 collapses binary subtrees of at most that
@@ -314,7 +318,10 @@ int fcpwgb_gpu_scene_update_vertices_device_static(fcpwgb_gpu_scene *scene, cons
  * one-thread-per-query schedules (0 or 16; the others in local memory).
  * Defaults: {0, 32, 128, 1, 1, 1, 0, 0, 16}. Results differ from the binary
  * order only on equidistant ties (and, with precise, by the FP32 rounding
- * removed). */
+ * removed). With branching > 0, closest silhouette points are answered by
+ * warp packets on the binary SNCH tree (unless squared_min_radius > 0),
+ * contains sorts its points spatially (sort_queries), and rays are sorted by
+ * direction octant, then origin (sort_queries). */
 typedef struct {
     int branching;     /* 0, 2, 4 or 8 */
     int bits;          /* 32, 16 or 8 */
