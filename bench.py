@@ -382,21 +382,24 @@ def run_suite(args):
         ray_ms = timed(ray_run)
         hits = float((out[:, 9].view(torch.int32) != -1).float().mean())
         table = []
-        for wb in [(2, 32, True), (4, 8, True), (4, 16, True), (4, 32, True), (4, 32, False), (8, 8, True),
-                   (8, 16, True), (8, 32, True)]:
-            g.set_traversal(*wb[:2], sort_queries=wb[2])
+        for wb in [(2, 32, True, False), (4, 8, True, False), (4, 16, True, False), (4, 32, True, False),
+                   (4, 32, False, False), (8, 8, True, False), (8, 16, True, False), (8, 32, True, False),
+                   (2, 32, True, True), (4, 8, True, True), (4, 32, True, True), (8, 32, True, True)]:
+            g.set_traversal(*wb[:2], sort_queries=wb[2], packet=wb[3])
             table.append((wb, timed(ray_run, reps=3)))
         (wb_best, _) = min(table, key=lambda t: t[1])
-        g.set_traversal(*wb_best[:2], sort_queries=wb_best[2])
+        g.set_traversal(*wb_best[:2], sort_queries=wb_best[2], packet=wb_best[3])
         fast_ms = timed(ray_run)
         nodes, prims, _ = s.cpu_bvh.export()
         cpu = cpu_rate(lambda m: O.intersect_rays_bvh(3, nodes, prims, rays_np[:m], nthreads=threads), n)
         lines.append({"config": "rays, torus 1,048,576 triangles, 4,194,304 rays (first hit)", "queries": n,
                       "plain": {"queries_per_s": n / (ray_ms / 1e3), "ms": ray_ms},
                       "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms,
-                               "variant": {"branching": wb_best[0], "bits": wb_best[1], "sort_queries": wb_best[2]}},
+                               "variant": {"branching": wb_best[0], "bits": wb_best[1], "sort_queries": wb_best[2],
+                                           "packet": wb_best[3]}},
                       "speedup_vs_plain": ray_ms / fast_ms, "hit_fraction": hits,
-                      "autotune_ms": [[w, b, int(o), round(t, 3)] for (w, b, o), t in table], "cpu_baseline": cpu})
+                      "autotune_ms": [[w, b, int(o), int(pk), round(t, 3)] for (w, b, o, pk), t in table],
+                      "cpu_baseline": cpu})
         del g, s
 
     # C3: 256 star polylines x 512 segments, 8,388,608 queries in [-3, 3]^2: closest point and silhouettes

@@ -1017,6 +1017,165 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
     }
 }
 
+// Ray packets: the 32 (sorted) rays of a warp walk the wide tree together,
+// as kWidePacketClosestPoint does for closest points. Each record is loaded
+// once for the warp; every lane slab-tests its own ray against every child
+// (within its own tMax) and takes part in a child only while the child's
+// entry distance is within its tMax, re-checked when the entry is popped;
+// children go in the order of the first active lane's entry distances. A
+// hit shrinks the lane's tMax; an occlusion ray leaves the packet at its
+// first hit. Rays sorted by direction octant and origin keep the lanes'
+// paths alike.
+template<int W, int BITS, class Prim>
+__global__ void __launch_bounds__(kWideBlock, 8) kWidePacketRay(const unsigned char *__restrict__ nodes,
+                                                             const unsigned char *__restrict__ prims,
+                                                             const DevRay *__restrict__ rays,
+                                                             const uint32_t *__restrict__ perm,
+                                                             DevInteraction *__restrict__ out, uint32_t n, int occl,
+                                                             uint32_t *errorWord, unsigned long long *stats) {
+    constexpr uint32_t kSlotMask = W - 1;
+    constexpr int kWarps = kWideBlock / 32;
+    __shared__ uint32_t sRef[kWarps][kPacketShort];
+    __shared__ float sDist[kWarps][kPacketShort][32];
+    uint32_t lRef[kWideStack - kPacketShort];
+    float lDist[kWideStack - kPacketShort];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
+    const bool valid = i < n;
+    DevRay r;
+    r.o = r.d = r.dInv = make_float3(0.0f, 0.0f, 0.0f);
+    r.tMax = -1.0f;  // a lane without a ray needs nothing
+    if (valid) {
+        const unsigned char *rp = reinterpret_cast<const unsigned char *>(rays + i);
+        float2 a = ldg2(rp), b = ldg2(rp + 8), cc = ldg2(rp + 16), d = ldg2(rp + 24), e = ldg2(rp + 32);
+        r.o = make_float3(a.x, a.y, b.x);
+        r.d = make_float3(b.y, cc.x, cc.y);
+        r.dInv = make_float3(d.x, d.y, e.x);
+        r.tMax = e.y;
+    }
+    DevInteraction best = defaultInteraction();
+    uint32_t tExp = 0, tTests = 0;
+    WideNodeRegs<W, BITS> node;
+    bool act = valid;
+    uint32_t cur = 0;
+    int sp = 0;  // warp-uniform
+    if (__ballot_sync(0xffffffffu, act)) {
+        for (;;) {
+            bool descend = false;
+            if (!(cur & kLeafBit)) {
+                node.load(nodes, cur);
+                if (act) tExp++;
+                float t0[W];
+                uint32_t needMask = 0;
+#pragma unroll
+                for (int k = 0; k < W; k++) {
+                    float a0, a1;
+                    const bool hit =
+                        act && node.cnt(k) != kWideEmpty &&
+                        boxRayIntersect(make_float3(node.bound(0, k), node.bound(1, k), node.bound(2, k)),
+                                        make_float3(node.bound(3, k), node.bound(4, k), node.bound(5, k)), r, a0, a1);
+                    // entry distances are >= 0 (+ 0 turns a -0 into +0); NaN where this lane misses
+                    t0[k] = hit ? a0 + 0.0f : __int_as_float(0x7fc00000);
+                    needMask |= hit ? (1u << k) : 0u;
+                }
+                const uint32_t anyMask = __reduce_or_sync(0xffffffffu, needMask);
+                const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
+                uint32_t key[W];
+#pragma unroll
+                for (int k = 0; k < W; k++) {
+                    // a child the leader misses sorts after the ones it enters (NaN bits)
+                    const float lead = __shfl_sync(0xffffffffu, t0[k], leader);
+                    key[k] = ((anyMask >> k) & 1u) ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
+                }
+                const int nh = __popc(anyMask);
+                sortNetwork<W>(key);
+                if (nh > 0) {
+                    if (sp + nh - 1 > kWideStack) {
+                        if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
+                        break;
+                    }
+                    uint32_t rawRefs[W];
+#pragma unroll
+                    for (int s = 0; s < W; s++) rawRefs[s] = node.ref(s);
+#pragma unroll
+                    for (int k = W - 1; k >= 0; k--) {
+                        if (k < nh) {
+                            const uint32_t slot = key[k] & kSlotMask;
+                            const uint32_t cnt = node.cntAt(slot);
+                            const uint32_t ref = selectBySlot<W>(rawRefs, slot);
+                            const uint32_t packed = cnt == 0 ? ref : packLeaf(ref, cnt);
+                            const float dl = selectBySlot<W>(t0, slot);
+                            if (k == 0) {
+                                cur = packed;
+                                act = dl <= r.tMax;
+                            } else {
+                                if (sp < kPacketShort) {
+                                    if (lane == 0) sRef[warp][sp] = packed;
+                                    sDist[warp][sp][lane] = dl;
+                                } else {
+                                    lRef[sp - kPacketShort] = packed;
+                                    lDist[sp - kPacketShort] = dl;
+                                }
+                                sp++;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                    descend = true;
+                }
+            } else {
+                const uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+                if (act) tTests += cnt;
+                for (uint32_t p = 0; p < cnt; p++) {
+                    const Prim prim = Prim::load(prims, off + p);
+                    if (act) {
+                        DevInteraction c = defaultInteraction();
+                        if (prim.intersect(r, occl != 0, c)) {
+                            c.index = prim.index;
+                            if (occl) {
+                                best.index = c.index;
+                                act = false;
+                                r.tMax = -1.0f;  // done: no entry is within it
+                            } else {
+                                r.tMax = fminf(r.tMax, c.d);
+                                best = c;
+                            }
+                        }
+                    }
+                }
+            }
+            if (descend) continue;
+            // pop until some lane needs the entry
+            bool next = false;
+            while (sp > 0) {
+                sp--;
+                uint32_t ref;
+                float dl;
+                if (sp < kPacketShort) {
+                    ref = sRef[warp][sp];
+                    dl = sDist[warp][sp][lane];
+                } else {
+                    ref = lRef[sp - kPacketShort];
+                    dl = lDist[sp - kPacketShort];
+                }
+                act = dl <= r.tMax;
+                if (__ballot_sync(0xffffffffu, act)) {
+                    cur = ref;
+                    next = true;
+                    break;
+                }
+            }
+            __syncwarp();
+            if (!next) break;
+        }
+    }
+    if (valid) out[perm ? __ldg(perm + i) : i] = best;
+    if (stats && valid) {
+        atomicAdd(stats + 1, (unsigned long long)tExp);
+        atomicAdd(stats + 2, (unsigned long long)tTests);
+    }
+}
+
 // Re-quantises every wide node from the (refit) binary boxes behind its slots.
 template<int W, int BITS>
 __global__ void kRequantize(unsigned char *wideNodes, const int32_t *childBinary, const unsigned char *binNodes,
@@ -1109,13 +1268,13 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
             kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.errorWord, l.stats);     \
         };                                                                                                         \
         if (dim == 3) {                                                                                            \
-            if (bits == 8) go(kWideRay<W, 8, Tri48Prim>);                                                          \
-            else if (bits == 16) go(kWideRay<W, 16, Tri48Prim>);                                                   \
-            else go(kWideRay<W, 32, Tri48Prim>);                                                                   \
+            if (bits == 8) l.packet ? go(kWidePacketRay<W, 8, Tri48Prim>) : go(kWideRay<W, 8, Tri48Prim>);         \
+            else if (bits == 16) l.packet ? go(kWidePacketRay<W, 16, Tri48Prim>) : go(kWideRay<W, 16, Tri48Prim>); \
+            else l.packet ? go(kWidePacketRay<W, 32, Tri48Prim>) : go(kWideRay<W, 32, Tri48Prim>);                 \
         } else {                                                                                                   \
-            if (bits == 8) go(kWideRay<W, 8, Seg24Prim>);                                                          \
-            else if (bits == 16) go(kWideRay<W, 16, Seg24Prim>);                                                   \
-            else go(kWideRay<W, 32, Seg24Prim>);                                                                   \
+            if (bits == 8) l.packet ? go(kWidePacketRay<W, 8, Seg24Prim>) : go(kWideRay<W, 8, Seg24Prim>);         \
+            else if (bits == 16) l.packet ? go(kWidePacketRay<W, 16, Seg24Prim>) : go(kWideRay<W, 16, Seg24Prim>); \
+            else l.packet ? go(kWidePacketRay<W, 32, Seg24Prim>) : go(kWideRay<W, 32, Seg24Prim>);                 \
         }                                                                                                          \
         return cudaGetLastError();                                                                                 \
     }                                                                                                              \

@@ -88,6 +88,7 @@ struct WideRayLaunch {
     DevInteraction *out = nullptr;
     uint32_t n = 0;
     int occl = 0;
+    int packet = 0;                         // 1: warp packets (kWidePacketRay)
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;
 };

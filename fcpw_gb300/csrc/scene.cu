@@ -149,6 +149,7 @@ int GpuScene::wideRays(const DevRay *r, DevInteraction *out, uint32_t n, int occ
     l.out = out;
     l.n = n;
     l.occl = occl;
+    l.packet = wideConfig.packet;
     l.errorWord = (uint32_t *)errorWord.ptr;
     cudaError_t e;
     if (wideConfig.sortQueries && n >= 4096) {

@@ -178,8 +178,10 @@ def _ray_check(got, ref_out, ref_hit, occl=False):
 
 @pytest.mark.parametrize("branching", [2, 4, 8])
 @pytest.mark.parametrize("bits", [32, 16, 8])
-def test_wide_rays_match_oracle(torus, branching, bits):
-    """Rays on the wide trees (sorted by origin) against the reference CPU order."""
+@pytest.mark.parametrize("packet", [False, True])
+def test_wide_rays_match_oracle(torus, branching, bits, packet):
+    """Rays on the wide trees (sorted by direction octant and origin), one
+    thread per ray or warp packets, against the reference CPU order."""
     s, g, pts, ref, prims = torus
     n = 60000
     o = W.uniform_points(n, 3, -2, 2, 51)
@@ -187,7 +189,7 @@ def test_wide_rays_match_oracle(torus, branching, bits):
     tmax = np.full(n, R.FLT_MAX, np.float32)
     nodes, _, _ = s.cpu_bvh.export()
     ref_out, ref_hit = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax))
-    g.set_traversal(branching, bits, sort_queries=True)
+    g.set_traversal(branching, bits, sort_queries=True, packet=packet)
     out = F.GPUInteractionList()
     g.intersect(o, d, tmax, out)
     _ray_check(out.array(), ref_out, ref_hit)
@@ -209,11 +211,17 @@ def test_wide_rays_finite_tmax_unsorted_and_2d():
     tmax = W.rng(56).uniform(0.1, 3.0, n).astype(np.float32)
     nodes, prims, _ = s.cpu_bvh.export()
     ref_out, ref_hit = O.intersect_rays_bvh(2, nodes, prims, R.make_rays(o, d, tmax))
-    for cfg in [(4, 8, True), (8, 16, False), (2, 32, True)]:
-        g.set_traversal(cfg[0], cfg[1], sort_queries=cfg[2])
+    for cfg in [(4, 8, True, False), (8, 16, False, False), (2, 32, True, False), (4, 32, True, True),
+                (8, 8, False, True)]:
+        g.set_traversal(cfg[0], cfg[1], sort_queries=cfg[2], packet=cfg[3])
         out = F.GPUInteractionList()
         g.intersect(o, d, tmax, out)
         _ray_check(out.array(), ref_out, ref_hit)
+        occ = F.GPUInteractionList()
+        g.intersect(o, d, tmax, occ, True)
+        ref2, hit2 = O.intersect_rays_bvh(2, nodes, prims, R.make_rays(o, d, tmax), occlusion=True)
+        _ray_check(occ.array(), ref2, hit2, occl=True)
+    assert g.check_errors() == 0
 
 
 @pytest.mark.parametrize("packet", [False, True])
