@@ -103,6 +103,16 @@ FCPWGB_D NodeBox loadNode(const unsigned char *nodes, uint32_t i) {
     n.offset = __float_as_uint(b.w);
     return n;
 }
+// The query sort's verdict on a batch of rays (k_sort.cu): sortInfo[6] counts
+// how many of up to kCoherenceSamples evenly spaced consecutive pairs point
+// alike; with 90 % of them alike the rays are already coherent (camera rays)
+// and keep the caller's order.
+constexpr uint32_t kCoherenceSamples = 16384;
+FCPWGB_D bool keepOrder(const int *sortInfo, uint32_t n) {
+    const uint32_t samples = min(n > 0 ? n - 1 : 0u, kCoherenceSamples);
+    return samples > 0 && (uint32_t)__ldg(sortInfo + 6) * 10u >= samples * 9u;
+}
+
 // SNCH node suffix (bytes 32..63)
 struct NodeCone { float3 axis; float halfAngle, radius; uint32_t nSil, silOffset; };
 FCPWGB_D NodeCone loadCone(const unsigned char *nodes, uint32_t i) {

@@ -20,8 +20,6 @@
 
 namespace fcpwgb {
 
-constexpr uint32_t kCoherenceSamples = 16384;  // consecutive ray pairs sampled by kRayCoherence
-
 FCPWGB_D uint32_t spread3(uint32_t v) {  // up to 8 bits -> every third bit
     v &= 0xffu;
     v = (v | (v << 8)) & 0x0300f00fu;
@@ -182,28 +180,29 @@ template<class Rec> __global__ void __launch_bounds__(kBoundsBlock) kQueryBounds
     }
 }
 
-// qb[6]: how many sampled consecutive pairs of rays point alike (kRayCoherence)
-FCPWGB_D bool keepOrder(const int *qb, uint32_t n) {
-    const uint32_t samples = min(n > 0 ? n - 1 : 0u, kCoherenceSamples);
-    return samples > 0 && (uint32_t)__ldg(qb + 6) * 10u >= samples * 9u;
-}
-
+// qb[6]: how many sampled consecutive pairs of rays point alike (kRayCoherence,
+// keepOrder); coherent rays keep the caller's order, and with skipInOrder set
+// the caller reads its own array (no sorted copy or permutation is written)
 template<class Rec>
 __global__ void kCellHistogram(SortLimits lim, const int *qb, const Rec *__restrict__ q, uint32_t n,
-                               uint32_t *cells, uint32_t nCells) {
+                               uint32_t *cells, uint32_t nCells, bool skipInOrder) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const bool inOrder = keepOrder(qb, n);
+    if (inOrder && skipInOrder) return;
     CellGrid g = cellGrid(lim, qb);
-    atomicAdd(cells + recordCell(lim.dim, g, q, i, keepOrder(qb, n), nCells), 1u);
+    atomicAdd(cells + recordCell(lim.dim, g, q, i, inOrder, nCells), 1u);
 }
 
 template<class Rec>
 __global__ void kScatterQueries(SortLimits lim, const int *qb, const Rec *__restrict__ q, uint32_t n,
-                                uint32_t *cells, uint32_t nCells, Rec *sorted, uint32_t *perm) {
+                                uint32_t *cells, uint32_t nCells, Rec *sorted, uint32_t *perm, bool skipInOrder) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const bool inOrder = keepOrder(qb, n);
+    if (inOrder && skipInOrder) return;
     CellGrid g = cellGrid(lim, qb);
-    uint32_t pos = atomicAdd(cells + recordCell(lim.dim, g, q, i, keepOrder(qb, n), nCells), 1u);
+    uint32_t pos = atomicAdd(cells + recordCell(lim.dim, g, q, i, inOrder, nCells), 1u);
     copyRecord(q, i, sorted, pos);
     perm[pos] = i;
 }
@@ -229,7 +228,7 @@ __global__ void kRayCoherence(const DevRay *__restrict__ q, uint32_t n, int *qb)
 
 template<class Rec>
 cudaError_t sortRecords(const SortLimits &lim, const Rec *recs, uint32_t n, uint32_t *cells, Rec *sorted,
-                        uint32_t *perm, int numSMs, cudaStream_t s) {
+                        uint32_t *perm, int numSMs, cudaStream_t s, bool skipInOrder = false) {
     if (n == 0) return cudaSuccess;
     int *qb = reinterpret_cast<int *>(cells + kSortCells);
     const uint32_t nCells = lim.dim == 3 ? 1u << 21 : 1u << 18;  // the cells cellOf can return
@@ -244,9 +243,9 @@ cudaError_t sortRecords(const SortLimits &lim, const Rec *recs, uint32_t n, uint
             reinterpret_cast<const DevRay *>(recs), n, qb);
     kQueryBounds<Rec><<<std::min<uint32_t>(blocks, (uint32_t)std::max(numSMs, 1) * 8u), kBoundsBlock, 0, s>>>(recs, n,
                                                                                                      qb);
-    kCellHistogram<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, nCells);
+    kCellHistogram<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, nCells, skipInOrder);
     if ((e = scanCounts(cells, nCells, cells + kSortCells + 8, s)) != cudaSuccess) return e;
-    kScatterQueries<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, nCells, sorted, perm);
+    kScatterQueries<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, nCells, sorted, perm, skipInOrder);
     return cudaGetLastError();
 }
 
@@ -256,8 +255,8 @@ cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, u
 }
 
 cudaError_t launchSortRays(const SortLimits &lim, const DevRay *rays, uint32_t n, uint32_t *cells, DevRay *sorted,
-                           uint32_t *perm, int numSMs, cudaStream_t s) {
-    return sortRecords(lim, rays, n, cells, sorted, perm, numSMs, s);
+                           uint32_t *perm, int numSMs, cudaStream_t s, bool skipInOrder) {
+    return sortRecords(lim, rays, n, cells, sorted, perm, numSMs, s, skipInOrder);
 }
 
 // ---------------------------------------------------------------- batches

@@ -992,7 +992,13 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
                                                        const DevRay *__restrict__ rays,
                                                        const uint32_t *__restrict__ perm,
                                                        DevInteraction *__restrict__ out, uint32_t n, int occl,
+                                                       const DevRay *__restrict__ callerRays, const int *sortInfo,
                                                        uint32_t *errorWord, unsigned long long *stats) {
+    // rays the sort left in the caller's order are read from the caller's array
+    if (sortInfo && keepOrder(sortInfo, n)) {
+        rays = callerRays;
+        perm = nullptr;
+    }
     __shared__ uint32_t sRef[kShortStack * kWideBlock];
     __shared__ float sD[kShortStack * kWideBlock];
     WideStack<kShortStack> st;
@@ -1032,7 +1038,13 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketRay(const unsigned c
                                                              const DevRay *__restrict__ rays,
                                                              const uint32_t *__restrict__ perm,
                                                              DevInteraction *__restrict__ out, uint32_t n, int occl,
-                                                             uint32_t *errorWord, unsigned long long *stats) {
+                                                             const DevRay *__restrict__ callerRays,
+                                                             const int *sortInfo, uint32_t *errorWord,
+                                                             unsigned long long *stats) {
+    if (sortInfo && keepOrder(sortInfo, n)) {  // rays left in the caller's order
+        rays = callerRays;
+        perm = nullptr;
+    }
     constexpr uint32_t kSlotMask = W - 1;
     constexpr int kWarps = kWideBlock / 32;
     __shared__ uint32_t sRef[kWarps][kPacketShort];
@@ -1265,7 +1277,8 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
         if (l.n == 0) return cudaSuccess;                                                                          \
         dim3 g((l.n + 127) / 128), b(128);                                                                         \
         auto go = [&](auto kern) {                                                                                 \
-            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.errorWord, l.stats);     \
+            kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.callerRays, l.sortInfo,  \
+                                 l.errorWord, l.stats);                                                            \
         };                                                                                                         \
         if (dim == 3) {                                                                                            \
             if (bits == 8) l.packet ? go(kWidePacketRay<W, 8, Tri48Prim>) : go(kWideRay<W, 8, Tri48Prim>);         \

@@ -85,6 +85,8 @@ struct WideRayLaunch {
     const unsigned char *prims = nullptr;
     const DevRay *rays = nullptr;           // (sorted when perm is set)
     const uint32_t *perm = nullptr;
+    const DevRay *callerRays = nullptr;     // with sortInfo: the caller's array, used when keepOrder holds
+    const int *sortInfo = nullptr;          // the sort's verdict (cells + kSortCells), or NULL
     DevInteraction *out = nullptr;
     uint32_t n = 0;
     int occl = 0;
@@ -107,9 +109,12 @@ struct SortLimits { float3 lo; float3 hi; int dim; };
 constexpr uint32_t kSortScratchWords = kSortCells + 8 + kSortCells / 4096;
 cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, uint32_t n, uint32_t *cells,
                               DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s);
-// the same for rays, by origin
+// the same for rays: by direction octant, then origin; rays that are already
+// coherent keep the caller's order (keepOrder on cells + kSortCells), and with
+// skipInOrder then nothing is written to sorted / perm (the caller reads its
+// own array)
 cudaError_t launchSortRays(const SortLimits &lim, const DevRay *rays, uint32_t n, uint32_t *cells, DevRay *sorted,
-                           uint32_t *perm, int numSMs, cudaStream_t s);
+                           uint32_t *perm, int numSMs, cudaStream_t s, bool skipInOrder = false);
 // exclusive scan of nCells counters in place; tileSums holds batchScanTiles(nCells) words
 cudaError_t scanCounts(uint32_t *cells, uint32_t nCells, uint32_t *tileSums, cudaStream_t s);
 // stable radix sort of n keys (low keyBits bits) carrying their input index:

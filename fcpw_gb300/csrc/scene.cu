@@ -157,10 +157,12 @@ int GpuScene::wideRays(const DevRay *r, DevInteraction *out, uint32_t n, int occ
         if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
         if ((rc = sortRays.ensure((size_t)n * sizeof(DevRay)))) return rc;
         if ((e = launchSortRays(sortLimits(), r, n, (uint32_t *)sortCells.ptr, (DevRay *)sortRays.ptr,
-                                (uint32_t *)sortPerm.ptr, numSMs, st)) != cudaSuccess)
+                                (uint32_t *)sortPerm.ptr, numSMs, st, true)) != cudaSuccess)
             return cudaFail(e, "sort rays");
         l.rays = (const DevRay *)sortRays.ptr;
         l.perm = (const uint32_t *)sortPerm.ptr;
+        l.callerRays = r;
+        l.sortInfo = (const int *)((const uint32_t *)sortCells.ptr + kSortCells);
     }
     if ((rc = timeStart(st))) return rc;
     if ((e = launchWideRays(wideConfig.branching, wideConfig.bits, dim, l, st)) != cudaSuccess)

@@ -200,6 +200,34 @@ def test_wide_rays_match_oracle(torus, branching, bits, packet):
     assert g.check_errors() == 0
 
 
+def test_coherent_rays_keep_the_callers_order(torus):
+    """Camera rays from one eye, in pixel order: the sort sees that consecutive
+    rays point alike and leaves them in the caller's order (the traversal
+    then reads the caller's array); the records equal those of the unsorted
+    configuration and match the oracle."""
+    s, g, pts, ref, prims = torus
+    h, w = 192, 256
+    ys, xs = np.mgrid[0:h, 0:w]
+    u = ((xs.ravel() + 0.5) / w * 2 - 1) * 0.45
+    v = ((ys.ravel() + 0.5) / h * 2 - 1) * 0.45 - 0.3
+    d = np.stack([u, np.ones_like(u), v], 1)
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    o = np.broadcast_to(np.array([0.0, -5.0, 1.5], np.float32), d.shape).copy()
+    tmax = np.full(len(d), R.FLT_MAX, np.float32)
+    nodes, _, _ = s.cpu_bvh.export()
+    ref_out, ref_hit = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax))
+    outs = []
+    for cfg in [dict(sort_queries=False), dict(sort_queries=True), dict(sort_queries=True, packet=True)]:
+        g.set_traversal(4, 32, **cfg)
+        out = F.GPUInteractionList()
+        g.intersect(o, d, tmax, out)
+        outs.append(out.array())
+        _ray_check(outs[-1], ref_out, ref_hit)
+    g.set_traversal(0)
+    assert outs[1].tobytes() == outs[0].tobytes()
+    assert g.check_errors() == 0
+
+
 def test_wide_rays_finite_tmax_unsorted_and_2d():
     v, sg = W.star_polylines(16, 64, W.SEED_BASE + 53)
     s = build_scene(2, v, sg)
