@@ -851,7 +851,7 @@ def run_ours(args):
                          + " + kRefineClosest",
                          "kernel_ms": kms,  # CUDA events around both kernels of the precise launch
                          "algorithmic_bytes_per_launch": fast_stats["bytes"], "per_query": fast_stats["per_query"],
-                         "limiter": "instruction issue (72 % of active cycles in ncu) on an L2-resident working set "
+                         "limiter": "instruction issue (70-72 % of active cycles in ncu) on an L2-resident working set "
                                     "(records and triangles, 57 MB); DRAM moves ~166 B per query "
                                     "(profiles/closest_point_wide4_q32_packet_torus1M.md)"},
             "clocks": clocks, "accuracy": accuracy,
