@@ -88,6 +88,9 @@ int ensureForest(fcpwgb_gpu_batch *b) {
     const int W = b->cfg.branching, bits = b->cfg.bits, leaf = b->cfg.leafSize;
     if (b->forestValid && b->forestW == W && b->forestBits == bits && b->forestLeaf == leaf) return FCPWGB_OK;
     if (b->scenes.empty()) return setError(FCPWGB_ERR_NOT_TRANSFERRED, "the batch holds no scenes");
+    // invalid until the rebuild completes: a failed allocation releases the old buffers
+    b->forestValid = false;
+    b->hostOffsets.clear();  // the layout records roots of the forest
     const size_t nS = b->scenes.size();
     std::vector<WideHost> wide(nS);
     std::vector<char> ok(nS, 0);
@@ -172,6 +175,7 @@ int ensureLayout(fcpwgb_gpu_batch *b, const uint32_t *offsets, uint32_t nOffsets
         std::memcmp(b->hostOffsets.data(), offsets, nOffsets * sizeof(uint32_t)) == 0)
         return FCPWGB_OK;
     if (offsets[0] != 0) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "query_offsets[0] must be 0");
+    b->hostOffsets.clear();  // no layout until this one is complete (a failed allocation releases buffers)
     for (uint32_t s = 0; s < nS; s++)
         if (offsets[s + 1] < offsets[s])
             return setError(FCPWGB_ERR_INVALID_ARGUMENT, "query_offsets must be non-decreasing");

@@ -610,6 +610,7 @@ int instancedPrepare(fcpwgb_gpu_scene *s, cudaStream_t st) {
     InstancedState &I = *s->inst;
     const WideConfig &c = s->wideConfig;
     if (I.tableBits == c.bits && I.tableLeaf == c.leafSize) return FCPWGB_OK;
+    I.tableBits = I.tableLeaf = -1;  // invalid until the rebuild completes
     std::vector<DevObject> table(I.objects.size());
     for (size_t k = 0; k < I.objects.size(); k++) {
         fcpwgb_gpu_scene *o = I.objects[k];

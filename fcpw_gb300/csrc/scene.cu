@@ -37,6 +37,8 @@ cudaError_t launchRequant(int W, int bits, unsigned char *wn, const int32_t *cb,
 int GpuScene::ensureWide(cudaStream_t st) {
     const WideConfig &c = wideConfig;
     if (wide.valid && wide.branching == c.branching && wide.bits == c.bits && wide.leafSize == c.leafSize) return 0;
+    // invalid until the rebuild completes: a failed allocation releases the old buffers
+    wide.valid = false;
     WideHost h;
     const WideHost *pre = nullptr;
     for (const auto &p : preloadedWide)

@@ -159,3 +159,45 @@ def test_mismatched_sizes_and_missing_transfer_raise():
         g.find_closest_points(pts, np.full(99, R.FLT_MAX, np.float32), F.GPUInteractionList())
     with pytest.raises(ValueError):
         g.intersect(pts, pts[:50], np.full(100, R.FLT_MAX, np.float32), F.GPUInteractionList())
+
+
+def test_injected_allocation_failures_in_a_batch():
+    """The same walk for a batch of meshes: the forest, the layout and sort
+    scratch, the refinement scratch and the captured graph; each failure
+    reports FCPWGB_ERR_OUT_OF_MEMORY and the same batch object then answers
+    byte-identically to one that never failed."""
+    meshes = [W.perturbed_sphere(8, W.SEED_BASE + 87), W.torus(32, 16, W.SEED_BASE + 88)]
+    scenes = [build_scene(3, v, f) for v, f in meshes]
+    pts = np.concatenate([W.uniform_points(6000, 3, -1.2, 1.2, 89), W.uniform_points(9000, 3, -1.5, 1.5, 90)])
+    offsets = np.array([0, 6000, 15000], np.uint32)
+    r2 = np.full(len(pts), R.FLT_MAX, np.float32)
+    b0 = F.GPUSceneBatch3D()
+    b0.set_scenes(scenes)
+    b0.set_traversal(4, 32, packet=True)
+    ref = F.GPUInteractionList()
+    b0.find_closest_points(pts, r2, offsets, ref)
+    failures = 0
+    try:
+        for skip in range(64):
+            b = F.GPUSceneBatch3D()
+            check(lib().fcpwgb_debug_fail_allocations(skip, 1))
+            try:
+                b.set_scenes(scenes)
+                b.set_traversal(4, 32, packet=True)
+                b.find_closest_points(pts, r2, offsets, F.GPUInteractionList())
+                failed = False
+            except F.FcpwError as e:
+                assert e.code == 5, e
+                failed = True
+            check(lib().fcpwgb_debug_fail_allocations(0, 0))
+            b.set_scenes(scenes)
+            b.set_traversal(4, 32, packet=True)
+            got = F.GPUInteractionList()
+            b.find_closest_points(pts, r2, offsets, got)
+            assert got.array().tobytes() == ref.array().tobytes(), skip
+            if not failed:
+                break
+            failures += 1
+    finally:
+        check(lib().fcpwgb_debug_fail_allocations(0, 0))
+    assert failures >= 4
