@@ -49,6 +49,7 @@ SIGNATURES = {
     "fcpwgb_gpu_scene_refit": (c_int, [P, P, P]),
     "fcpwgb_gpu_scene_update_vertices_device": (c_int, [P, P, c_uint32, P]),
     "fcpwgb_gpu_scene_update_vertices_device_static": (c_int, [P, P, c_uint32, P]),
+    "fcpwgb_debug_fill_static_scratch": (c_int, [P, c_uint32, c_uint32]),
     "fcpwgb_find_closest_points": (c_int, [P, P, P, c_uint32, c_int]),
     "fcpwgb_intersect_rays": (c_int, [P, P, P, c_uint32, c_int]),
     "fcpwgb_intersect_spheres": (c_int, [P, P, P, P, c_uint32]),

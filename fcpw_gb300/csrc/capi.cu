@@ -437,6 +437,7 @@ extern "C" int fcpwgb_gpu_scene_transfer(fcpwgb_gpu_scene *s, int bvh_type, cons
     std::memcpy(s->rootBox, s->hostBoxes.data(), 24);
     s->transferred = true;
     s->treeVersion++;
+    resolveStaticScratch(s);
     return FCPWGB_OK;
 }
 
@@ -601,7 +602,8 @@ extern "C" int fcpwgb_gpu_scene_build(fcpwgb_gpu_scene *s, const float *position
     return rc;
 }
 
-static int requireTree(fcpwgb_gpu_scene *s) {
+namespace fcpwgb {
+int requireTree(fcpwgb_gpu_scene *s) {
     if (!s) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL scene");
     if (s->inst)
         return setError(FCPWGB_ERR_UNSUPPORTED,
@@ -609,6 +611,7 @@ static int requireTree(fcpwgb_gpu_scene *s) {
     if (!s->transferred) return setError(FCPWGB_ERR_NOT_TRANSFERRED, "transferToGPU has not been called");
     return s->activate();
 }
+}  // namespace fcpwgb
 
 namespace fcpwgb {
 int runRefit(fcpwgb_gpu_scene *s, cudaStream_t st) {

@@ -170,6 +170,10 @@ FCPWGB_HD bool boxRayIntersect(float3 pMin, float3 pMax, const DevRay &r, float 
     return true;
 }
 
+}  // namespace fcpwgb
+#include "exact_ops.cuh"
+namespace fcpwgb {
+
 // ----------------------------------------------------------- primitives
 
 // Ericson's closest point on a triangle (Real-Time Collision Detection,
@@ -224,51 +228,14 @@ FCPWGB_HD float closestPointSegment(float3 pa, float3 pb, float3 x, float3 &p, f
     return len3(x - p);
 }
 
-// Moller-Trumbore, geometry.slang:202-249
-FCPWGB_HD bool intersectTriangle(float3 pa, float3 pb, float3 pc, const DevRay &r, bool occl,
-                                 DevInteraction &i) {
-    float3 v1 = pb - pa, v2 = pc - pa;
-    float3 q = cross3(r.d, v2);
-    float det = dot3(v1, q);
-    if (fabsf(det) <= kFltEps) return false;
-    float invDet = 1.0f / det;
-    float3 rr = r.o - pa;
-    float v = dot3(rr, q) * invDet;
-    if (v < 0.0f || v > 1.0f) return false;
-    float3 s = cross3(rr, v1);
-    float w = dot3(r.d, s) * invDet;
-    if (w < 0.0f || v + w > 1.0f) return false;
-    float t = dot3(v2, s) * invDet;
-    if (t >= 0.0f && t <= r.tMax) {
-        if (occl) return true;
-        i.p = pa + v1 * v + v2 * w;
-        i.n = normalize3(cross3(v1, v2));
-        i.uv = make_float2(1.0f - v - w, v);
-        i.d = t;
-        return true;
-    }
-    return false;
+// Ray-primitive tests: the reference's Moller-Trumbore and segment test in its
+// own float arithmetic (exact_ops.cuh), so hit distances, points, normals and
+// uvs equal the reference's bit for bit
+FCPWGB_D bool intersectTriangle(float3 pa, float3 pb, float3 pc, const DevRay &r, bool occl, DevInteraction &i) {
+    return xIntersectTriangle(pa, pb, pc, r, occl, i);
 }
-
-// 2D segment-ray intersection, geometry.slang:37-77
-FCPWGB_HD bool intersectSegment(float3 pa, float3 pb, const DevRay &r, bool occl, DevInteraction &i) {
-    float3 u = pa - r.o, v = pb - pa;
-    float dv = r.d.x * v.y - r.d.y * v.x;
-    if (fabsf(dv) <= kFltEps) return false;
-    float ud = u.x * r.d.y - u.y * r.d.x;
-    float s = ud / dv;
-    if (s >= 0.0f && s <= 1.0f) {
-        float t = (u.x * v.y - u.y * v.x) / dv;
-        if (t >= 0.0f && t <= r.tMax) {
-            if (occl) return true;
-            i.p = pa + v * s;
-            i.n = normalize3(make_float3(v.y, -v.x, 0.0f));
-            i.uv = make_float2(s, 0.0f);
-            i.d = t;
-            return true;
-        }
-    }
-    return false;
+FCPWGB_D bool intersectSegment(float3 pa, float3 pb, const DevRay &r, bool occl, DevInteraction &i) {
+    return xIntersectSegment(pa, pb, r, occl, i);
 }
 
 // -------------------------------------------------- primitive accessors
@@ -291,7 +258,7 @@ struct TriPrim {
     }
     FCPWGB_HD float3 normal() const { return normalize3(cross3(pb - pa, pc - pa)); }
     FCPWGB_HD float surfaceArea() const { return 0.5f * len3(cross3(pb - pa, pc - pa)); }
-    FCPWGB_HD bool intersect(const DevRay &r, bool occl, DevInteraction &i) const {
+    FCPWGB_D bool intersect(const DevRay &r, bool occl, DevInteraction &i) const {
         return intersectTriangle(pa, pb, pc, r, occl, i);
     }
     // geometry.slang:410-424
@@ -331,7 +298,7 @@ struct SegPrim {
         return normalize3(make_float3(s.y, -s.x, 0.0f));
     }
     FCPWGB_HD float surfaceArea() const { return len3(pb - pa); }
-    FCPWGB_HD bool intersect(const DevRay &r, bool occl, DevInteraction &i) const {
+    FCPWGB_D bool intersect(const DevRay &r, bool occl, DevInteraction &i) const {
         return intersectSegment(pa, pb, r, occl, i);
     }
     // geometry.slang:183-193

@@ -22,23 +22,6 @@ namespace {
 
 constexpr int kMaxHits = 64;  // hits kept per ray; more sets kErrStepBudget and answer 2
 
-FCPWGB_D float3 xsub(float3 a, float3 b) {
-    return make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
-}
-FCPWGB_D float3 xadd(float3 a, float3 b) {
-    return make_float3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
-}
-FCPWGB_D float3 xmul(float3 a, float s) { return make_float3(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)); }
-FCPWGB_D float3 xdiv(float3 a, float s) { return make_float3(__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)); }
-FCPWGB_D float xdot(int dim, float3 a, float3 b) {
-    return dim == 3 ? __fadd_rn(__fmul_rn(a.x, b.x), __fadd_rn(__fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z)))
-                    : __fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
-}
-FCPWGB_D float3 xcross(float3 a, float3 b) {
-    return make_float3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)),
-                       __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
-                       __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
-}
 FCPWGB_D float cmin(float a, float b) { return b < a ? b : a; }  // std::min
 FCPWGB_D float cmax(float a, float b) { return a < b ? b : a; }  // std::max
 FCPWGB_D float comp(float3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }

@@ -96,6 +96,10 @@ struct GpuScene {
     }
 
     bool hasTopology = false;  // prim_vertices were given at transfer (device updates, gradients)
+    // device address of the static refit scratch (static_scratch.cu), resolved when the tree is
+    // transferred; NULL when that failed (staticScratchError says why)
+    uint32_t *staticCounters = nullptr;
+    std::string staticScratchError;
     // differentiation: corner -> caller vertex table and the static vertex -> corner CSR
     DeviceBuffer origVerts, csrOff, csrCorner, gradCorners, gradMax;
 
@@ -147,6 +151,10 @@ struct fcpwgb_gpu_scene : fcpwgb::GpuScene {};
 
 namespace fcpwgb {
 int runRefit(fcpwgb_gpu_scene *s, cudaStream_t st);
+// the checks every single-tree operation makes first (capi.cu)
+int requireTree(fcpwgb_gpu_scene *s);
+// resolves the static refit scratch on the scene's (current) device (static_scratch.cu)
+void resolveStaticScratch(fcpwgb_gpu_scene *s);
 // instanced scenes (instanced.cu); instOut may be NULL
 int instancedClosest(fcpwgb_gpu_scene *s, const DevSphere *spheres, DevInteraction *out, uint32_t *instOut,
                      uint32_t n, int recordNormal, cudaStream_t st);

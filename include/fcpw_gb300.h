@@ -294,9 +294,19 @@ int fcpwgb_gpu_scene_update_vertices_device(fcpwgb_gpu_scene *scene, const float
  * with FCPWGB_ERR_INVALID_ARGUMENT. Each call clears the counters it uses;
  * the array is shared by all calls on a device, so calls that overlap on the
  * GPU (other streams, scenes or threads) race and must be ordered by the
- * caller. Asynchronous on stream (NULL is the CUDA default stream). */
+ * caller. The array's device address is looked up (and the code holding it
+ * loaded, which is when the 4 MiB is reserved) while the scene is
+ * transferred, not in this call; after a cudaDeviceReset the scene must be
+ * transferred again, as for any of its device buffers. Status codes and
+ * their order of checks are those of fcpwgb_gpu_scene_update_vertices_device.
+ * Asynchronous on stream (NULL is the CUDA default stream). */
 int fcpwgb_gpu_scene_update_vertices_device_static(fcpwgb_gpu_scene *scene, const float *positions,
                                                    uint32_t n_vertices, void *stream);
+/* Testing aid (no counterpart in the reference): writes `word` into the first
+ * n words of the static refit array on the scene's device, synchronously,
+ * without allocating device memory; a test uses it to check that
+ * fcpwgb_gpu_scene_update_vertices_device_static clears what it reads. */
+int fcpwgb_debug_fill_static_scratch(fcpwgb_gpu_scene *scene, uint32_t word, uint32_t n);
 
 /* Traversal variant used by the closest point entry points of a scene. With
  * branching 0 the transferred binary tree is traversed in the reference GPU

@@ -9,6 +9,7 @@
 // read, include/fcpw/gpu/bvh_interop_structures.h:172-298) and run its CPU
 // queries. The private tree is reached through a partial specialisation of
 // the reference's friend template CPUBvhDataExtractor (bvh.h:221-222).
+#include <chrono>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -194,12 +195,22 @@ template<size_t DIM> Vector<DIM> vecOf(const float *p) {
     return v;
 }
 
+// seconds spent in f()
+template<typename F> double secondsOf(F f) {
+    auto t0 = std::chrono::steady_clock::now();
+    f();
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
 }  // namespace
 
 extern "C" {
 
-void *ref_scene_create(int dim, const float *positions, int nV, const int *indices, int nP, int aggregate,
-                       int silhouettes) {
+// vectorize: Scene::build(aggregate, true), the reference's Mbvh with FCPW_SIMD_WIDTH-wide
+// leaves and nodes where this file is compiled with FCPW_USE_ENOKI (without it the
+// reference builds the same binary Bvh as with false, fcpw.inl:815-820,855-866)
+void *ref_scene_create_ex(int dim, const float *positions, int nV, const int *indices, int nP, int aggregate,
+                          int silhouettes, int vectorize) {
     RefScene *r = new RefScene;
     r->dim = dim;
     r->snch = silhouettes != 0;
@@ -212,7 +223,7 @@ void *ref_scene_create(int dim, const float *positions, int nV, const int *indic
         r->s3.setObjectVertices(pos, 0);
         r->s3.setObjectTriangles(idx, 0);
         if (r->snch) r->s3.computeSilhouettes();
-        r->s3.build((AggregateType)aggregate, false);
+        r->s3.build((AggregateType)aggregate, vectorize != 0);
     } else {
         std::vector<Vector2> pos(nV);
         std::vector<Vector2i> idx(nP);
@@ -222,9 +233,22 @@ void *ref_scene_create(int dim, const float *positions, int nV, const int *indic
         r->s2.setObjectVertices(pos, 0);
         r->s2.setObjectLineSegments(idx, 0);
         if (r->snch) r->s2.computeSilhouettes();
-        r->s2.build((AggregateType)aggregate, false);
+        r->s2.build((AggregateType)aggregate, vectorize != 0);
     }
     return r;
+}
+
+void *ref_scene_create(int dim, const float *positions, int nV, const int *indices, int nP, int aggregate,
+                       int silhouettes) {
+    return ref_scene_create_ex(dim, positions, nV, indices, nP, aggregate, silhouettes, 0);
+}
+
+int ref_simd_width(void) {
+#ifdef FCPW_USE_ENOKI
+    return FCPW_SIMD_WIDTH;
+#else
+    return 0;
+#endif
 }
 
 // A scene of several objects (Scene::setObjectCount, fcpw.h:29-58), each with
@@ -483,6 +507,63 @@ int ref_line_of_sight(void *h, const float *pa, const float *pb, int n, uint32_t
     if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
     else run(r->s2, std::integral_constant<size_t, 2>());
     return 0;
+}
+
+// ---- the reference's public bundled query API (Scene<DIM>::findClosestPoints,
+// intersect, findClosestSilhouettePoints over std::vector, fcpw.h:172-245,
+// fcpw.inl:1224-1660: one std::thread per hardware thread, contiguous query
+// ranges). Each returns the seconds spent inside that one call; the records are
+// converted to and from the interop layouts outside the timed span.
+double ref_scene_closest_points_timed(void *h, const float *spheres, int n, void *out) {
+    RefScene *r = (RefScene *)h;
+    double sec = 0.0;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        std::vector<BoundingSphere<D>> q;
+        q.reserve(n);
+        for (int k = 0; k < n; k++) q.emplace_back(vecOf<D>(spheres + 4 * k), spheres[4 * k + 3]);
+        std::vector<Interaction<D>> is;
+        sec = secondsOf([&]() { scene.findClosestPoints(q, is, false); });
+        for (int k = 0; k < n; k++) writeInteraction<D>(is[k], (unsigned char *)out + 40 * (size_t)k);
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return sec;
+}
+
+double ref_scene_intersect_rays_timed(void *h, const float *rays, int n, int occl, void *out) {
+    RefScene *r = (RefScene *)h;
+    double sec = 0.0;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        std::vector<Ray<D>> q;
+        q.reserve(n);
+        for (int k = 0; k < n; k++) q.emplace_back(vecOf<D>(rays + 10 * k), vecOf<D>(rays + 10 * k + 3), rays[10 * k + 9]);
+        std::vector<Interaction<D>> is;
+        sec = secondsOf([&]() { scene.intersect(q, is, occl != 0); });
+        for (int k = 0; k < n; k++) writeInteraction<D>(is[k], (unsigned char *)out + 40 * (size_t)k);
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return sec;
+}
+
+double ref_scene_silhouettes_timed(void *h, const float *spheres, const uint32_t *flip, int n, void *out) {
+    RefScene *r = (RefScene *)h;
+    double sec = 0.0;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        std::vector<BoundingSphere<D>> q;
+        q.reserve(n);
+        for (int k = 0; k < n; k++) q.emplace_back(vecOf<D>(spheres + 4 * k), spheres[4 * k + 3]);
+        std::vector<uint32_t> fl(flip, flip + n);
+        std::vector<Interaction<D>> is;
+        sec = secondsOf([&]() { scene.findClosestSilhouettePoints(q, is, fl, 0.0f, 1e-3f, false); });
+        for (int k = 0; k < n; k++) writeInteraction<D>(is[k], (unsigned char *)out + 40 * (size_t)k);
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return sec;
 }
 
 }  // extern "C"

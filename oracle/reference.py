@@ -1,38 +1,48 @@
 """ctypes wrapper of oracle/_ref/libfcpw_ref.so, the reference's own CPU Scene
-compiled from its sources (TEST INFRASTRUCTURE ONLY; available only where the
-reference checkout exists, i.e. never on the GPU machine)."""
+compiled from its sources (TEST INFRASTRUCTURE ONLY; available where the
+reference headers are staged, see build.py), and of oracle/_ref/libfcpw_ref_simd.so,
+the same built with Enoki packets for the reference's vectorised Mbvh (timing only)."""
 from __future__ import annotations
 
 import ctypes as C
 
 import numpy as np
 
-from .build import REF_LIB, build_reference
+from .build import build_reference, build_reference_simd
 
-_lib = None
+_libs = {}
 P = C.c_void_p
 
 
-def available() -> bool:
+def available(simd: bool = False) -> bool:
     try:
-        return build_reference() is not None
+        return (build_reference_simd() if simd else build_reference()) is not None
     except RuntimeError:
         return False
 
 
-def _load():
-    global _lib
-    if _lib is None:
-        path = build_reference()
+def _load(simd: bool = False):
+    if simd not in _libs:
+        path = build_reference_simd() if simd else build_reference()
         if path is None:
-            raise RuntimeError("the reference checkout is not available on this machine")
-        _lib = C.CDLL(str(path))
+            raise RuntimeError("the reference headers are not staged on this machine")
+        lib = C.CDLL(str(path))
         i, f = C.c_int, C.c_float
-        _lib.ref_scene_create.restype = P
-        _lib.ref_scene_create.argtypes = [i, P, i, P, i, i, i]
-        _lib.ref_scene_destroy.argtypes = [P]
-        _lib.ref_scene_create_multi.restype = P
-        _lib.ref_scene_create_multi.argtypes = [i, i, P, P, P, P, P, P, i]
+        lib.ref_scene_create.restype = P
+        lib.ref_scene_create.argtypes = [i, P, i, P, i, i, i]
+        lib.ref_scene_create_ex.restype = P
+        lib.ref_scene_create_ex.argtypes = [i, P, i, P, i, i, i, i]
+        lib.ref_scene_destroy.argtypes = [P]
+        lib.ref_scene_create_multi.restype = P
+        lib.ref_scene_create_multi.argtypes = [i, i, P, P, P, P, P, P, i]
+        lib.ref_simd_width.restype = i
+        lib.ref_simd_width.argtypes = []
+        for name, args in {"ref_scene_closest_points_timed": [P, P, i, P],
+                           "ref_scene_intersect_rays_timed": [P, P, i, i, P],
+                           "ref_scene_silhouettes_timed": [P, P, P, i, P]}.items():
+            fn = getattr(lib, name)
+            fn.restype = C.c_double
+            fn.argtypes = args
         for name, args in {"ref_export": [P, P, P, P, P], "ref_closest_points": [P, P, i, i, P, P],
                            "ref_intersect_rays": [P, P, i, i, P, P], "ref_silhouettes": [P, P, P, i, f, f, P],
                            "ref_sphere_sample": [P, P, P, i, P, P], "ref_update_and_refit": [P, P, i],
@@ -40,10 +50,16 @@ def _load():
                            "ref_closest_points_objects": [P, P, i, i, P, P],
                            "ref_intersect_rays_objects": [P, P, i, i, P, P, P],
                            "ref_export_top": [P, P, P]}.items():
-            fn = getattr(_lib, name)
+            fn = getattr(lib, name)
             fn.restype = i
             fn.argtypes = args
-    return _lib
+        _libs[simd] = lib
+    return _libs[simd]
+
+
+def simd_width() -> int:
+    """FCPW_SIMD_WIDTH of the vectorised build (0 when it is not available)."""
+    return int(_load(True).ref_simd_width()) if available(True) else 0
 
 
 def _p(a):
@@ -51,20 +67,49 @@ def _p(a):
 
 
 class RefScene:
-    """The reference Scene<DIM> with one object, built with vectorize=False."""
+    """The reference Scene<DIM> with one object, built with vectorize=False, or
+    with vectorize=True (the Mbvh; needs the Enoki build, timing calls only)."""
+    _simd = False
 
-    def __init__(self, dim, positions, indices, aggregate_type=3, silhouettes=False):
+    def __init__(self, dim, positions, indices, aggregate_type=3, silhouettes=False, vectorize=False):
         self.dim = dim
         self.silhouettes = bool(silhouettes)
+        self._simd = bool(vectorize)
         self.positions = np.ascontiguousarray(positions, np.float32)
         self.indices = np.ascontiguousarray(indices, np.int32)
-        self._h = _load().ref_scene_create(dim, _p(self.positions), len(self.positions), _p(self.indices),
-                                           len(self.indices), int(aggregate_type), int(self.silhouettes))
+        self._h = _load(self._simd).ref_scene_create_ex(dim, _p(self.positions), len(self.positions),
+                                                        _p(self.indices), len(self.indices), int(aggregate_type),
+                                                        int(self.silhouettes), int(self._simd))
 
     def __del__(self):
         if getattr(self, "_h", None):
-            _load().ref_scene_destroy(self._h)
+            _load(self._simd).ref_scene_destroy(self._h)
             self._h = None
+
+    # ---- the reference's public bundled API (Scene::findClosestPoints / intersect /
+    # findClosestSilhouettePoints over std::vector, its own std::thread split); each returns
+    # (records, seconds inside that call)
+    def closest_points_timed(self, spheres):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        sec = _load(self._simd).ref_scene_closest_points_timed(self._h, _p(self._sph(spheres)), len(spheres),
+                                                               _p(out))
+        return out, float(sec)
+
+    def intersect_rays_timed(self, rays, occlusion=False):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(rays), R.INTERACTION)
+        r = np.ascontiguousarray(rays).view(np.float32)
+        sec = _load(self._simd).ref_scene_intersect_rays_timed(self._h, _p(r), len(rays), int(occlusion), _p(out))
+        return out, float(sec)
+
+    def silhouettes_timed(self, spheres, flip):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        fl = np.ascontiguousarray(flip, np.uint32)
+        sec = _load(self._simd).ref_scene_silhouettes_timed(self._h, _p(self._sph(spheres)), _p(fl), len(spheres),
+                                                            _p(out))
+        return out, float(sec)
 
     def export(self):
         from fcpw_gb300 import records as R

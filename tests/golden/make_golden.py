@@ -1,7 +1,7 @@
 """Generates the golden fixtures in this directory from the REFERENCE ITSELF.
 
-Run where the reference checkout exists (default /root/reference, override with
-FCPW_REFERENCE_ROOT):
+Run where the reference headers can be staged (oracle/build.py stages them
+from the reference checkout into baseline/_ref):
 
     python tests/golden/make_golden.py [fixture names]
 

@@ -115,21 +115,15 @@ def test_rays_torus():
     g.intersect(o, d, tmax, out)
     got = out.array()
     nodes, prims, _ = s.cpu_bvh.export()
-    ref, hit = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax))
-    compare_rays(got, ref, hit)
+    rays = R.make_rays(o, d, tmax)
+    ref, hit = O.intersect_rays_bvh(3, nodes, prims, rays)
+    compare_rays(3, prims, rays, got, ref, hit)
     assert 0.05 < hit.mean() < 0.9
     # occlusion variant
     out2 = F.GPUInteractionList()
     g.intersect(o, d, tmax, out2, True)
-    ref2, hit2 = O.intersect_rays_bvh(3, nodes, prims, R.make_rays(o, d, tmax), occlusion=True)
-    compare_rays(out2.array(), ref2, hit2, occl=True)
-    # FP64 brute force agreement on a sample
-    t64, i64 = O.intersect_rays_brute_f64(3, prims, R.make_rays(o[:2000], d[:2000], tmax[:2000]))
-    h64 = np.isfinite(t64)
-    gh = got["index"][:2000] != R.UINT_MAX
-    assert (h64 != gh).sum() <= 2
-    both = h64 & gh
-    assert np.all(np.abs(got["d"][:2000][both] - t64[both]) <= 1e-5 * np.maximum(t64[both], 1))
+    ref2, hit2 = O.intersect_rays_bvh(3, nodes, prims, rays, occlusion=True)
+    compare_rays(3, prims, rays, out2.array(), ref2, hit2, occl=True)
 
 
 def test_rays_2d(stars2d):
@@ -141,8 +135,13 @@ def test_rays_2d(stars2d):
     out = F.GPUInteractionList()
     g.intersect(o, d, tmax, out)
     nodes, prims, _ = s.cpu_bvh.export()
-    ref, hit = O.intersect_rays_bvh(2, nodes, prims, R.make_rays(o, d, tmax))
-    compare_rays(out.array(), ref, hit)
+    rays = R.make_rays(o, d, tmax)
+    ref, hit = O.intersect_rays_bvh(2, nodes, prims, rays)
+    compare_rays(2, prims, rays, out.array(), ref, hit)
+    occ = F.GPUInteractionList()
+    g.intersect(o, d, tmax, occ, True)
+    ref2, hit2 = O.intersect_rays_bvh(2, nodes, prims, rays, occlusion=True)
+    compare_rays(2, prims, rays, occ.array(), ref2, hit2, occl=True)
 
 
 def test_silhouettes_2d(stars2d):

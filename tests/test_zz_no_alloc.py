@@ -2,7 +2,9 @@
 device array, no allocation) against fcpwgb_gpu_scene_update_vertices_device
 (counters owned by the scene), called through the C ABI. Two calls in a row
 on the same scene check that the shared array, which keeps the previous call's
-arrival counts, is cleared before each refit. The refit unions child boxes
+arrival counts, is cleared before each refit: before each call the array is
+filled with non-zero words, and free device memory is compared around the
+call. The refit unions child boxes
 with exact min/max and merges cones in a fixed child order, so the two entry
 points must agree bit for bit: the tolerance here is exact equality of the
 exported nodes and of the closest point records that use them.
@@ -63,11 +65,18 @@ def test_static_scratch_refit_matches_scene_scratch_refit(dim):
     assert s.cpu_bvh.info.n_nodes <= MAX_NODES
     pts = W.uniform_points(20000, dim, lo, hi, 42)
     stream = torch.cuda.current_stream().cuda_stream
+    n_nodes = s.cpu_bvh.info.n_nodes
     for call, seed in enumerate((43, 44)):
         pos = torch.from_numpy(_moved(v, seed, amp)).cuda()
         check(_update("fcpwgb_gpu_scene_update_vertices_device", a, pos, stream))
+        # every arrival counter the refit reads starts non-zero unless the call clears it: a refit
+        # that skipped the clear would merge nodes before their children are ready
+        check(lib().fcpwgb_debug_fill_static_scratch(b.handle, 0x5A5A5A5A if call else 1, n_nodes))
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         check(_update("fcpwgb_gpu_scene_update_vertices_device_static", b, pos, stream))
         torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free_before, "the allocation-free refit changed free device memory"
         na, nb = a.export_nodes(), b.export_nodes()
         assert na.tobytes() == nb.tobytes(), f"call {call}: refit nodes differ"
         ra, rb = _closest(a, pts), _closest(b, pts)
@@ -92,3 +101,25 @@ def test_static_scratch_refit_rejects_trees_beyond_the_maximum():
     assert "static refit scratch holds at most 1048576" in msg, msg
     with pytest.raises(FcpwError):
         check(rc)
+
+
+def test_static_scratch_refit_status_codes_equal_the_scene_scratch_entry():
+    """Both entry points answer an unsupported scene with the same status."""
+    import torch
+    v, f = W.perturbed_sphere(8, W.SEED_BASE + 46)
+    s = F.Scene3D()
+    s.set_object_count(1)
+    s.set_object_vertices(v, 0)
+    s.set_object_triangles(f, 0)
+    s.set_object_instance_transforms([np.eye(4, dtype=np.float32)] * 2, 0)
+    s.build(F.AggregateType.Bvh_SurfaceArea, False)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    pos = torch.from_numpy(v).cuda()
+    stream = torch.cuda.current_stream().cuda_stream
+    rc_scene = _update("fcpwgb_gpu_scene_update_vertices_device", g, pos, stream)
+    rc_static = _update("fcpwgb_gpu_scene_update_vertices_device_static", g, pos, stream)
+    assert rc_scene == rc_static != 0
+    fresh = F.GPUScene3D()
+    assert (_update("fcpwgb_gpu_scene_update_vertices_device", fresh, pos, stream)
+            == _update("fcpwgb_gpu_scene_update_vertices_device_static", fresh, pos, stream) != 0)
