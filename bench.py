@@ -7,9 +7,10 @@ built on the host. A step is one closest-point pass over all queries of the
 rank, inputs resident on the device; L2 is flushed (a 256 MiB device write)
 before every timed step, outside the timed events.
 
-Prints one JSON line (rank 0). ``--impl reference`` instead times the reference
-CPU algorithm (the C restatement in oracle/, all host threads) on bounded
-samples of the same workload.
+Prints one JSON line (rank 0). ``--impl reference`` instead times the
+reference's own CPU implementation (its Scene<3> compiled on this host from its
+headers, oracle/_ref; scalar and vectorised builds, the faster one timed) on
+all queries of the same workload, with all host threads.
 """
 from __future__ import annotations
 
@@ -17,6 +18,7 @@ import argparse
 import ctypes as C
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -47,6 +49,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-loss", action="store_true", help="skip the fwd/fwd+bwd distance loss measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched uneven scenes measurement")
+    ap.add_argument("--no-quantised", action="store_true", help="skip the 8/16-bit box measurement")
+    ap.add_argument("--no-suite", action="store_true",
+                    help="skip the other configurations (icosphere, rays, 2D, 3D silhouettes) in the headline line")
     ap.add_argument("--suite", action="store_true",
                     help="instead of the headline line, one line per other configuration of the scope")
     ap.add_argument("--only", default="",
@@ -150,18 +155,78 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_baseline(scene, pts, budget_s: float = 12.0, max_queries: int = N_QUERIES):
-    """The reference CPU closest-point traversal (oracle port), all host threads,
-    on a bounded prefix of the query set sized to about budget_s seconds."""
+def reference_cpu(dim, positions, indices, silhouettes=False):
+    """The reference's own CPU Scene<DIM> (oracle/_ref, compiled from its headers on this
+    host), scalar and, where Enoki builds, vectorised: {"scalar": RefScene, "vectorized":
+    RefScene or None}; None when the reference is not available here."""
+    from oracle import reference as REF
+    if not REF.available():
+        return None
+    out = {"scalar": REF.RefScene(dim, positions, indices, silhouettes=silhouettes), "vectorized": None}
+    if REF.available(simd=True):
+        out["vectorized"] = REF.RefScene(dim, positions, indices, silhouettes=silhouettes, vectorize=True)
+    return out
+
+
+def _ref_call(ref_scene, kind, queries, flip=None):
+    """One bundled call of the reference's public API; returns the seconds inside it."""
+    if kind == "closest":
+        return ref_scene.closest_points_timed(queries)[1]
+    if kind == "rays":
+        return ref_scene.intersect_rays_timed(queries)[1]
+    return ref_scene.silhouettes_timed(queries, flip)[1]
+
+
+def reference_rate(refs, kind, queries, flip=None, budget_s: float = 6.0):
+    """Queries/s of the reference CPU on a bounded prefix of `queries` sized to about
+    budget_s seconds per build (scalar Bvh and, where it builds, the vectorised Mbvh); the
+    faster build is the reported value."""
+    threads = os.cpu_count() or 1
+    n_all = len(queries)
+    rates = {}
+    for name in ("scalar", "vectorized"):
+        r = refs.get(name)
+        if r is None:
+            continue
+        n0 = min(n_all, 16384)
+        sec = _ref_call(r, kind, queries[:n0], None if flip is None else flip[:n0])
+        n = int(min(n_all, max(n0, n0 / max(sec, 1e-9) * budget_s)))
+        sec = _ref_call(r, kind, queries[:n], None if flip is None else flip[:n])
+        rates[name] = (n / sec, n, sec)
+    best = max(rates, key=lambda k: rates[k][0])
+    v, n, sec = rates[best]
+    from oracle import reference as REF
+    width = REF.simd_width() if rates.get("vectorized") else 0
+    return {"value": v, "unit": UNIT, "cores": threads, "kind": "reference",
+            "sample": f"first {n} of {n_all} queries through the reference's Scene<{3}>::"
+                      f"{'findClosestPoints' if kind == 'closest' else ('intersect' if kind == 'rays' else 'findClosestSilhouettePoints')}"
+                      f" ({best}{f', FCPW_SIMD_WIDTH={width}' if best == 'vectorized' else ''}), "
+                      f"its own std::thread split over {threads} hardware threads, {sec:.2f} s",
+            "builds": {k: {"queries_per_s": r[0], "queries": r[1], "seconds": round(r[2], 3)} for k, r in rates.items()}}
+
+
+def cpu_baseline(v, f, pts, budget_s: float = 12.0):
+    """The reference CPU closest-point path (its own compiled Scene<3>, all host threads)
+    on a bounded prefix of the query set sized to about budget_s seconds; the oracle's C
+    restatement (kind "port") where the reference is not available on this host."""
+    from fcpw_gb300 import records as R
+    refs = reference_cpu(3, v, f)
+    if refs is not None:
+        return reference_rate(refs, "closest", R.make_spheres(pts, R.FLT_MAX), budget_s=budget_s / 2)
+    return _port_baseline(v, f, pts, budget_s)
+
+
+def _port_baseline(v, f, pts, budget_s):
     from fcpw_gb300 import records as R
     from oracle import oracle as O
+    scene, _ = build_scene(v, f)
     nodes, prims, _ = scene.cpu_bvh.export()
     threads = os.cpu_count() or 1
     n0 = min(len(pts), 20000)
     t = time.perf_counter()
     O.closest_points_bvh(3, nodes, prims, R.make_spheres(pts[:n0], R.FLT_MAX), nthreads=threads)
     rate = n0 / max(time.perf_counter() - t, 1e-9)
-    n = int(min(max_queries, len(pts), max(n0, rate * budget_s)))
+    n = int(min(len(pts), max(n0, rate * budget_s)))
     sph = R.make_spheres(pts[:n], R.FLT_MAX)
     t = time.perf_counter()
     O.closest_points_bvh(3, nodes, prims, sph, nthreads=threads)
@@ -179,13 +244,27 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(variant: str):
-    """DRAM bytes per launch from the committed ncu summary of this kernel, if any."""
-    p = ROOT / "profiles" / "closest_point_traffic.json"
-    if not p.exists():
-        return None
-    d = json.loads(p.read_text())
-    return d.get(variant)
+def measure_l2_gbs(dev, reps: int = 50) -> float:
+    """Measured L2 throughput of this GPU, for the L2 roofline of the traversal: the best of
+    a read (torch sum) and a copy of a 32 MiB float buffer that stays resident in L2,
+    CUDA events over `reps` back-to-back calls after warm-up (bytes read + written / time)."""
+    import torch
+    x = torch.ones(8 << 20, dtype=torch.float32, device=dev)
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+    best = 0.0
+    for fn, nbytes in ((lambda: x.sum(), x.numel() * 4), (lambda: y.copy_(x), 2 * x.numel() * 4)):
+        for _ in range(10):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        best = max(best, nbytes * reps / (a.elapsed_time(b) / 1e3) / 1e9)
+    return best
 
 
 def distance_loss_bench(device_index: int, steps: int = 20, warmup: int = 5):
@@ -238,12 +317,52 @@ def distance_loss_bench(device_index: int, steps: int = 20, warmup: int = 5):
             "fwd_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "ratio": fb_ms / fwd_ms, "target_ratio_max": 2.5}
 
 
+def algorithmic_bytes(L, g, spheres, out, n, node_bytes, prim_bytes, in_bytes, packet=False):
+    """Algorithmic bytes of one closest-point launch, counted by the traversal-statistics
+    mode of the same kernel on the same queries (fcpwgb_closest_points_traversal_stats):
+    per query in_bytes read and a 40 B record written; per expansion one record of
+    node_bytes (the binary kernel loads two 32 B child records per expansion plus the
+    root), per primitive test one prim_bytes record; for warp packets one record or
+    triangle load serves the 32 queries of a warp."""
+    from fcpw_gb300._lib import check
+    stats = (C.c_uint64 * 8)()
+    check(L.fcpwgb_closest_points_traversal_stats(g.handle, spheres.data_ptr(), out.data_ptr(), n, stats))
+    n_q, n_pop, n_inner, n_prim, w_rec, w_prim = [int(x) for x in stats[:6]]
+    if node_bytes == 32:
+        nb, pb = 32 * (n_q + 2 * n_inner), prim_bytes * n_prim
+    elif packet:
+        nb, pb = node_bytes * w_rec, prim_bytes * w_prim
+    else:
+        nb, pb = node_bytes * n_inner, prim_bytes * n_prim
+    per_query = {"nodes_popped": n_pop / n_q if node_bytes == 32 else n_inner / n_q,
+                 "inner_expanded": n_inner / n_q, "prim_tests": n_prim / n_q}
+    if packet:
+        per_query.update({"warp_record_loads": w_rec / n_q, "warp_prim_loads": w_prim / n_q})
+    return {"bytes": n_q * (in_bytes + 40) + nb + pb, "per_query": per_query}
+
+
 def run_suite(args):
-    """One JSON line per configuration of the scope (1M-query icosphere, rays on
+    for line in suite_records(args, args.only):
+        print(json.dumps(line), flush=True)
+
+
+def _compulsory(n, in_b, out_b, scene_bytes, ms, peak):
+    """Compulsory-traffic roofline: every query read and every result written once, plus
+    the scene's records, over the kernel time, against the HBM peak."""
+    b = n * (in_b + out_b) + scene_bytes
+    a = b / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "compulsory_bytes": int(b), "achieved": a, "peak": peak, "unit": "GB/s",
+            "frac": a / peak, "traffic": None}
+
+
+def suite_records(args, only_arg="", cpu_budget=6.0):
+    """One record per configuration of the scope (1M-query icosphere, rays on
     the 1M-triangle torus, 2D segments and silhouettes, 3D silhouettes on the
-    torus): GPU kernels timed with CUDA events on device-resident inputs (L2
-    flushed before each timed call), next to the reference CPU algorithm (the
-    oracle port, all host threads) on a bounded sample of the same inputs."""
+    torus, and on request contains / line of sight, instances, scene set-up, the
+    batch): GPU kernels timed with CUDA events on device-resident inputs (L2
+    flushed before each timed call), next to the reference's own CPU Scene
+    (its public bundled API, all host threads; the oracle's C restatement where
+    the reference is not available) on a bounded sample of the same inputs."""
     import torch
     import fcpw_gb300 as F
     from fcpw_gb300 import records as R
@@ -272,7 +391,9 @@ def run_suite(args):
             tot += a.elapsed_time(b)
         return tot / reps
 
-    def cpu_rate(fn, n_all, budget_s=6.0):
+    peak, _ = peaks()
+
+    def cpu_rate(fn, n_all, budget_s=cpu_budget):
         n0 = min(n_all, 8192)
         t = time.perf_counter()
         fn(n0)
@@ -315,22 +436,36 @@ def run_suite(args):
         plain_ms = timed(run)
         best, _ = autotune_closest_points(g, sph[: min(n, 1 << 20)])
         fast_ms = timed(run)
+        from fcpw_gb300.wide_format import layout
+        node_bytes = layout(best["branching"], best["bits"])["size"]
+        prim_bytes = 48 if dim == 3 else 24
+        alg = algorithmic_bytes(L, g, sph, out, n, node_bytes, prim_bytes, 20, packet=bool(best.get("packet")))
+        run()
         k = 1024
         d64 = g.closest_distances_f64_tensor(sph[:k].contiguous()).cpu().numpy()
         rel = np.abs(out[:k, 8].cpu().numpy().astype(np.float64) - d64) / d64
         nodes, prims, sils = s.cpu_bvh.export()
-        cpu = cpu_rate(lambda m: O.closest_points_bvh(dim, nodes, prims, R.make_spheres(pts[:m], R.FLT_MAX),
-                                                      nthreads=threads), n)
+        refs = reference_cpu(dim, v, idx, silhouettes=silhouettes)
+        if refs is not None:
+            cpu = reference_rate(refs, "closest", R.make_spheres(pts, R.FLT_MAX), budget_s=cpu_budget / 2)
+        else:
+            cpu = cpu_rate(lambda m: O.closest_points_bvh(dim, nodes, prims, R.make_spheres(pts[:m], R.FLT_MAX),
+                                                          nthreads=threads), n)
+        roof = _compulsory(n, 16, 40, nodes.nbytes + prims.nbytes, fast_ms, peak)
+        a = alg["bytes"] / (fast_ms / 1e3) / 1e9
+        roof.update({"algorithmic_bytes": alg["bytes"], "algorithmic_gbs": a, "algorithmic_frac": a / peak,
+                     "per_query": alg["per_query"],
+                     "time": "CUDA events around the whole call (sort, traversal, refinement)"})
         return s, g, {"config": name, "queries": n, "primitives": int(len(idx)),
                       "plain": {"queries_per_s": n / (plain_ms / 1e3), "ms": plain_ms},
                       "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms, "variant": best},
                       "speedup_vs_plain": plain_ms / fast_ms,
                       "accuracy": {"samples": k, "max_rel_err_vs_fp64": float(rel.max()),
                                    "mean_rel_err_vs_fp64": float(rel.mean())},
-                      "cpu_baseline": cpu}
+                      "roofline": roof, "cpu_baseline": cpu}
 
     lines = []
-    only = set(args.only.split(",")) if args.only else None
+    only = set(only_arg.split(",")) if only_arg else None
 
     def want(name):
         return only is None or name in only
@@ -391,8 +526,28 @@ def run_suite(args):
         g.set_traversal(*wb_best[:2], sort_queries=wb_best[2], packet=wb_best[3])
         fast_ms = timed(ray_run)
         nodes, prims, _ = s.cpu_bvh.export()
-        cpu = cpu_rate(lambda m: O.intersect_rays_bvh(3, nodes, prims, rays_np[:m], nthreads=threads), n)
+        refs = reference_cpu(3, v, f)
+        if refs is not None:
+            cpu = reference_rate(refs, "rays", rays_np, budget_s=cpu_budget / 2)
+        else:
+            cpu = cpu_rate(lambda m: O.intersect_rays_bvh(3, nodes, prims, rays_np[:m], nthreads=threads), n)
+        del refs
+        # FP64 hit parameter of the triangle each of 1024 rays hit (the plane through its vertices)
+        res = out[:1024].cpu().numpy().view(R.INTERACTION).reshape(-1)
+        hk = np.nonzero(res["index"] != R.UINT_MAX)[0]
+        pos = np.empty(len(prims), np.int64)
+        pos[prims["index"].astype(np.int64)] = np.arange(len(prims))
+        pk = pos[res["index"][hk].astype(np.int64)]
+        a, b, c = (prims[x][pk].astype(np.float64) for x in ("pa", "pb", "pc"))
+        nrm = np.cross(b - a, c - a)
+        ro, rd = o[hk].astype(np.float64), d[hk].astype(np.float64)
+        t64 = np.einsum("ij,ij->i", nrm, a - ro) / np.einsum("ij,ij->i", nrm, rd)
+        rel_t = np.abs(res["d"][hk].astype(np.float64) - t64) / t64
         lines.append({"config": "rays, torus 1,048,576 triangles, 4,194,304 rays (first hit)", "queries": n,
+                      "accuracy": {"samples": int(len(hk)), "max_rel_err_vs_fp64": float(rel_t.max()),
+                                   "mean_rel_err_vs_fp64": float(rel_t.mean()),
+                                   "what": "hit distance against the FP64 plane parameter of the same triangle"},
+                      "roofline": _compulsory(n, 40, 40, nodes.nbytes + prims.nbytes, fast_ms, peak),
                       "plain": {"queries_per_s": n / (ray_ms / 1e3), "ms": ray_ms},
                       "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms,
                                "variant": {"branching": wb_best[0], "bits": wb_best[1], "sort_queries": wb_best[2],
@@ -416,10 +571,19 @@ def run_suite(args):
         times = sil_times(g2, sph, flip, out, n)
         nodes, _, sils = s2.cpu_bvh.export()
         zf = np.zeros(n, np.uint32)
-        cpu = cpu_rate(lambda m: O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts2[:m], R.FLT_MAX), zf[:m],
-                                                   nthreads=threads), n)
+        refs = reference_cpu(2, v, sg, silhouettes=True)
+        if refs is not None:
+            cpu = reference_rate(refs, "silhouettes", R.make_spheres(pts2, R.FLT_MAX), flip=zf,
+                                 budget_s=cpu_budget / 2)
+        else:
+            cpu = cpu_rate(lambda m: O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts2[:m], R.FLT_MAX), zf[:m],
+                                                       nthreads=threads), n)
+        del refs
         lines.append({"config": "2D stars 131,072 segments, 8,388,608 closest-silhouette queries (flip 0)",
-                      "queries": n, **times, "cpu_baseline": cpu})
+                      "queries": n, **times,
+                      "roofline": _compulsory(n, 20, 40, nodes.nbytes + sils.nbytes, times["fast"]["ms"], peak),
+                      "accuracy": "no FP64 silhouette oracle; parity with the reference's answers is tested",
+                      "cpu_baseline": cpu})
         del g2, s2
 
     # 3D silhouettes on the 1M-triangle torus (SNCH), 4,194,304 queries in [-2, 2]^3
@@ -440,11 +604,22 @@ def run_suite(args):
         times = sil_times(g, sph, flip, out, n)
         nodes, _, sils = s.cpu_bvh.export()
         zf = np.zeros(n, np.uint32)
-        cpu = None if args.no_cpu_baseline else cpu_rate(
-            lambda m: O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pts[:m], R.FLT_MAX), zf[:m], nthreads=threads),
-            n)
+        cpu = None
+        if not args.no_cpu_baseline:
+            refs = reference_cpu(3, v, f, silhouettes=True)
+            if refs is not None:
+                cpu = reference_rate(refs, "silhouettes", R.make_spheres(pts, R.FLT_MAX), flip=zf,
+                                     budget_s=cpu_budget / 2)
+            else:
+                cpu = cpu_rate(lambda m: O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pts[:m], R.FLT_MAX), zf[:m],
+                                                           nthreads=threads), n)
+            del refs
         lines.append({"config": f"3D silhouettes, torus 1,048,576 triangles (SNCH), {n:,} queries (flip 0)",
-                      "queries": n, **times, "cpu_baseline": cpu})
+                      "queries": n, **times,
+                      "roofline": _compulsory(n, 20, 40, nodes.nbytes + sils.nbytes, times["fast"]["ms"], peak),
+                      "accuracy": "no FP64 silhouette oracle; parity with the reference's answers is tested",
+                      "cpu_baseline": cpu})
+        del g, s
 
     # contains / line of sight (CPU-only in the reference) on the 1M-triangle torus
     if want("inside"):
@@ -579,8 +754,7 @@ def run_suite(args):
     if want("batch") and only is not None:
         lines.append({"config": "batched uneven scenes", **batched_scenes_bench(0)})
 
-    for line in lines:
-        print(json.dumps(line), flush=True)
+    return lines
 
 
 def _schedule(c) -> str:
@@ -733,20 +907,7 @@ def run_ours(args):
         check(L.fcpwgb_find_closest_points_device(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, 0, sptr))
 
     def traversal_stats(node_bytes, prim_bytes, in_bytes, packet=False):
-        stats = (C.c_uint64 * 8)()
-        check(L.fcpwgb_closest_points_traversal_stats(gpu.handle, spheres.data_ptr(), out.data_ptr(), n, stats))
-        n_q, n_pop, n_inner, n_prim, w_rec, w_prim = [int(x) for x in stats[:6]]
-        if node_bytes == 32:  # binary: every expansion loads two 32 B child records, plus the root
-            nb, pb = 32 * (n_q + 2 * n_inner), prim_bytes * n_prim
-        elif packet:  # warp packets: one record / triangle load serves the 32 queries of a warp
-            nb, pb = node_bytes * w_rec, prim_bytes * w_prim
-        else:  # wide, a thread per query: every expansion loads one record holding all child boxes
-            nb, pb = node_bytes * n_inner, prim_bytes * n_prim
-        per_query = {"nodes_popped": n_pop / n_q if node_bytes == 32 else n_inner / n_q,
-                     "inner_expanded": n_inner / n_q, "prim_tests": n_prim / n_q}
-        if packet:
-            per_query.update({"warp_record_loads": w_rec / n_q, "warp_prim_loads": w_prim / n_q})
-        return {"bytes": n_q * (in_bytes + 40) + nb + pb, "per_query": per_query}
+        return algorithmic_bytes(L, gpu, spheres, out, n, node_bytes, prim_bytes, in_bytes, packet)
 
     def timed(steps, warmup):
         for _ in range(warmup):
@@ -797,6 +958,35 @@ def run_ours(args):
     ms_max = max_over_ranks(ms, world, dev)
     value = world * n / (ms_max / 1e3)
 
+    # quantised child boxes: the best 4- or 8-wide, one-thread or packet variant per precision, all queries
+    quantised = {}
+    if args.variant == "auto" and not args.no_quantised:
+        for bits in (8, 16):
+            rows = []
+            for br in (4, 8):
+                for sch in ("thread", "packet"):
+                    cfg = dict(best, branching=br, bits=bits, persistent=False, packet=sch == "packet", leaf_size=0,
+                               short_stack=16)
+                    try:
+                        gpu.set_traversal(**cfg)
+                        rows.append((cfg, timed(3, 2)[0]))
+                    except Exception:  # a layout this tree cannot be encoded in is skipped
+                        pass
+            if rows:
+                cfg, qms = min(rows, key=lambda t: t[1])
+                gpu.set_traversal(**cfg)
+                step()
+                d64q = gpu.closest_distances_f64_tensor(spheres[:1024]).cpu().numpy()
+                relq = np.abs(out[:1024, 8].cpu().numpy().astype(np.float64) - d64q) / d64q
+                quantised[f"q{bits}"] = {
+                    "variant": f"wide{cfg['branching']}_q{bits}_" + _schedule(cfg),
+                    "queries_per_s": world * n / (qms / 1e3), "ms_per_step": qms,
+                    "speedup_vs_plain": plain_ms / qms, "vs_float_boxes": ms / qms,
+                    "accuracy": {"samples": 1024, "max_rel_err_vs_fp64": float(relq.max()),
+                                 "mean_rel_err_vs_fp64": float(relq.mean())},
+                    "all_ms": {f"wide{c['branching']}_q{bits}_" + _schedule(c): round(t, 3) for c, t in rows}}
+        gpu.set_traversal(**best)
+
     # end to end through the host-array C ABI call (pinned host buffers, copies inside)
     h_sph = torch.empty((n, 4), dtype=torch.float32, pin_memory=True)
     h_sph.copy_(spheres.cpu())
@@ -824,7 +1014,7 @@ def run_ours(args):
         peak, peak_kind = peaks()
         achieved = fast_stats["bytes"] / (kms / 1e3) / 1e9
         variant = f"wide{best['branching']}_q{best['bits']}_" + _schedule(best)
-        traffic = profiled_traffic(variant)
+        l2_peak = measure_l2_gbs(dev)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -846,14 +1036,19 @@ def run_ours(args):
             # the spatial sort (when on), then the traversal kernel and the precise mode's refinement pass
             "gpu_launches": args.steps * ((7 if best.get("sort_queries", True) else 1) + 1),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": f"hbm_gbs ({peak_kind})",
+                         "frac": achieved / peak, "traffic": None, "peak_source": f"hbm_gbs ({peak_kind})",
                          "kernel": ("kWidePacketClosestPoint" if best.get("packet") else "kWideClosestPoint")
                          + " + kRefineClosest",
                          "kernel_ms": kms,  # CUDA events around both kernels of the precise launch
                          "algorithmic_bytes_per_launch": fast_stats["bytes"], "per_query": fast_stats["per_query"],
-                         "limiter": "instruction issue (70-72 % of active cycles in ncu) on an L2-resident working set "
-                                    "(records and triangles, 57 MB); DRAM moves ~166 B per query "
-                                    "(profiles/closest_point_wide4_q32_packet_torus1M.md)"},
+                         # the records and triangles (24-57 MB) stay in L2, so the loads counted above are
+                         # served by L2: the ceiling that applies is L2 throughput and instruction issue
+                         "l2": {"achieved": achieved, "peak": l2_peak, "unit": "GB/s", "frac": achieved / l2_peak,
+                                "peak_source": "measured in this run: best of a read and a copy of a 32 MiB "
+                                               "L2-resident buffer"},
+                         "limiter": "instruction issue and dependent L2 loads of an L2-resident tree; DRAM traffic "
+                                    "is below the algorithmic bytes (ncu, profiles/)"},
+            "quantised": quantised,
             "clocks": clocks, "accuracy": accuracy,
         }
         if not args.no_loss:
@@ -861,7 +1056,10 @@ def run_ours(args):
         if not args.no_batch:
             result["batched_scenes"] = batched_scenes_bench(local)
         if world == 1 and not args.no_cpu_baseline:
-            result["cpu_baseline"] = cpu_baseline(scene, pts)
+            result["cpu_baseline"] = cpu_baseline(v, f, pts)
+        if not args.no_suite:
+            del gpu
+            result["suite"] = suite_records(args, "c1,rays,c3,sil3d", cpu_budget=4.0)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
@@ -870,39 +1068,78 @@ def run_ours(args):
 
 
 def run_reference(args):
-    """The reference CPU implementation of the path (its C restatement, all host threads)."""
+    """The reference's own CPU implementation of the path: its Scene<3> built by its own
+    SAH build and queried through its public bundled API (Scene::findClosestPoints over
+    std::vector, one std::thread per hardware thread), compiled on this host from its
+    headers (oracle/_ref). The scalar Bvh (the configuration's comparator) and the
+    vectorised Mbvh (Enoki, FCPW_SIMD_WIDTH=4) are both measured on the warm-up calls;
+    the faster one is timed on every step, all queries of the workload per step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from fcpw_gb300 import records as R
-    from oracle import oracle as O
+    from oracle import reference as REF
+    base = {"impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded torus + uniform queries)"}
+    if not REF.available():
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's CPU headers are not staged on this "
+                                                              "host (oracle/build.py), so it cannot be compiled"}))
+        return
     v, f, pts = make_workload(0, args.queries)
-    scene, _ = build_scene(v, f)
-    nodes, prims, _ = scene.cpu_bvh.export()
+    n = len(pts)
     threads = os.cpu_count() or 1
-    sample = min(len(pts), 262_144)
-    sph = R.make_spheres(pts[:sample], R.FLT_MAX)
-    for _ in range(args.warmup):
-        O.closest_points_bvh(3, nodes, prims, sph[: sample // 8], nthreads=threads)
+    t0 = time.perf_counter()
+    refs = reference_cpu(3, v, f)
+    build_s = time.perf_counter() - t0
+    sph = R.make_spheres(pts, R.FLT_MAX)
+    m = max(1, n // 16)
+    warm = {}
+    for name in ("scalar", "vectorized"):
+        if refs.get(name) is None:
+            continue
+        secs = [refs[name].closest_points_timed(sph[:m])[1] for _ in range(max(1, args.warmup))]
+        warm[name] = m / min(secs)
+    best = max(warm, key=warm.get)
+    # every step answers all n queries unless K such steps would take more than about 4 minutes
+    budget_s = 240.0
+    sample = n if args.steps * n / warm[best] <= budget_s else max(m, int(budget_s * warm[best] / args.steps))
     times = []
-    for i in range(args.steps):
-        t = time.perf_counter()
-        O.closest_points_bvh(3, nodes, prims, sph, nthreads=threads)
-        times.append(time.perf_counter() - t)
+    for _ in range(args.steps):
+        out, sec = refs[best].closest_points_timed(sph[:sample])
+        times.append(sec)
     ms = 1e3 * sum(times) / len(times)
     value = sample / (ms / 1e3)
-    desc = (f"{sample} of the {len(pts)} queries per step, oracle/fcpw_oracle.c closest_point_bvh "
-            f"(reference bvh.inl:1291-1418 restated), {threads} threads")
+    builds = {best: {"queries_per_s": value, "queries_per_step": sample, "ms_per_step": ms}}
+    other = [k for k in warm if k != best]
+    if other:
+        sec = refs[other[0]].closest_points_timed(sph[:sample])[1]
+        builds[other[0]] = {"queries_per_s": sample / sec, "queries_per_step": sample, "ms_per_step": 1e3 * sec,
+                            "note": "one call, for the record"}
+    width = REF.simd_width() if "vectorized" in warm else 0
+    desc = (f"{sample:,} of the {n:,} queries per step through the reference's Scene<3>::findClosestPoints "
+            f"({best}{f', Mbvh FCPW_SIMD_WIDTH={width}' if best == 'vectorized' else ', binary SAH Bvh'}), its own "
+            f"std::thread split over {threads} hardware threads; timed inside the call")
     print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded torus + uniform queries)",
+        **base, "value": value, "ms_per_step": ms,
         "config": {"workload": "closest point, seeded torus 1,048,576 triangles, 4,194,304 queries "
-                               "uniform in [-2,2]^3 per GPU, r2 = FLT_MAX, binary SAH BVH",
-                   "sample_queries_per_step": sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+                               "uniform in [-2,2]^3 per GPU, r2 = FLT_MAX, SAH BVH",
+                   "queries_per_step": sample, "same_config": sample == n, "build": best,
+                   "reference_build_s": round(build_s, 2), "builds": builds,
+                   "host": {"machine": platform.machine(), "cpu": _cpu_model(), "threads": threads}},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "reference", "sample": desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def _cpu_model() -> str:
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part", "hardware")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or "unknown"
 
 
 if __name__ == "__main__":

@@ -106,11 +106,13 @@ def _build_ref(out: Path, extra: list[str], force: bool) -> Path | None:
     if not force and out.exists() and out.stat().st_mtime >= newest:
         return out
     tmp = out.with_suffix(".so.tmp")
-    cmd = [_cxx(), "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread", *extra,
+    cmd = [_cxx(), "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread", "-Wno-psabi", *extra,
            "-I", str(HERE / "compat"), "-I", str(inc), str(HERE / "ref_driver.cpp"), "-o", str(tmp)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"reference build failed ({out.name}):\n{r.stderr[-6000:]}")
+        errors = [ln for ln in r.stderr.splitlines() if "error" in ln]
+        raise RuntimeError(f"reference build failed ({out.name}):\n" + "\n".join(errors[:20]) + "\n" +
+                           r.stderr[-3000:])
     os.replace(tmp, out)
     return out
 

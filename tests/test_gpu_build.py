@@ -102,7 +102,7 @@ def test_rays_and_refit_on_device_tree():
     nodes, prims, _ = O.lbvh_build(3, v, f, 4)
     rays = R.make_rays(o, d, np.full(5000, R.FLT_MAX, np.float32))
     ref, hit = O.intersect_rays_bvh(3, nodes, prims, rays)
-    compare_rays(out.array(), ref, hit)
+    compare_rays(3, prims, rays, out.array(), ref, hit)
     # moved vertices: the device refit of the built tree equals the oracle's
     # refit of the model tree over the moved primitives, and so do the queries
     moved = (v * 1.05).astype(np.float32)
