@@ -758,10 +758,12 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
 
 
 def _schedule(c) -> str:
-    s = "packet" if c.get("packet") else ("persistent" if c.get("persistent") else "thread")
+    lanes = c.get("threads_per_query", 1)
+    s = "packet" if c.get("packet") else (f"coop{lanes}" if lanes > 1 else
+                                          ("persistent" if c.get("persistent") else "thread"))
     if c.get("leaf_size"):
         s += f"+leaf{c['leaf_size']}"
-    if not c.get("packet") and c.get("short_stack", 16) != 16:
+    if not c.get("packet") and lanes == 1 and c.get("short_stack", 16) != 16:
         s += f"+stack{c['short_stack']}"
     return s
 
@@ -942,10 +944,11 @@ def run_ours(args):
     sample = spheres[: min(n, 1 << 20)]
     if args.variant == "auto":
         best, table = autotune_closest_points(gpu, sample)
-    else:  # fixed "branching,bits,schedule" (0 thread, 1 persistent, 2 packet), e.g. for profiling one kernel
+    else:  # fixed "branching,bits,schedule" (0 thread, 1 persistent, 2 packet, 3/4/5 groups of 2/4/8 lanes),
+        # e.g. for profiling one kernel
         b, q, p = (int(x) for x in args.variant.split(","))
         best = {"branching": b, "bits": q, "persistent": p == 1, "packet": p == 2, "sort_queries": True,
-                "precise": True}
+                "precise": True, "threads_per_query": {3: 2, 4: 4, 5: 8}.get(p, 1)}
         gpu.set_traversal(**best)
         table = []
     from fcpw_gb300.wide_format import layout

@@ -99,7 +99,7 @@ class BvhInfo(C.Structure):
 class TraversalConfig(C.Structure):
     _fields_ = [("branching", c_int), ("bits", c_int), ("block_size", c_int), ("sort_queries", c_int),
                 ("persistent", c_int), ("precise", c_int), ("packet", c_int), ("leaf_size", c_int),
-                ("short_stack", c_int)]
+                ("short_stack", c_int), ("threads_per_query", c_int)]
 
 
 class FcpwError(RuntimeError):

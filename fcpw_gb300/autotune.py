@@ -1,7 +1,9 @@
 """Autotuner of the closest point traversal: times candidate variants on a
 sample of the caller's queries and keeps the fastest. Stage 1 covers the
 branching factor (2/4/8), the child box precision (8/16/32 bits) and the
-schedule (a thread per query, persistent blocks, or warp packets); stage 2
+schedule (a thread per query, persistent blocks, warp packets, or a group
+of 2, 4 or 8 lanes per query that splits each record's child boxes and each
+leaf's primitives); stage 2
 tries merged leaves (subtrees of up to 6, 8 or 12 primitives as one leaf) on
 the stage-1 winner; stage 3, for the one-thread-per-query schedules, the
 stack placement: 16 entries per thread in shared memory (the default) or the
@@ -11,9 +13,15 @@ from __future__ import annotations
 import itertools
 
 # schedule: "thread" = one thread per query, "persistent" = persistent blocks
-# with neighbour seeding, "packet" = the queries of a warp traverse together
-DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "persistent", "packet"],
+# with neighbour seeding, "packet" = the queries of a warp traverse together,
+# "coopL" = L lanes (2, 4, 8) answer one query together
+DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32],
+                 "schedule": ["thread", "persistent", "packet", "coop2", "coop4", "coop8"],
                  "leaf_size": [6, 8, 12], "short_stack": [0]}
+
+
+def lanes_of(schedule: str) -> int:
+    return int(schedule[4:]) if schedule.startswith("coop") else 1
 
 
 def candidates(space=None, sort_queries=True, precise=True):
@@ -21,7 +29,8 @@ def candidates(space=None, sort_queries=True, precise=True):
     space = dict(DEFAULT_SPACE, **(space or {}))
     for b, q, sch in itertools.product(space["branching"], space["bits"], space["schedule"]):
         yield {"branching": b, "bits": q, "persistent": sch == "persistent", "packet": sch == "packet",
-               "sort_queries": sort_queries, "precise": precise, "leaf_size": 0, "short_stack": 16}
+               "sort_queries": sort_queries, "precise": precise, "leaf_size": 0, "short_stack": 16,
+               "threads_per_query": lanes_of(sch)}
 
 
 def staged_search(measure, space=None, sort_queries=True, precise=True):
@@ -42,7 +51,7 @@ def staged_search(measure, space=None, sort_queries=True, precise=True):
     for leaf in space["leaf_size"]:
         run(dict(best, leaf_size=leaf))
     best = min(table, key=lambda t: t[1])[0]
-    if not best["packet"]:
+    if not best["packet"] and best.get("threads_per_query", 1) == 1:
         for short in space["short_stack"]:
             run(dict(best, short_stack=short))
     best = min(table, key=lambda t: t[1])[0]

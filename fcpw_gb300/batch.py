@@ -56,10 +56,11 @@ class _GPUSceneBatch:
         self._n_scenes = len(bvhs)
 
     def set_traversal(self, branching: int = 8, bits: int = 8, persistent: bool = False,
-                      precise: bool = True, packet: bool = False, leaf_size: int = 0, short_stack: int = 16) -> None:
+                      precise: bool = True, packet: bool = False, leaf_size: int = 0, short_stack: int = 16,
+                      threads_per_query: int = 1) -> None:
         from ._lib import TraversalConfig
         cfg = TraversalConfig(int(branching), int(bits), 128, 1, int(bool(persistent)), int(bool(precise)),
-                              int(bool(packet)), int(leaf_size), int(short_stack))
+                              int(bool(packet)), int(leaf_size), int(short_stack), int(threads_per_query))
         check(lib().fcpwgb_gpu_batch_set_traversal(self._h, C.byref(cfg)))
 
     def get_traversal(self) -> dict:
@@ -148,7 +149,7 @@ def autotune_batch(batch: _GPUSceneBatch, spheres, query_offsets, space=None, re
 
     def set_cfg(cfg):
         batch.set_traversal(cfg["branching"], cfg["bits"], cfg["persistent"], precise, cfg["packet"],
-                            cfg["leaf_size"], cfg["short_stack"])
+                            cfg["leaf_size"], cfg["short_stack"], cfg.get("threads_per_query", 1))
 
     def measure(cfg):
         set_cfg(cfg)

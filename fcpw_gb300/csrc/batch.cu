@@ -32,7 +32,7 @@ struct BatchScene {
 
 struct GraphKey {
     const void *spheres, *out, *nodes, *prims, *cells, *perm, *sorted, *roots, *grids, *offsets, *sel;
-    uint32_t n, recordNormal, branching, bits, persistent, precise, sort, packet, leaf, shortStack;
+    uint32_t n, recordNormal, branching, bits, persistent, precise, sort, packet, leaf, shortStack, lanes;
     bool operator==(const GraphKey &o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
 };
 
@@ -255,7 +255,8 @@ int enqueue(fcpwgb_gpu_batch *b, const DevSphere *spheres, DevInteraction *out, 
     uint32_t blocks = (n + 127) / 128;
     l.packet = b->cfg.packet;
     l.shortStack = b->cfg.shortStack;
-    if (b->cfg.persistent && !b->cfg.packet) {
+    l.lanes = b->cfg.lanes;
+    if (b->cfg.persistent && !b->cfg.packet && b->cfg.lanes == 1) {
         if ((e = cudaMemsetAsync(b->counter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)b->counter.ptr;
         blocks = std::min<uint32_t>(blocks, (uint32_t)b->numSMs * 8u);
@@ -292,6 +293,7 @@ int runDevice(fcpwgb_gpu_batch *b, const DevSphere *spheres, const uint32_t *off
     k.packet = (uint32_t)b->cfg.packet;
     k.leaf = (uint32_t)b->cfg.leafSize;
     k.shortStack = (uint32_t)b->cfg.shortStack;
+    k.lanes = (uint32_t)b->cfg.lanes;
     cudaError_t e;
     if (!b->exec || !(k == b->key)) {
         b->dropGraph();
@@ -416,6 +418,11 @@ extern "C" int fcpwgb_gpu_batch_set_traversal(fcpwgb_gpu_batch *b, const fcpwgb_
     if (c->leaf_size < 0 || c->leaf_size > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf_size must be 0..15");
     if (c->short_stack != 0 && c->short_stack != 16)
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0 or 16");
+    if (!(c->threads_per_query == 1 || c->threads_per_query == 2 || c->threads_per_query == 4 ||
+          c->threads_per_query == 8))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "threads_per_query must be 1, 2, 4 or 8");
+    if (c->threads_per_query > 1 && c->packet)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "threads_per_query > 1 and packet are exclusive");
     b->dropGraph();
     b->cfg.branching = c->branching;
     b->cfg.bits = c->bits;
@@ -425,6 +432,7 @@ extern "C" int fcpwgb_gpu_batch_set_traversal(fcpwgb_gpu_batch *b, const fcpwgb_
     b->cfg.packet = c->packet != 0;
     b->cfg.leafSize = c->leaf_size;
     b->cfg.shortStack = c->short_stack;
+    b->cfg.lanes = c->threads_per_query;
     return FCPWGB_OK;
 }
 
@@ -439,6 +447,7 @@ extern "C" int fcpwgb_gpu_batch_get_traversal(const fcpwgb_gpu_batch *b, fcpwgb_
     c->packet = b->cfg.packet;
     c->leaf_size = b->cfg.leafSize;
     c->short_stack = b->cfg.shortStack;
+    c->threads_per_query = b->cfg.lanes;
     return FCPWGB_OK;
 }
 

@@ -896,6 +896,11 @@ extern "C" int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *s, const fcpwgb_
     if (c->leaf_size < 0 || c->leaf_size > 15) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "leaf_size must be 0..15");
     if (c->short_stack != 0 && c->short_stack != 16)
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "short_stack must be 0 or 16");
+    if (!(c->threads_per_query == 1 || c->threads_per_query == 2 || c->threads_per_query == 4 ||
+          c->threads_per_query == 8))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "threads_per_query must be 1, 2, 4 or 8");
+    if (c->threads_per_query > 1 && c->packet)
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "threads_per_query > 1 and packet are exclusive");
     WideConfig w;
     w.branching = c->branching;
     w.bits = c->bits;
@@ -906,6 +911,7 @@ extern "C" int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *s, const fcpwgb_
     w.packet = c->packet != 0;
     w.leafSize = c->leaf_size;
     w.shortStack = c->short_stack;
+    w.lanes = c->threads_per_query;
     s->wideConfig = w;
     return FCPWGB_OK;
 }
@@ -921,6 +927,7 @@ extern "C" int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *s, fcpwgb_
     c->packet = s->wideConfig.packet;
     c->leaf_size = s->wideConfig.leafSize;
     c->short_stack = s->wideConfig.shortStack;
+    c->threads_per_query = s->wideConfig.lanes;
     return FCPWGB_OK;
 }
 

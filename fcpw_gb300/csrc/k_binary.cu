@@ -3,6 +3,7 @@
 // the reference GPU path (include/fcpw/gpu/bvh.slang). These are the parity
 // kernels; the wide/quantised kernels in k_wide.cu are the fast path.
 #include "kernels.h"
+#include "binary_queries.cuh"
 #include "silhouette.cuh"
 
 namespace fcpwgb {
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(256) kRayBinary(const unsigned char *__restric
 
 // ------------------------------------------------- sphere sampling
 // Bvh.intersect(sphere, randNums) with constant branch weights, bvh.slang:257-392
+// (sphereSampleBinary, binary_queries.cuh)
 template<class Prim, int NODE_STRIDE>
 __global__ void __launch_bounds__(256) kSphereSampleBinary(const unsigned char *__restrict__ nodes,
                                                            const unsigned char *__restrict__ prims,
@@ -180,102 +182,15 @@ __global__ void __launch_bounds__(256) kSphereSampleBinary(const unsigned char *
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     float4 s4 = ldg4(spheres + q);
-    float3 c = make_float3(s4.x, s4.y, s4.z);
-    float r2 = s4.w;
-    float3 rn = randNums[q];
-    DevInteraction best = defaultInteraction();
-    uint32_t selected = kUintMax;
-    bool didIntersect = false;
-
-    NodeBox root = loadNode<NODE_STRIDE>(nodes, 0);
-    float d2Min, d2Max;
-    boxSphereDist(root.pMin, root.pMax, c, d2Min, d2Max);
-    if (d2Min <= r2) {
-        float maxDistToChild = d2Max;
-        float traversalPdf = 1.0f;
-        float u = rn.x;
-        uint32_t ni = 0;
-        for (uint32_t step = 0; step <= depthLimit; step++) {
-            NodeBox node = loadNode<NODE_STRIDE>(nodes, ni);
-            if (node.nPrims > 0) {
-                float total = 0.0f;
-                for (uint32_t p = 0; p < node.nPrims; p++) {
-                    uint32_t pi = node.offset + p;
-                    Prim prim = Prim::load(prims, pi);
-                    DevInteraction cI = defaultInteraction();
-                    bool hit = false;
-                    if (maxDistToChild <= r2) {
-                        hit = true;
-                        cI.d = prim.surfaceArea();
-                        cI.index = prim.index;
-                    } else {
-                        float3 pt;
-                        float2 uv;
-                        float d = prim.closestPoint(c, pt, uv);
-                        if (d * d <= r2) {
-                            hit = true;
-                            cI.p = pt;
-                            cI.uv = uv;
-                            cI.d = prim.surfaceArea();
-                            cI.index = prim.index;
-                        }
-                    }
-                    if (hit) {
-                        didIntersect = true;
-                        total += cI.d;
-                        float prob = cI.d / total;
-                        if (u < prob) {
-                            u = u / prob;
-                            best = cI;
-                            best.d *= traversalPdf;
-                            selected = pi;
-                        } else {
-                            u = (u - prob) / (1.0f - prob);
-                        }
-                    }
-                }
-                if (total > 0.0f) best.d /= total;
-                break;
-            }
-            uint32_t li = ni + 1, ri = ni + node.offset;
-            NodeBox l = loadNode<NODE_STRIDE>(nodes, li);
-            NodeBox r = loadNode<NODE_STRIDE>(nodes, ri);
-            float l0, l1, r0, r1;
-            boxSphereDist(l.pMin, l.pMax, c, l0, l1);
-            boxSphereDist(r.pMin, r.pMax, c, r0, r1);
-            float wl = l0 <= r2 ? 1.0f : 0.0f;
-            float wr = r0 <= r2 ? 1.0f : 0.0f;
-            float total = wl + wr;
-            if (!(total > 0.0f)) break;
-            float pl = wl / total, pr = 1.0f - pl;
-            if (u < pl) {
-                u = u / pl;
-                ni = li;
-                traversalPdf *= pl;
-                maxDistToChild = l1;
-            } else {
-                u = (u - pl) / pr;
-                ni = ri;
-                traversalPdf *= pr;
-                maxDistToChild = r1;
-            }
-            if (step == depthLimit) atomicOr(errorWord, kErrStepBudget);
-        }
-    }
-    if (didIntersect) {
-        if (best.index == kUintMax || selected == kUintMax) {
-            didIntersect = false;
-        } else {
-            Prim prim = Prim::load(prims, selected);
-            float pdf = prim.samplePoint(make_float2(rn.y, rn.z), best.uv, best.p, best.n);
-            best.d *= pdf;
-        }
-    }
-    out[q] = didIntersect ? best : defaultInteraction();
+    DevInteraction best;
+    sphereSampleBinary<Prim, NODE_STRIDE>(nodes, prims, make_float3(s4.x, s4.y, s4.z), s4.w, randNums[q], depthLimit,
+                                          errorWord, best);
+    out[q] = best;
 }
 
 // ------------------------------------------- closest silhouette point
-// Bvh.findClosestSilhouettePoint, bvh.slang:505-646 (SNCH nodes only)
+// Bvh.findClosestSilhouettePoint, bvh.slang:505-646 (SNCH nodes only; silhouetteBinary,
+// binary_queries.cuh)
 template<class Sil, int DIM>
 __global__ void __launch_bounds__(256) kSilhouetteBinary(const unsigned char *__restrict__ nodes,
                                                          const unsigned char *__restrict__ sils,
@@ -288,66 +203,10 @@ __global__ void __launch_bounds__(256) kSilhouetteBinary(const unsigned char *__
     if (q >= n) return;
     const uint32_t src = perm ? __ldg(perm + q) : q;  // sorted queries: the caller's slot
     float4 s4 = ldg4(spheres + q);
-    float3 c = make_float3(s4.x, s4.y, s4.z);
     float r2 = s4.w;
-    bool flipNormal = __ldg(flip + src) != 0;
-    DevInteraction best = defaultInteraction();
-
-    if (!(sqMinR >= r2)) {
-        uint32_t stack[kStackDepth];
-        NodeBox root = loadNode<64>(nodes, 0);
-        if (boxSphereD2Min(root.pMin, root.pMax, c) <= r2) {
-            stack[0] = 0;
-            int sp = 0;
-            while (sp >= 0) {
-                uint32_t ni = stack[sp--];
-                NodeBox node = loadNode<64>(nodes, ni);
-                if (!(boxSphereD2Min(node.pMin, node.pMax, c) <= r2)) continue;
-                if (node.nPrims > 0) {
-                    NodeCone cone = loadCone(nodes, ni);
-                    for (uint32_t p = 0; p < cone.nSil; p++) {
-                        Sil sil = Sil::load(sils, cone.silOffset + p);
-                        if (sil.index == best.index) continue;  // already checked
-                        DevInteraction cI = defaultInteraction();
-                        if (sil.closestSilhouettePoint(c, r2, flipNormal, sqMinR, precision, cI)) {
-                            r2 = fminf(r2, cI.d * cI.d);
-                            best = cI;
-                            if (sqMinR >= r2) break;
-                        }
-                    }
-                } else {
-                    uint32_t li = ni + 1, ri = ni + node.offset;
-                    float dl = 0.0f, dr = 0.0f;
-                    NodeCone lc = loadCone(nodes, li);
-                    bool hitL = lc.halfAngle >= 0.0f;
-                    if (hitL) {
-                        NodeBox lb = loadNode<64>(nodes, li);
-                        dl = boxSphereD2Min(lb.pMin, lb.pMax, c);
-                        hitL = dl <= r2;
-                        if (hitL) hitL = coneOverlap<DIM>(lc.axis, lc.halfAngle, lc.radius, c, lb.pMin, lb.pMax, dl);
-                    }
-                    NodeCone rc = loadCone(nodes, ri);
-                    bool hitR = rc.halfAngle >= 0.0f;
-                    if (hitR) {
-                        NodeBox rb = loadNode<64>(nodes, ri);
-                        dr = boxSphereD2Min(rb.pMin, rb.pMax, c);
-                        hitR = dr <= r2;
-                        if (hitR) hitR = coneOverlap<DIM>(rc.axis, rc.halfAngle, rc.radius, c, rb.pMin, rb.pMax, dr);
-                    }
-                    if (hitL && hitR) {
-                        uint32_t closer = li, other = ri;
-                        if (dr < dl) { closer = ri; other = li; }
-                        if (sp + 2 >= kStackDepth) { atomicOr(errorWord, kErrStackOverflow); break; }
-                        stack[++sp] = other;
-                        stack[++sp] = closer;
-                    } else if (hitL || hitR) {
-                        if (sp + 1 >= kStackDepth) { atomicOr(errorWord, kErrStackOverflow); break; }
-                        stack[++sp] = hitL ? li : ri;
-                    }
-                }
-            }
-        }
-    }
+    DevInteraction best;
+    silhouetteBinary<Sil, DIM>(nodes, sils, make_float3(s4.x, s4.y, s4.z), r2, __ldg(flip + src) != 0, sqMinR,
+                               precision, errorWord, best);
     out[src] = best;
 }
 

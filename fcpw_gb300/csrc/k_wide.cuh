@@ -898,6 +898,10 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
     }
 }
 
+}  // namespace fcpwgb
+#include "k_wide_coop.cuh"
+namespace fcpwgb {
+
 // Ray first hit / occlusion on a wide tree, one thread per ray, with the
 // semantics of bvh.slang:144-254: a child is entered when the slab test with
 // the parallel-slab guard passes against the current tMax, nearest entry
@@ -1215,10 +1219,24 @@ __global__ void kRequantize(unsigned char *wideNodes, const int32_t *childBinary
     for (int k = 0; k < WideLayout<W, BITS>::kSize; k++) dst[k] = rec[k];
 }
 
+template<int W, int B, class Prim, bool PRECISE, bool STATS, int L>
+void launchCoop(const WideLaunch &l, cudaStream_t s) {
+    constexpr uint32_t perBlock = kWideBlock / L;
+    kWideCoopClosestPoint<W, B, Prim, PRECISE, STATS, L><<<dim3((l.n + perBlock - 1) / perBlock), dim3(kWideBlock),
+                                                          0, s>>>(l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out,
+                                                                  l.sel, l.n, l.recordNormal, l.errorWord, l.stats);
+}
+
 template<int W, int B, class Prim, bool PRECISE, bool STATS>
 cudaError_t launchWideClosestKernel(const WideLaunch &l, cudaStream_t s) {
     dim3 g(l.grid), b(kWideBlock);
-    if (l.packet)
+    if (l.lanes == 2)
+        launchCoop<W, B, Prim, PRECISE, STATS, 2>(l, s);
+    else if (l.lanes == 4)
+        launchCoop<W, B, Prim, PRECISE, STATS, 4>(l, s);
+    else if (l.lanes == 8)
+        launchCoop<W, B, Prim, PRECISE, STATS, 8>(l, s);
+    else if (l.packet)
         kWidePacketClosestPoint<W, B, Prim, PRECISE, STATS><<<g, b, 0, s>>>(
             l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.errorWord, l.stats);
     else if (l.counter) {

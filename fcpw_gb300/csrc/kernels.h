@@ -62,6 +62,7 @@ struct WideLaunch {
     uint32_t *counter = nullptr;           // work counter (zero on entry) for persistent blocks, or NULL
     int packet = 0;                        // 1: warp packets (kWidePacketClosestPoint), counter unused
     int shortStack = 16;                   // per-thread stack entries in shared memory (thread schedules): 0 or 16
+    int lanes = 1;                         // > 1: lane groups per query (kWideCoopClosestPoint), counter unused
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;   // traversal statistics, or NULL
     uint32_t grid = 0;

@@ -115,7 +115,8 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
     uint32_t blocks = (n + 127) / 128;
     l.packet = c.packet;
     l.shortStack = c.shortStack;
-    if (c.persistent && !c.packet) {
+    l.lanes = c.lanes;
+    if (c.persistent && !c.packet && c.lanes == 1) {
         if ((rc = workCounter.ensure(16))) return rc;
         if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)workCounter.ptr;

@@ -30,6 +30,7 @@ struct WideConfig {
     int packet = 0;      // traverse the 32 queries of a warp as one packet
     int leafSize = 0;    // > 0: binary subtrees of at most this many primitives collapse into one leaf
     int shortStack = 16; // traversal stack entries per thread in shared memory (thread schedules): 0 or 16
+    int lanes = 1;       // lanes answering one query together (1, 2, 4 or 8)
 };
 
 constexpr int wideHeaderBytes(int bits) { return bits == 32 ? 0 : 16; }

@@ -203,18 +203,21 @@ class _GPUScene:
     # -- traversal variant -------------------------------------------------
     def set_traversal(self, branching: int = 0, bits: int = 32, sort_queries: bool = True,
                       persistent: bool = True, precise: bool = True, packet: bool = False, leaf_size: int = 0,
-                      short_stack: int = 16) -> None:
+                      short_stack: int = 16, threads_per_query: int = 1) -> None:
         """Selects the closest point traversal (see fcpwgb_traversal_config):
         branching 0 is the reference-order binary traversal; 2/4/8 use a wide
         tree with 32-, 16- or 8-bit child boxes; packet walks the queries of a
         warp together; precise refines distances to within 1e-6 of FP64;
         leaf_size merges small subtrees into wide leaves; short_stack (0 or 16)
-        is the per-thread stack depth kept in shared memory. With branching
+        is the per-thread stack depth kept in shared memory; threads_per_query
+        (1, 2, 4 or 8) answers each query with that many cooperating lanes,
+        which split each record's child boxes and each leaf's primitives. With branching
         > 0, silhouette queries use warp packets and contains and rays are
         sorted spatially (sort_queries)."""
         from ._lib import TraversalConfig
         cfg = TraversalConfig(int(branching), int(bits), 128, int(bool(sort_queries)), int(bool(persistent)),
-                              int(bool(precise)), int(bool(packet)), int(leaf_size), int(short_stack))
+                              int(bool(precise)), int(bool(packet)), int(leaf_size), int(short_stack),
+                              int(threads_per_query))
         check(lib().fcpwgb_gpu_scene_set_traversal(self._h, C.byref(cfg)))
 
     def get_traversal(self) -> dict:

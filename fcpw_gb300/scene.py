@@ -109,7 +109,7 @@ class CpuBvh:
         for k, w in enumerate(wide):
             b, q = int(w[0]), int(w[1])
             leaf = int(w[2]) if len(w) > 2 else 0
-            cfgs[k] = TraversalConfig(b, q, 128, 1, 0, 1, 0, leaf, 16)
+            cfgs[k] = TraversalConfig(b, q, 128, 1, 0, 1, 0, leaf, 16, 1)
         check(lib().fcpwgb_cpu_bvh_save(self._h, str(path).encode(), cfgs, len(wide)))
 
     def update_positions(self, positions: np.ndarray) -> None:

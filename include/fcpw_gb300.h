@@ -325,8 +325,12 @@ int fcpwgb_debug_fill_static_scratch(fcpwgb_gpu_scene *scene, uint32_t word, uin
  * is then ignored); leaf_size > 0 collapses binary subtrees of at most that
  * many primitives (up to 15) into one wide leaf; short_stack is the number of
  * traversal-stack entries per thread kept in shared memory by the
- * one-thread-per-query schedules (0 or 16; the others in local memory).
- * Defaults: {0, 32, 128, 1, 1, 1, 0, 0, 16}. Results differ from the binary
+ * one-thread-per-query schedules (0 or 16; the others in local memory);
+ * threads_per_query > 1 answers each query with a group of that many
+ * consecutive lanes (2, 4 or 8): the lanes split the child boxes of every
+ * record and the primitives of every leaf and combine their candidates by
+ * shuffles (not with packet; persistent is then ignored).
+ * Defaults: {0, 32, 128, 1, 1, 1, 0, 0, 16, 1}. Results differ from the binary
  * order only on equidistant ties (and, with precise, by the FP32 rounding
  * removed). With branching > 0, closest silhouette points are answered by
  * warp packets on the binary SNCH tree (unless squared_min_radius > 0),
@@ -342,6 +346,7 @@ typedef struct {
     int packet;        /* 0 or 1 */
     int leaf_size;     /* 0 (binary leaves) or 1..15 */
     int short_stack;   /* 0 or 16 */
+    int threads_per_query; /* 1, 2, 4 or 8 */
 } fcpwgb_traversal_config;
 int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *scene, const fcpwgb_traversal_config *config);
 int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *scene, fcpwgb_traversal_config *config);

@@ -129,6 +129,10 @@ def build_reference_simd(force: bool = False) -> Path | None:
     if reference_include() is None or not (STAGED_ENOKI / "enoki" / "array.h").exists():
         return None
     extra = ["-DFCPW_USE_ENOKI", "-DFCPW_SIMD_WIDTH=4", "-I", str(STAGED_ENOKI), "-O3"]
+    if host_isa() in ("aarch64", "arm64"):
+        # Enoki's NEON backend converts between vector register types implicitly, which GCC 13 rejects
+        # unless told otherwise
+        extra += ["-flax-vector-conversions", "-fpermissive"]
     return _build_ref(REF_SIMD_LIB, extra, force)
 
 

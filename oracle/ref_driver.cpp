@@ -202,6 +202,29 @@ template<typename F> double secondsOf(F f) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// the top-level Bvh of a scene of several instances, node type N (BvhNode, or SnchNode with silhouettes)
+template<size_t D, typename N> int exportTop(const Aggregate<D> *agg, void *nodes, int *refs) {
+    using B = Bvh<D, N, Aggregate<D>, SilhouettePrimitive<D>>;
+    using X = CPUBvhDataExtractor<D, N, Aggregate<D>, SilhouettePrimitive<D>, RefTag, RefTag, RefTag>;
+    const B *b = dynamic_cast<const B *>(agg);
+    if (!b) return -1;
+    const auto &flat = X::flat(b);
+    const auto &pr = X::prims(b);
+    for (size_t i = 0; nodes && i < flat.size(); i++) {
+        const N &n = flat[i];
+        float f[6] = {n.box.pMin[0], n.box.pMin[1], D == 3 ? n.box.pMin[D - 1] : 0.0f,
+                      n.box.pMax[0], n.box.pMax[1], D == 3 ? n.box.pMax[D - 1] : 0.0f};
+        unsigned char *d = (unsigned char *)nodes + i * 32;
+        std::memcpy(d, f, 24);
+        uint32_t np = (uint32_t)n.nReferences;
+        uint32_t off = (uint32_t)(n.nReferences > 0 ? n.referenceOffset : n.secondChildOffset);
+        std::memcpy(d + 24, &np, 4);
+        std::memcpy(d + 28, &off, 4);
+    }
+    for (size_t k = 0; refs && k < pr.size(); k++) refs[k] = pr[k]->getIndex();
+    return (int)flat.size();
+}
+
 }  // namespace
 
 extern "C" {
@@ -256,12 +279,14 @@ int ref_simd_width(void) {
 // transforms (setObjectInstanceTransforms, fcpw.h:70): nTransforms[k]
 // matrices of (DIM+1)^2 row-major floats, concatenated in object order in
 // transforms. An object with no transforms is one untransformed instance.
-void *ref_scene_create_multi(int dim, int nObjects, const float *const *positions, const int *nV,
-                             const int *const *indices, const int *nP, const int *nTransforms,
-                             const float *transforms, int aggregate) {
+// silhouettes: Scene::computeSilhouettes before the build (every object's tree
+// and the top level become SNCH trees)
+void *ref_scene_create_multi_ex(int dim, int nObjects, const float *const *positions, const int *nV,
+                                const int *const *indices, const int *nP, const int *nTransforms,
+                                const float *transforms, int aggregate, int silhouettes) {
     RefScene *r = new RefScene;
     r->dim = dim;
-    r->snch = false;
+    r->snch = silhouettes != 0;
     const float *tm = transforms;
     auto fill = [&](auto &scene, auto dimTag) {
         constexpr int D = (int)decltype(dimTag)::value;
@@ -292,11 +317,19 @@ void *ref_scene_create_multi(int dim, int nObjects, const float *const *position
                 scene.setObjectInstanceTransforms(ts, k);
             }
         }
+        if (r->snch) scene.computeSilhouettes();
         scene.build((AggregateType)aggregate, false);
     };
     if (dim == 3) fill(r->s3, std::integral_constant<size_t, 3>());
     else fill(r->s2, std::integral_constant<size_t, 2>());
     return r;
+}
+
+void *ref_scene_create_multi(int dim, int nObjects, const float *const *positions, const int *nV,
+                             const int *const *indices, const int *nP, const int *nTransforms,
+                             const float *transforms, int aggregate) {
+    return ref_scene_create_multi_ex(dim, nObjects, positions, nV, indices, nP, nTransforms, transforms, aggregate,
+                                     0);
 }
 
 void ref_scene_destroy(void *h) { delete (RefScene *)h; }
@@ -336,25 +369,10 @@ int ref_export_top(void *h, void *nodes, int *refs) {
     RefScene *r = (RefScene *)h;
     auto run = [&](auto &scene, auto dimTag) -> int {
         constexpr size_t D = decltype(dimTag)::value;
-        using B = Bvh<D, BvhNode<D>, Aggregate<D>, SilhouettePrimitive<D>>;
-        using X = CPUBvhDataExtractor<D, BvhNode<D>, Aggregate<D>, SilhouettePrimitive<D>, RefTag, RefTag, RefTag>;
-        const B *b = dynamic_cast<const B *>(scene.getSceneData()->aggregate.get());
-        if (!b) return 0;
-        const auto &flat = X::flat(b);
-        const auto &pr = X::prims(b);
-        for (size_t i = 0; nodes && i < flat.size(); i++) {
-            const BvhNode<D> &n = flat[i];
-            float f[6] = {n.box.pMin[0], n.box.pMin[1], D == 3 ? n.box.pMin[D - 1] : 0.0f,
-                          n.box.pMax[0], n.box.pMax[1], D == 3 ? n.box.pMax[D - 1] : 0.0f};
-            unsigned char *d = (unsigned char *)nodes + i * 32;
-            std::memcpy(d, f, 24);
-            uint32_t np = (uint32_t)n.nReferences;
-            uint32_t off = (uint32_t)(n.nReferences > 0 ? n.referenceOffset : n.secondChildOffset);
-            std::memcpy(d + 24, &np, 4);
-            std::memcpy(d + 28, &off, 4);
-        }
-        for (size_t k = 0; refs && k < pr.size(); k++) refs[k] = pr[k]->getIndex();
-        return (int)flat.size();
+        const Aggregate<D> *agg = scene.getSceneData()->aggregate.get();
+        int k = exportTop<D, BvhNode<D>>(agg, nodes, refs);  // an SNCH tree when the scene has silhouettes
+        if (k < 0) k = exportTop<D, SnchNode<D>>(agg, nodes, refs);
+        return k < 0 ? 0 : k;
     };
     if (r->dim == 3) return run(r->s3, std::integral_constant<size_t, 3>());
     return run(r->s2, std::integral_constant<size_t, 2>());
@@ -506,6 +524,63 @@ int ref_line_of_sight(void *h, const float *pa, const float *pb, int n, uint32_t
     };
     if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
     else run(r->s2, std::integral_constant<size_t, 2>());
+    return 0;
+}
+
+// silhouettes and sphere samples on any scene, with the interaction's objectIndex
+int ref_silhouettes_objects(void *h, const float *spheres, const uint32_t *flip, int n, float sqMinR,
+                            float precision, void *out, int *object) {
+    RefScene *r = (RefScene *)h;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        const Aggregate<D> *agg = scene.getSceneData()->aggregate.get();
+        parallelFor(n, [&](int q) {
+            BoundingSphere<D> s(vecOf<D>(spheres + 4 * q), spheres[4 * q + 3]);
+            Interaction<D> i;
+            bool found = agg->findClosestSilhouettePoint(s, i, flip[q] != 0, sqMinR, precision, false);
+            writeInteraction<D>(i, (unsigned char *)out + 40 * (size_t)q);
+            object[q] = found ? i.objectIndex : -1;
+        });
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return 0;
+}
+
+int ref_sphere_sample_objects(void *h, const float *spheres, const float *rand, int n, void *out, int *hit,
+                              int *object) {
+    RefScene *r = (RefScene *)h;
+    auto run = [&](auto &scene, auto dimTag) {
+        constexpr size_t D = decltype(dimTag)::value;
+        const Aggregate<D> *agg = scene.getSceneData()->aggregate.get();
+        parallelFor(n, [&](int q) {
+            BoundingSphere<D> s(vecOf<D>(spheres + 4 * q), spheres[4 * q + 3]);
+            Interaction<D> i;
+            int hits = agg->intersect(s, i, vecOf<D>(rand + 3 * q));
+            writeInteraction<D>(i, (unsigned char *)out + 40 * (size_t)q);
+            hit[q] = hits > 0 ? 1 : 0;
+            object[q] = hits > 0 ? i.objectIndex : -1;
+        });
+    };
+    if (r->dim == 3) run(r->s3, std::integral_constant<size_t, 3>());
+    else run(r->s2, std::integral_constant<size_t, 2>());
+    return 0;
+}
+
+// updateObjectVertices of one object (its own vertex order) followed by Scene::refit
+int ref_update_object_and_refit(void *h, int object, const float *positions, int nV) {
+    RefScene *r = (RefScene *)h;
+    if (r->dim == 3) {
+        std::vector<Vector3> pos(nV);
+        for (int i = 0; i < nV; i++) pos[i] = Vector3(positions[3 * i], positions[3 * i + 1], positions[3 * i + 2]);
+        r->s3.updateObjectVertices(pos, object);
+        r->s3.refit();
+    } else {
+        std::vector<Vector2> pos(nV);
+        for (int i = 0; i < nV; i++) pos[i] = Vector2(positions[2 * i], positions[2 * i + 1]);
+        r->s2.updateObjectVertices(pos, object);
+        r->s2.refit();
+    }
     return 0;
 }
 

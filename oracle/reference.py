@@ -35,6 +35,8 @@ def _load(simd: bool = False):
         lib.ref_scene_destroy.argtypes = [P]
         lib.ref_scene_create_multi.restype = P
         lib.ref_scene_create_multi.argtypes = [i, i, P, P, P, P, P, P, i]
+        lib.ref_scene_create_multi_ex.restype = P
+        lib.ref_scene_create_multi_ex.argtypes = [i, i, P, P, P, P, P, P, i, i]
         lib.ref_simd_width.restype = i
         lib.ref_simd_width.argtypes = []
         for name, args in {"ref_scene_closest_points_timed": [P, P, i, P],
@@ -49,7 +51,10 @@ def _load(simd: bool = False):
                            "ref_contains": [P, P, i, P], "ref_line_of_sight": [P, P, P, i, P],
                            "ref_closest_points_objects": [P, P, i, i, P, P],
                            "ref_intersect_rays_objects": [P, P, i, i, P, P, P],
-                           "ref_export_top": [P, P, P]}.items():
+                           "ref_export_top": [P, P, P],
+                           "ref_silhouettes_objects": [P, P, P, i, f, f, P, P],
+                           "ref_sphere_sample_objects": [P, P, P, i, P, P, P],
+                           "ref_update_object_and_refit": [P, i, P, i]}.items():
             fn = getattr(lib, name)
             fn.restype = i
             fn.argtypes = args
@@ -186,9 +191,9 @@ class RefMultiScene(RefScene):
     objects: list of (positions, indices); transforms: per object a list of
     (DIM+1)x(DIM+1) matrices (empty: one untransformed instance)."""
 
-    def __init__(self, dim, objects, transforms, aggregate_type=3):
+    def __init__(self, dim, objects, transforms, aggregate_type=3, silhouettes=False):
         self.dim = dim
-        self.silhouettes = False
+        self.silhouettes = bool(silhouettes)
         self._pos = [np.ascontiguousarray(p, np.float32) for p, _ in objects]
         self._idx = [np.ascontiguousarray(f, np.int32) for _, f in objects]
         k = len(objects)
@@ -201,8 +206,9 @@ class RefMultiScene(RefScene):
         mats = [np.asarray(m, np.float32).reshape(dim + 1, dim + 1) for t in transforms for m in t]
         self._tm = np.ascontiguousarray(np.concatenate([m.reshape(-1) for m in mats]) if mats
                                         else np.zeros(1, np.float32))
-        self._h = _load().ref_scene_create_multi(dim, k, C.cast(pp, C.c_void_p), _p(nv), C.cast(ip, C.c_void_p),
-                                                 _p(npr), _p(nt), _p(self._tm), int(aggregate_type))
+        self._h = _load().ref_scene_create_multi_ex(dim, k, C.cast(pp, C.c_void_p), _p(nv), C.cast(ip, C.c_void_p),
+                                                    _p(npr), _p(nt), _p(self._tm), int(aggregate_type),
+                                                    int(self.silhouettes))
 
     def closest_points_objects(self, spheres, record_normals=False):
         from fcpw_gb300 import records as R
@@ -220,6 +226,30 @@ class RefMultiScene(RefScene):
         r = np.ascontiguousarray(rays).view(np.float32)
         _load().ref_intersect_rays_objects(self._h, _p(r), len(rays), int(occlusion), _p(out), _p(hit), _p(obj))
         return out, hit.astype(bool), obj
+
+    def silhouettes_objects(self, spheres, flip, squared_min_radius=0.0, precision=1e-3):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        obj = np.zeros(len(spheres), np.int32)
+        fl = np.ascontiguousarray(flip, np.uint32)
+        _load().ref_silhouettes_objects(self._h, _p(self._sph(spheres)), _p(fl), len(spheres),
+                                        float(squared_min_radius), float(precision), _p(out), _p(obj))
+        return out, obj
+
+    def sphere_sample_objects(self, spheres, rand_nums):
+        from fcpw_gb300 import records as R
+        out = np.zeros(len(spheres), R.INTERACTION)
+        hit = np.zeros(len(spheres), np.int32)
+        obj = np.zeros(len(spheres), np.int32)
+        rn = np.ascontiguousarray(rand_nums, np.float32)
+        _load().ref_sphere_sample_objects(self._h, _p(self._sph(spheres)), _p(rn), len(spheres), _p(out), _p(hit),
+                                          _p(obj))
+        return out, hit.astype(bool), obj
+
+    def update_object_and_refit(self, object_index, positions):
+        pos = np.ascontiguousarray(positions, np.float32)
+        self._pos[object_index] = pos
+        _load().ref_update_object_and_refit(self._h, int(object_index), _p(pos), len(pos))
 
     def export_top(self):
         """(nodes, aggregate index per leaf reference) of the top-level tree."""

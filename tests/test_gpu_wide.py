@@ -330,13 +330,50 @@ def test_every_wide_layout_and_schedule_agrees_exactly(torus, precise, scale):
     for cfg in [dict(branching=4, bits=32, packet=True), dict(branching=4, bits=32, persistent=False),
                 dict(branching=4, bits=32, persistent=True), dict(branching=2, bits=16),
                 dict(branching=8, bits=8), dict(branching=4, bits=8, leaf_size=8, short_stack=0),
-                dict(branching=8, bits=32, packet=True), dict(branching=4, bits=16, sort_queries=False)]:
+                dict(branching=8, bits=32, packet=True), dict(branching=4, bits=16, sort_queries=False),
+                dict(branching=4, bits=32, threads_per_query=4), dict(branching=8, bits=8, threads_per_query=8),
+                dict(branching=2, bits=32, threads_per_query=2), dict(branching=8, bits=16, threads_per_query=2),
+                dict(branching=4, bits=8, leaf_size=12, threads_per_query=8)]:
         g.set_traversal(precise=precise, **cfg)
         outs[str(cfg)] = _run(g, sub).tobytes()
     g.set_traversal(0)
     first = next(iter(outs.values()))
     differ = [k for k, v in outs.items() if v != first]
     assert not differ, f"configurations that differ from the first: {differ}"
+
+
+@pytest.mark.parametrize("lanes", [2, 4, 8])
+@pytest.mark.parametrize("branching,bits", [(2, 32), (4, 16), (8, 8), (8, 32)])
+def test_cooperative_lanes_match_oracle(torus, lanes, branching, bits):
+    """Groups of 2, 4 or 8 lanes per query (child boxes and leaf primitives
+    split over the lanes) against the reference CPU order, with and without
+    the precise refinement and merged leaves."""
+    s, g, pts, ref, prims = torus
+    for precise, leaf in ((False, 0), (True, 0), (True, 8)):
+        g.set_traversal(branching, bits, sort_queries=True, precise=precise, leaf_size=leaf, threads_per_query=lanes)
+        compare_closest(3, prims, pts, _run(g, pts), ref, f"coop{lanes} {branching}/{bits} leaf {leaf}")
+    g.set_traversal(0)
+    assert g.check_errors() == 0
+
+
+def test_cooperative_lanes_2d_and_finite_radius():
+    v, sg = W.star_polylines(16, 64, W.SEED_BASE + 59)
+    s = build_scene(2, v, sg)
+    g = F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    pts = W.uniform_points(30000, 2, -3, 3, 60)
+    r2 = W.rng(61).uniform(0.0, 0.5, len(pts)).astype(np.float32)
+    nodes, prims, _ = s.cpu_bvh.export()
+    ref = O.closest_points_bvh(2, nodes, prims, R.make_spheres(pts, r2))
+    for lanes in (2, 4, 8):
+        g.set_traversal(4, 16, sort_queries=True, precise=True, threads_per_query=lanes)
+        compare_closest(2, prims, pts, _run(g, pts, r2), ref, f"2D coop{lanes}")
+    with pytest.raises(F.FcpwError):
+        g.set_traversal(4, 32, packet=True, threads_per_query=4)
+    with pytest.raises(F.FcpwError):
+        g.set_traversal(4, 32, threads_per_query=3)
+    g.set_traversal(0)
+    assert g.check_errors() == 0
 
 
 @pytest.mark.parametrize("dim", [3, 2])
