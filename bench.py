@@ -1120,6 +1120,11 @@ def run_reference(args):
         builds[other[0]] = {"queries_per_s": sample / sec, "queries_per_step": sample, "ms_per_step": 1e3 * sec,
                             "note": "one call, for the record"}
     width = REF.simd_width() if "vectorized" in warm else 0
+    if "vectorized" not in warm:
+        from oracle.build import REF_SIMD_ERROR
+        why = REF_SIMD_ERROR.read_text().strip().splitlines()[:1] if REF_SIMD_ERROR.exists() else []
+        builds["vectorized"] = {"unavailable": "the reference's Enoki build (vectorize=true, FCPW_SIMD_WIDTH=4) "
+                                               "does not compile on this host" + (f": {why[0]}" if why else "")}
     desc = (f"{sample:,} of the {n:,} queries per step through the reference's Scene<3>::findClosestPoints "
             f"({best}{f', Mbvh FCPW_SIMD_WIDTH={width}' if best == 'vectorized' else ', binary SAH Bvh'}), its own "
             f"std::thread split over {threads} hardware threads; timed inside the call")

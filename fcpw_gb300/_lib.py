@@ -44,6 +44,14 @@ SIGNATURES = {
     "fcpwgb_find_closest_points_instanced_device": (c_int, [P, P, P, P, c_uint32, c_int, P]),
     "fcpwgb_intersect_rays_instanced": (c_int, [P, P, P, P, c_uint32, c_int]),
     "fcpwgb_intersect_rays_instanced_device": (c_int, [P, P, P, P, c_uint32, c_int, P]),
+    "fcpwgb_intersect_spheres_instanced": (c_int, [P, P, P, P, P, c_uint32]),
+    "fcpwgb_intersect_spheres_instanced_device": (c_int, [P, P, P, P, P, c_uint32, P]),
+    "fcpwgb_find_closest_silhouette_points_instanced": (c_int, [P, P, P, P, P, c_uint32, c_float, c_float]),
+    "fcpwgb_find_closest_silhouette_points_instanced_device": (c_int, [P, P, P, P, P, c_uint32, c_float, c_float,
+                                                                       P]),
+    "fcpwgb_gpu_scene_refit_object": (c_int, [P, c_uint32, P, P]),
+    "fcpwgb_gpu_scene_update_object_vertices_device": (c_int, [P, c_uint32, P, c_uint32, P]),
+    "fcpwgb_gpu_scene_export_top_nodes": (c_int, [P, P, C.POINTER(c_uint32)]),
     "fcpwgb_gpu_scene_build_device": (c_int, [P, P, c_uint32, P, c_uint32, c_uint32, P]),
     "fcpwgb_gpu_scene_info": (c_int, [P, P]),
     "fcpwgb_gpu_scene_refit": (c_int, [P, P, P]),

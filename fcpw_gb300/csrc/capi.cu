@@ -725,6 +725,14 @@ extern "C" int fcpwgb_intersect_rays_device(fcpwgb_gpu_scene *s, const fcpwgb_ra
 extern "C" int fcpwgb_intersect_spheres_device(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
                                                const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out, uint32_t n,
                                                void *stream) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc) return rc;
+        if (n > 0 && (!spheres || !rand_nums || !out))
+            return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedSample(s, (const DevSphere *)spheres, (const float3 *)rand_nums, (DevInteraction *)out,
+                               nullptr, n, s->pick(stream));
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n > 0 && (!spheres || !rand_nums || !out))
@@ -739,6 +747,14 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
                                                             const uint32_t *flip, fcpwgb_interaction *out,
                                                             uint32_t n, float sq_min_r, float precision,
                                                             void *stream) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc) return rc;
+        if (n > 0 && (!spheres || !flip || !out))
+            return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedSilhouettes(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, nullptr, n, sq_min_r,
+                                    precision, s->pick(stream));
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n > 0 && (!spheres || !flip || !out))
@@ -835,6 +851,13 @@ extern "C" int fcpwgb_intersect_rays(fcpwgb_gpu_scene *s, const fcpwgb_ray *rays
 
 extern "C" int fcpwgb_intersect_spheres(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
                                         const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out, uint32_t n) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc || n == 0) return rc;
+        if (!spheres || !rand_nums || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedHostQuery(s, InstancedQuery::Sample, spheres, (size_t)n * sizeof(DevSphere), rand_nums,
+                                  (size_t)n * sizeof(float3), out, nullptr, n, 0, 0.0f, 0.0f);
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n == 0) return FCPWGB_OK;
@@ -850,6 +873,13 @@ extern "C" int fcpwgb_intersect_spheres(fcpwgb_gpu_scene *s, const fcpwgb_boundi
 extern "C" int fcpwgb_find_closest_silhouette_points(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
                                                      const uint32_t *flip, fcpwgb_interaction *out, uint32_t n,
                                                      float sq_min_r, float precision) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc || n == 0) return rc;
+        if (!spheres || !flip || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedHostQuery(s, InstancedQuery::Silhouette, spheres, (size_t)n * sizeof(DevSphere), flip,
+                                  (size_t)n * sizeof(uint32_t), out, nullptr, n, 0, sq_min_r, precision);
+    }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n == 0) return FCPWGB_OK;

@@ -30,6 +30,7 @@
 #include <string>
 #include <vector>
 
+#include "binary_queries.cuh"
 #include "host_bvh.h"
 #include "k_wide.cuh"
 #include "kernels.h"
@@ -57,13 +58,18 @@ struct DevInstance {
 static_assert(sizeof(DevInstance) == 112, "instance record");
 
 struct DevObject {
-    const unsigned char *nodes;  // 4-wide records
-    const unsigned char *prims;  // Tri48 / Seg24 records
+    const unsigned char *nodes;     // 4-wide records
+    const unsigned char *prims;     // Tri48 / Seg24 records
+    const unsigned char *binNodes;  // the transferred binary tree (32 B, or 64 B SNCH records)
+    const unsigned char *binPrims;  // its primitives (40 B triangles / 24 B segments)
+    const unsigned char *sils;      // silhouette records of an SNCH tree, else NULL
+    uint32_t maxDepth, snch;
 };
 
 struct InstancedState {
     int dim = 3;
-    uint32_t nInstances = 0, nTopNodes = 0;
+    bool snch = false;  // every object carries a silhouette (SNCH) tree
+    uint32_t nInstances = 0, nTopNodes = 0, topDepth = 0;
     std::vector<fcpwgb_gpu_scene *> objects;
     std::vector<uint32_t> instObject;
     DeviceBuffer topNodes, topRefs, instances, objectTable, instOut;
@@ -298,10 +304,13 @@ FCPWGB_D float xfR2(int dim, const float *__restrict__ m, float3 c, float3 tc, f
 
 // Interaction::applyTransform: p to world space, distance to the query
 // recomputed, normal through the transposed inverse and renormalised
-FCPWGB_D void xfInteraction(int dim, const DevInstance &I, float3 query, DevInteraction &c) {
+FCPWGB_D void xfInteraction(int dim, const DevInstance &I, float3 query, DevInteraction &c,
+                             bool overwriteDistance = true) {
     c.p = xfPoint(dim, I.t, c.p);
-    float3 d = xsub3(c.p, query);
-    c.d = __fsqrt_rn(xdot3(dim, d, d));
+    if (overwriteDistance) {
+        float3 d = xsub3(c.p, query);
+        c.d = __fsqrt_rn(xdot3(dim, d, d));
+    }
     float r[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -416,6 +425,54 @@ FCPWGB_D bool instanceRay(int dim, const DevInstance &I, const DevObject &O, Dev
     } else {
         r.tMax = rq.tMax;
     }
+    return hit;
+}
+
+// TransformedAggregate::findClosestSilhouettePointFromNode (core/primitive.h:444-466),
+// or the object's own traversal for an untransformed object: the query and
+// the minimum radius go to object space, the object's SNCH tree is walked
+// (silhouetteBinary), the radius comes back through t and the answer is
+// mapped to world space; r2 is updated as the reference updates the sphere
+template<class Sil, int DIM>
+FCPWGB_D bool instanceSilhouette(const DevInstance &I, const DevObject &O, float3 c, float &r2, bool flipNormal,
+                                 float sqMinR, float precision, DevInteraction &cand, uint32_t *errorWord) {
+    cand = defaultInteraction();
+    if (!O.sils) return false;
+    float3 cq = c;
+    float r2q = r2, minq = sqMinR;
+    if (I.transformed) {
+        cq = xfPoint(DIM, I.ti, c);
+        r2q = xfR2(DIM, I.ti, c, cq, r2);
+        minq = xfR2(DIM, I.ti, c, cq, sqMinR);
+    }
+    bool found = silhouetteBinary<Sil, DIM>(O.binNodes, O.sils, cq, r2q, flipNormal, minq, precision, errorWord,
+                                            cand);
+    if (I.transformed) {
+        r2 = xfR2(DIM, I.t, cq, xfPoint(DIM, I.t, cq), r2q);
+        if (found) xfInteraction(DIM, I, c, cand);
+    } else {
+        r2 = r2q;
+    }
+    return found;
+}
+
+// TransformedAggregate::intersectFromNode for sphere sampling (core/primitive.h:392-410):
+// the sphere goes to object space, the object's binary tree is sampled
+// (sphereSampleBinary, rn = (u, rn1, rn2)), and the sample's point and normal
+// are mapped to world space; its pdf stays the object's (applyTransform
+// without overwriting the distance)
+template<class Prim, int NODE_STRIDE>
+FCPWGB_D bool instanceSample(int dim, const DevInstance &I, const DevObject &O, float3 c, float r2, float3 rn,
+                             DevInteraction &cand, uint32_t *errorWord) {
+    float3 cq = c;
+    float r2q = r2;
+    if (I.transformed) {
+        cq = xfPoint(dim, I.ti, c);
+        r2q = xfR2(dim, I.ti, c, cq, r2);
+    }
+    bool hit = sphereSampleBinary<Prim, NODE_STRIDE>(O.binNodes, O.binPrims, cq, r2q, rn, O.maxDepth + 1, errorWord,
+                                                     cand);
+    if (hit && I.transformed) xfInteraction(dim, I, c, cand, false);
     return hit;
 }
 
@@ -603,6 +660,254 @@ __global__ void __launch_bounds__(kWideBlock) kInstancedRay(
     if (instOut) instOut[slot] = bestInst;
 }
 
+// One thread per query: the top-level walk of bvh.inl:1435-1596 with aggregate
+// leaves. The top level of a scene with silhouettes is an SNCH tree whose
+// nodes keep the default cone (half angle pi: valid, always overlapping), so a
+// child is entered when its box is within the radius; every silhouette found
+// replaces the answer and tightens r2, and the walk stops once r2 is within
+// the minimum radius.
+template<class Sil, int DIM>
+__global__ void __launch_bounds__(kWideBlock) kInstancedSilhouette(
+    const unsigned char *__restrict__ topNodes, const uint32_t *__restrict__ topRefs, uint32_t nInstances,
+    const DevInstance *__restrict__ insts, const DevObject *__restrict__ objs, const DevSphere *__restrict__ spheres,
+    const uint32_t *__restrict__ flip, DevInteraction *__restrict__ out, uint32_t *__restrict__ instOut, uint32_t n,
+    float sqMinR, float precision, uint32_t *errorWord) {
+    const uint32_t q = blockIdx.x * kWideBlock + threadIdx.x;
+    if (q >= n) return;
+    float4 s4 = ldg4(spheres + q);
+    const float3 c = make_float3(s4.x, s4.y, s4.z);
+    float r2 = s4.w;
+    const bool flipNormal = __ldg(flip + q) != 0;
+    DevInteraction best = defaultInteraction();
+    uint32_t bestInst = kUintMax;
+    if (!(sqMinR >= r2)) {
+        if (nInstances == 1) {
+            DevInteraction cand;
+            if (instanceSilhouette<Sil, DIM>(insts[0], objs[insts[0].object], c, r2, flipNormal, sqMinR, precision,
+                                             cand, errorWord)) {
+                best = cand;
+                bestInst = 0;
+            }
+        } else {
+            uint32_t stackNode[kTopStack];
+            float stackDist[kTopStack];
+            NodeBox root = topNode(topNodes, 0);
+            float b0, b1;
+            xboxSphere(DIM, root.pMin, root.pMax, c, b0, b1);
+            if (b0 <= r2) {
+                stackNode[0] = 0;
+                stackDist[0] = b0;
+                int sp = 0;
+                bool done = false;
+                while (sp >= 0 && !done) {
+                    uint32_t ni = stackNode[sp];
+                    float cur = stackDist[sp];
+                    sp--;
+                    if (cur > r2) continue;
+                    NodeBox node = topNode(topNodes, ni);
+                    if (node.nPrims > 0) {
+                        for (uint32_t p = 0; p < node.nPrims; p++) {
+                            uint32_t k = __ldg(topRefs + node.offset + p);
+                            const DevInstance &I = insts[k];
+                            DevInteraction cand;
+                            if (instanceSilhouette<Sil, DIM>(I, objs[I.object], c, r2, flipNormal, sqMinR, precision,
+                                                             cand, errorWord)) {
+                                r2 = fminf(r2, cand.d * cand.d);
+                                best = cand;
+                                bestInst = k;
+                                if (sqMinR >= r2) {
+                                    done = true;
+                                    break;
+                                }
+                            }
+                        }
+                    } else {
+                        uint32_t li = ni + 1, ri = ni + node.offset;
+                        NodeBox l = topNode(topNodes, li), rr = topNode(topNodes, ri);
+                        float l0, l1, r0, r1;
+                        xboxSphere(DIM, l.pMin, l.pMax, c, l0, l1);
+                        xboxSphere(DIM, rr.pMin, rr.pMax, c, r0, r1);
+                        bool hit0 = l0 <= r2, hit1 = r0 <= r2;
+                        if (hit0 && hit1) {
+                            uint32_t closer = li, other = ri;
+                            float dc = l0, dother = r0;
+                            if (r0 < l0) { closer = ri; other = li; dc = r0; dother = l0; }
+                            if (sp + 2 >= kTopStack) { atomicOr(errorWord, kErrStackOverflow); break; }
+                            ++sp; stackNode[sp] = other; stackDist[sp] = dother;
+                            ++sp; stackNode[sp] = closer; stackDist[sp] = dc;
+                        } else if (hit0 || hit1) {
+                            if (sp + 1 >= kTopStack) { atomicOr(errorWord, kErrStackOverflow); break; }
+                            ++sp;
+                            stackNode[sp] = hit0 ? li : ri;
+                            stackDist[sp] = hit0 ? l0 : r0;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    out[q] = best;
+    if (instOut) instOut[q] = bestInst;
+}
+
+// One thread per query: the stochastic top-level descent of bvh.inl:1140-1288
+// with aggregate leaves: a child is chosen with probability proportional to
+// its overlap weight (u = rn.x rescaled at every choice); in the leaf every
+// instance is sampled with the current u (instanceSample), and one of the
+// instances that hit is chosen uniformly, its sample's pdf multiplied by the
+// top-level traversal pdf and divided by the number that hit.
+template<class Prim, int NODE_STRIDE>
+__global__ void __launch_bounds__(kWideBlock) kInstancedSphereSample(
+    const unsigned char *__restrict__ topNodes, const uint32_t *__restrict__ topRefs, uint32_t nInstances,
+    uint32_t topDepth, const DevInstance *__restrict__ insts, const DevObject *__restrict__ objs,
+    const DevSphere *__restrict__ spheres, const float3 *__restrict__ randNums, DevInteraction *__restrict__ out,
+    uint32_t *__restrict__ instOut, uint32_t n, int dim, uint32_t *errorWord) {
+    const uint32_t q = blockIdx.x * kWideBlock + threadIdx.x;
+    if (q >= n) return;
+    float4 s4 = ldg4(spheres + q);
+    const float3 c = make_float3(s4.x, s4.y, s4.z);
+    const float r2 = s4.w;
+    const float3 rn = randNums[q];
+    DevInteraction best = defaultInteraction();
+    uint32_t bestInst = kUintMax;
+    if (nInstances == 1) {
+        DevInteraction cand;
+        if (instanceSample<Prim, NODE_STRIDE>(dim, insts[0], objs[insts[0].object], c, r2, rn, cand, errorWord)) {
+            best = cand;
+            bestInst = 0;
+        }
+    } else {
+        NodeBox root = topNode(topNodes, 0);
+        float b0, b1;
+        xboxSphere(dim, root.pMin, root.pMax, c, b0, b1);
+        if (b0 <= r2) {
+            float traversalPdf = 1.0f, u = rn.x;
+            uint32_t ni = 0;
+            for (uint32_t step = 0; step <= topDepth; step++) {
+                NodeBox node = topNode(topNodes, ni);
+                if (node.nPrims > 0) {
+                    float total = 0.0f;
+                    for (uint32_t p = 0; p < node.nPrims; p++) {
+                        uint32_t k = __ldg(topRefs + node.offset + p);
+                        const DevInstance &I = insts[k];
+                        DevInteraction cand;
+                        if (instanceSample<Prim, NODE_STRIDE>(dim, I, objs[I.object], c, r2,
+                                                              make_float3(u, rn.y, rn.z), cand, errorWord)) {
+                            total += 1.0f;
+                            const float prob = 1.0f / total;
+                            if (u < prob) {
+                                u = u / prob;
+                                best = cand;
+                                best.d *= traversalPdf;
+                                bestInst = k;
+                            } else {
+                                u = (u - prob) / (1.0f - prob);
+                            }
+                        }
+                    }
+                    if (total > 0.0f) best.d /= total;
+                    break;
+                }
+                uint32_t li = ni + 1, ri = ni + node.offset;
+                NodeBox l = topNode(topNodes, li), rr = topNode(topNodes, ri);
+                float l0, l1, r0, r1;
+                xboxSphere(dim, l.pMin, l.pMax, c, l0, l1);
+                xboxSphere(dim, rr.pMin, rr.pMax, c, r0, r1);
+                const float w0 = l0 <= r2 ? 1.0f : 0.0f, w1 = r0 <= r2 ? 1.0f : 0.0f;
+                const float total = w0 + w1;
+                if (!(total > 0.0f)) break;
+                const float p0 = w0 / total, p1 = 1.0f - p0;
+                if (u < p0) {
+                    u = u / p0;
+                    ni = li;
+                    traversalPdf *= p0;
+                } else {
+                    u = (u - p0) / p1;
+                    ni = ri;
+                    traversalPdf *= p1;
+                }
+                if (step == topDepth) atomicOr(errorWord, kErrStepBudget);
+            }
+        }
+    }
+    out[q] = best;
+    if (instOut) instOut[q] = bestInst;
+}
+
+// Scene::refit of the top level after objects were refit (bvh.inl:548-599 over
+// the instances; TransformedAggregate::boundingBox, core/primitive.h:297-300):
+// every instance's box is its object's root box, or that box's corners
+// mapped by t, each padded by FLT_EPSILON; a leaf's box is the union of its
+// instances' boxes, an inner node's the union of its children's, nodes in
+// reverse pre-order (children before parents). One thread: the top level has
+// about two nodes per instance.
+__global__ void kInstancedTopRefit(unsigned char *__restrict__ topNodes, const uint32_t *__restrict__ topRefs,
+                                   uint32_t nTopNodes, const DevInstance *__restrict__ insts,
+                                   const DevObject *__restrict__ objs, int dim) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (uint32_t ii = nTopNodes; ii-- > 0;) {
+        float *f = reinterpret_cast<float *>(topNodes + (size_t)ii * 32);
+        const uint32_t np = __float_as_uint(f[6]), off = __float_as_uint(f[7]);
+        float lo[3] = {kFltMax, kFltMax, kFltMax}, hi[3] = {-kFltMax, -kFltMax, -kFltMax};
+        if (np > 0) {
+            for (uint32_t p = 0; p < np; p++) {
+                const DevInstance &I = insts[topRefs[off + p]];
+                const float *rb = reinterpret_cast<const float *>(objs[I.object].binNodes);
+                float bl[3], bh[3];
+                if (!I.transformed) {
+                    for (int a = 0; a < 3; a++) {
+                        bl[a] = rb[a];
+                        bh[a] = rb[3 + a];
+                    }
+                } else {
+                    for (int a = 0; a < 3; a++) {
+                        bl[a] = kFltMax;
+                        bh[a] = -kFltMax;
+                    }
+                    for (int corner = 0; corner < (1 << dim); corner++) {
+                        int temp = corner;
+                        float3 pc;
+                        float *pp = &pc.x;
+                        pc = make_float3(0.0f, 0.0f, 0.0f);
+                        for (int a = 0; a < dim; a++) {
+                            pp[a] = temp % 2 == 0 ? rb[a] : rb[3 + a];
+                            temp /= 2;
+                        }
+                        float3 tq = xfPoint(dim, I.t, pc);
+                        const float *qq = &tq.x;
+                        for (int a = 0; a < dim; a++) {
+                            const float l = __fsub_rn(qq[a], kFltEps), u = __fadd_rn(qq[a], kFltEps);
+                            bl[a] = l < bl[a] ? l : bl[a];
+                            bh[a] = bh[a] < u ? u : bh[a];
+                        }
+                    }
+                    if (dim == 2) {
+                        bl[2] = 0.0f;
+                        bh[2] = 0.0f;
+                    }
+                }
+                for (int a = 0; a < 3; a++) {
+                    lo[a] = bl[a] < lo[a] ? bl[a] : lo[a];
+                    hi[a] = hi[a] < bh[a] ? bh[a] : hi[a];
+                }
+            }
+        } else {
+            const float *lf = reinterpret_cast<const float *>(topNodes + (size_t)(ii + 1) * 32);
+            const float *rf = reinterpret_cast<const float *>(topNodes + (size_t)(ii + off) * 32);
+            for (int a = 0; a < 3; a++) {
+                lo[a] = lf[a];
+                hi[a] = lf[3 + a];
+                lo[a] = rf[a] < lo[a] ? rf[a] : lo[a];
+                hi[a] = hi[a] < rf[3 + a] ? rf[3 + a] : hi[a];
+            }
+        }
+        for (int a = 0; a < 3; a++) {
+            f[a] = lo[a];
+            f[3 + a] = hi[a];
+        }
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ scene methods
@@ -620,6 +925,11 @@ int instancedPrepare(fcpwgb_gpu_scene *s, cudaStream_t st) {
         if (rc) return rc;
         table[k].nodes = (const unsigned char *)o->wideNodes.ptr;
         table[k].prims = I.dim == 3 ? (const unsigned char *)o->widePrims.ptr : (const unsigned char *)o->prims.ptr;
+        table[k].binNodes = (const unsigned char *)o->nodes.ptr;
+        table[k].binPrims = (const unsigned char *)o->prims.ptr;
+        table[k].sils = o->snch && o->nSils > 0 ? (const unsigned char *)o->sils.ptr : nullptr;
+        table[k].maxDepth = o->maxDepth;
+        table[k].snch = o->snch ? 1u : 0u;
     }
     for (auto *o : I.objects) {
         cudaError_t e = cudaStreamSynchronize(o->stream);
@@ -729,21 +1039,108 @@ int instancedRays(fcpwgb_gpu_scene *s, const DevRay *rays, DevInteraction *out, 
     return s->timeEnd(st);
 }
 
-// host arrays: copies in, device call on the scene's stream, copies out, error word
-int instancedHost(fcpwgb_gpu_scene *s, const void *queries, size_t queryBytes, void *out, uint32_t *instOut,
-                  uint32_t n, bool rays, int flag) {
+int instancedSilhouettes(fcpwgb_gpu_scene *s, const DevSphere *spheres, const uint32_t *flip, DevInteraction *out,
+                         uint32_t *instOut, uint32_t n, float sqMinR, float precision, cudaStream_t st) {
+    int rc = instancedPrepare(s, st);
+    if (rc || n == 0) return rc;
+    InstancedState &I = *s->inst;
+    if (!I.snch) {  // no silhouette data: every result keeps its default, as for one object
+        cudaError_t e = launchFillDefault(out, n, st);
+        if (e == cudaSuccess && instOut) e = cudaMemsetAsync(instOut, 0xff, (size_t)n * sizeof(uint32_t), st);
+        return e == cudaSuccess ? 0 : cudaFail(e, "silhouettes without silhouette data");
+    }
+    const unsigned char *tn = (const unsigned char *)I.topNodes.ptr;
+    const uint32_t *tr = (const uint32_t *)I.topRefs.ptr;
+    const DevInstance *ins = (const DevInstance *)I.instances.ptr;
+    const DevObject *obs = (const DevObject *)I.objectTable.ptr;
+    uint32_t *ew = (uint32_t *)s->errorWord.ptr;
+    dim3 g((n + kWideBlock - 1) / kWideBlock), b(kWideBlock);
+    if ((rc = s->timeStart(st))) return rc;
+    if (I.dim == 3)
+        kInstancedSilhouette<EdgeSil, 3><<<g, b, 0, st>>>(tn, tr, I.nInstances, ins, obs, spheres, flip, out, instOut,
+                                                           n, sqMinR, precision, ew);
+    else
+        kInstancedSilhouette<VertexSil, 2><<<g, b, 0, st>>>(tn, tr, I.nInstances, ins, obs, spheres, flip, out,
+                                                             instOut, n, sqMinR, precision, ew);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cudaFail(e, "instanced silhouette launch");
+    return s->timeEnd(st);
+}
+
+int instancedSample(fcpwgb_gpu_scene *s, const DevSphere *spheres, const float3 *randNums, DevInteraction *out,
+                    uint32_t *instOut, uint32_t n, cudaStream_t st) {
+    int rc = instancedPrepare(s, st);
+    if (rc || n == 0) return rc;
+    InstancedState &I = *s->inst;
+    const unsigned char *tn = (const unsigned char *)I.topNodes.ptr;
+    const uint32_t *tr = (const uint32_t *)I.topRefs.ptr;
+    const DevInstance *ins = (const DevInstance *)I.instances.ptr;
+    const DevObject *obs = (const DevObject *)I.objectTable.ptr;
+    uint32_t *ew = (uint32_t *)s->errorWord.ptr;
+    dim3 g((n + kWideBlock - 1) / kWideBlock), b(kWideBlock);
+    const uint32_t depth = I.topDepth + 1;
+#define FCPWGB_INST_SS(P, STRIDE)                                                                              \
+    kInstancedSphereSample<P, STRIDE><<<g, b, 0, st>>>(tn, tr, I.nInstances, depth, ins, obs, spheres, randNums, \
+                                                       out, instOut, n, I.dim, ew)
+    if (I.dim == 3) {
+        if (I.snch) FCPWGB_INST_SS(TriPrim, 64);
+        else FCPWGB_INST_SS(TriPrim, 32);
+    } else {
+        if (I.snch) FCPWGB_INST_SS(SegPrim, 64);
+        else FCPWGB_INST_SS(SegPrim, 32);
+    }
+#undef FCPWGB_INST_SS
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : cudaFail(e, "instanced sphere sampling launch");
+}
+
+// the top level after one of the objects was refit on stream st
+int instancedTopRefit(fcpwgb_gpu_scene *s, cudaStream_t st) {
+    int rc = instancedPrepare(s, st);
+    if (rc) return rc;
+    InstancedState &I = *s->inst;
+    if (I.nTopNodes == 0) return FCPWGB_OK;
+    kInstancedTopRefit<<<1, 1, 0, st>>>((unsigned char *)I.topNodes.ptr, (const uint32_t *)I.topRefs.ptr,
+                                         I.nTopNodes, (const DevInstance *)I.instances.ptr,
+                                         (const DevObject *)I.objectTable.ptr, I.dim);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : cudaFail(e, "top-level refit");
+}
+
+// host arrays: copies in (queries, and for sampling the random numbers, for
+// silhouettes the flip flags), device call on the scene's stream, copies out,
+// error word
+int instancedHostQuery(fcpwgb_gpu_scene *s, InstancedQuery kind, const void *queries, size_t queryBytes,
+                       const void *second, size_t secondBytes, void *out, uint32_t *instOut, uint32_t n, int flag,
+                       float sqMinR, float precision) {
     int rc;
     size_t ob = (size_t)n * sizeof(DevInteraction);
     if ((rc = s->qIn0.ensure(queryBytes))) return rc;
+    if (second && (rc = s->qIn1.ensure(secondBytes))) return rc;
     if ((rc = s->qOut.ensure(ob))) return rc;
     if (instOut && (rc = s->inst->instOut.ensure((size_t)n * sizeof(uint32_t)))) return rc;
     cudaError_t e = cudaMemcpyAsync(s->qIn0.ptr, queries, queryBytes, cudaMemcpyHostToDevice, s->stream);
     if (e != cudaSuccess) return cudaFail(e, "cudaMemcpyAsync");
+    if (second &&
+        (e = cudaMemcpyAsync(s->qIn1.ptr, second, secondBytes, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess)
+        return cudaFail(e, "cudaMemcpyAsync");
     uint32_t *dInst = instOut ? (uint32_t *)s->inst->instOut.ptr : nullptr;
-    rc = rays ? instancedRays(s, (const DevRay *)s->qIn0.ptr, (DevInteraction *)s->qOut.ptr, dInst, n, flag,
-                              s->stream)
-              : instancedClosest(s, (const DevSphere *)s->qIn0.ptr, (DevInteraction *)s->qOut.ptr, dInst, n, flag,
+    DevInteraction *dOut = (DevInteraction *)s->qOut.ptr;
+    switch (kind) {
+        case InstancedQuery::Rays:
+            rc = instancedRays(s, (const DevRay *)s->qIn0.ptr, dOut, dInst, n, flag, s->stream);
+            break;
+        case InstancedQuery::Sample:
+            rc = instancedSample(s, (const DevSphere *)s->qIn0.ptr, (const float3 *)s->qIn1.ptr, dOut, dInst, n,
                                  s->stream);
+            break;
+        case InstancedQuery::Silhouette:
+            rc = instancedSilhouettes(s, (const DevSphere *)s->qIn0.ptr, (const uint32_t *)s->qIn1.ptr, dOut, dInst, n,
+                                      sqMinR, precision, s->stream);
+            break;
+        default:
+            rc = instancedClosest(s, (const DevSphere *)s->qIn0.ptr, dOut, dInst, n, flag, s->stream);
+    }
     if (rc) return rc;
     uint32_t err[4] = {0, 0, 0, 0};
     if ((e = cudaMemcpyAsync(out, s->qOut.ptr, ob, cudaMemcpyDeviceToHost, s->stream)) != cudaSuccess)
@@ -760,6 +1157,12 @@ int instancedHost(fcpwgb_gpu_scene *s, const void *queries, size_t queryBytes, v
         return setError(FCPWGB_ERR_TRAVERSAL, "device traversal error word " + std::to_string(err[0]));
     }
     return FCPWGB_OK;
+}
+
+int instancedHost(fcpwgb_gpu_scene *s, const void *queries, size_t queryBytes, void *out, uint32_t *instOut,
+                  uint32_t n, bool rays, int flag) {
+    return instancedHostQuery(s, rays ? InstancedQuery::Rays : InstancedQuery::Closest, queries, queryBytes, nullptr,
+                              0, out, instOut, n, flag, 0.0f, 0.0f);
 }
 
 }  // namespace fcpwgb
@@ -779,6 +1182,8 @@ extern "C" int fcpwgb_gpu_scene_transfer_instanced(fcpwgb_gpu_scene *s, const fc
         st->objects.push_back(o);
         if ((rc = fcpwgb_gpu_scene_transfer_cpu_bvh(o, inst->objects[k]))) return rc;
     }
+    st->snch = true;
+    for (auto *o : st->objects) st->snch = st->snch && o->snch;
     std::vector<DevInstance> recs(st->nInstances);
     for (uint32_t i = 0; i < st->nInstances; i++) {
         std::memcpy(recs[i].t, &inst->t[(size_t)i * 12], 48);
@@ -799,6 +1204,7 @@ extern "C" int fcpwgb_gpu_scene_transfer_instanced(fcpwgb_gpu_scene *s, const fc
         }
     if (inst->top) {
         st->nTopNodes = inst->top->nNodes();
+        st->topDepth = inst->top->maxDepth();
         std::vector<unsigned char> nodes((size_t)st->nTopNodes * 32);
         inst->top->exportNodes(nodes.data());
         std::vector<uint32_t> refs(inst->top->primOrder().begin(), inst->top->primOrder().end());
@@ -858,4 +1264,91 @@ extern "C" int fcpwgb_intersect_rays_instanced_device(fcpwgb_gpu_scene *s, const
     if (rc) return rc;
     if (n > 0 && (!rays || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
     return instancedRays(s, (const DevRay *)rays, (DevInteraction *)out, instance_out, n, occl, s->pick(stream));
+}
+
+extern "C" int fcpwgb_intersect_spheres_instanced(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                  const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out,
+                                                  uint32_t *instance_out, uint32_t n) {
+    int rc = requireInstanced(s);
+    if (rc || n == 0) return rc;
+    if (!spheres || !rand_nums || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return instancedHostQuery(s, InstancedQuery::Sample, spheres, (size_t)n * sizeof(DevSphere), rand_nums,
+                              (size_t)n * sizeof(float3), out, instance_out, n, 0, 0.0f, 0.0f);
+}
+
+extern "C" int fcpwgb_intersect_spheres_instanced_device(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                         const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out,
+                                                         uint32_t *instance_out, uint32_t n, void *stream) {
+    int rc = requireInstanced(s);
+    if (rc) return rc;
+    if (n > 0 && (!spheres || !rand_nums || !out))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return instancedSample(s, (const DevSphere *)spheres, (const float3 *)rand_nums, (DevInteraction *)out,
+                           instance_out, n, s->pick(stream));
+}
+
+extern "C" int fcpwgb_find_closest_silhouette_points_instanced(fcpwgb_gpu_scene *s,
+                                                               const fcpwgb_bounding_sphere *spheres,
+                                                               const uint32_t *flip, fcpwgb_interaction *out,
+                                                               uint32_t *instance_out, uint32_t n, float sq_min_r,
+                                                               float precision) {
+    int rc = requireInstanced(s);
+    if (rc || n == 0) return rc;
+    if (!spheres || !flip || !out) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return instancedHostQuery(s, InstancedQuery::Silhouette, spheres, (size_t)n * sizeof(DevSphere), flip,
+                              (size_t)n * sizeof(uint32_t), out, instance_out, n, 0, sq_min_r, precision);
+}
+
+extern "C" int fcpwgb_find_closest_silhouette_points_instanced_device(fcpwgb_gpu_scene *s,
+                                                                      const fcpwgb_bounding_sphere *spheres,
+                                                                      const uint32_t *flip, fcpwgb_interaction *out,
+                                                                      uint32_t *instance_out, uint32_t n,
+                                                                      float sq_min_r, float precision, void *stream) {
+    int rc = requireInstanced(s);
+    if (rc) return rc;
+    if (n > 0 && (!spheres || !flip || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return instancedSilhouettes(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, instance_out, n, sq_min_r,
+                                precision, s->pick(stream));
+}
+
+static int requireObject(fcpwgb_gpu_scene *s, uint32_t object) {
+    int rc = requireInstanced(s);
+    if (rc) return rc;
+    if (object >= s->inst->objects.size()) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "object index out of range");
+    return FCPWGB_OK;
+}
+
+extern "C" int fcpwgb_gpu_scene_refit_object(fcpwgb_gpu_scene *s, uint32_t object, const void *primitives,
+                                             const void *silhouettes) {
+    int rc = requireObject(s, object);
+    if (rc) return rc;
+    fcpwgb_gpu_scene *o = s->inst->objects[object];
+    if ((rc = fcpwgb_gpu_scene_refit(o, primitives, silhouettes))) return rc;
+    if ((rc = s->activate())) return rc;
+    if ((rc = instancedTopRefit(s, s->stream))) return rc;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? FCPWGB_OK : cudaFail(e, "top-level refit");
+}
+
+extern "C" int fcpwgb_gpu_scene_update_object_vertices_device(fcpwgb_gpu_scene *s, uint32_t object,
+                                                              const float *positions, uint32_t n_vertices,
+                                                              void *stream) {
+    int rc = requireObject(s, object);
+    if (rc) return rc;
+    fcpwgb_gpu_scene *o = s->inst->objects[object];
+    cudaStream_t st = s->pick(stream);
+    if ((rc = fcpwgb_gpu_scene_update_vertices_device(o, positions, n_vertices, st))) return rc;
+    if ((rc = s->activate())) return rc;
+    return instancedTopRefit(s, st);
+}
+
+extern "C" int fcpwgb_gpu_scene_export_top_nodes(fcpwgb_gpu_scene *s, void *nodes, uint32_t *n_nodes) {
+    int rc = requireInstanced(s);
+    if (rc) return rc;
+    InstancedState &I = *s->inst;
+    if (n_nodes) *n_nodes = I.nTopNodes;
+    if (!nodes || I.nTopNodes == 0) return FCPWGB_OK;
+    cudaError_t e = cudaMemcpyAsync(nodes, I.topNodes.ptr, (size_t)I.nTopNodes * 32, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    return e == cudaSuccess ? FCPWGB_OK : cudaFail(e, "export top-level nodes");
 }

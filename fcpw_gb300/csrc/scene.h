@@ -162,4 +162,13 @@ int instancedRays(fcpwgb_gpu_scene *s, const DevRay *rays, DevInteraction *out, 
                   int occl, cudaStream_t st);
 int instancedHost(fcpwgb_gpu_scene *s, const void *queries, size_t queryBytes, void *out, uint32_t *instOut,
                   uint32_t n, bool rays, int flag);
+enum class InstancedQuery { Closest, Rays, Sample, Silhouette };
+int instancedHostQuery(fcpwgb_gpu_scene *s, InstancedQuery kind, const void *queries, size_t queryBytes,
+                       const void *second, size_t secondBytes, void *out, uint32_t *instOut, uint32_t n, int flag,
+                       float sqMinR, float precision);
+int instancedSilhouettes(fcpwgb_gpu_scene *s, const DevSphere *spheres, const uint32_t *flip, DevInteraction *out,
+                         uint32_t *instOut, uint32_t n, float sqMinR, float precision, cudaStream_t st);
+int instancedSample(fcpwgb_gpu_scene *s, const DevSphere *spheres, const float3 *randNums, DevInteraction *out,
+                    uint32_t *instOut, uint32_t n, cudaStream_t st);
+int instancedTopRefit(fcpwgb_gpu_scene *s, cudaStream_t st);
 }

@@ -338,7 +338,19 @@ class _GPUScene:
 
     def refit(self, scene: _Scene, update_geometry: bool = True) -> None:
         """GPUScene::refit (include/fcpw/fcpw_gpu.h:27): with update_geometry the moved
-        primitives (and silhouettes) are re-extracted from the scene and uploaded."""
+        primitives (and silhouettes) are re-extracted from the scene and uploaded. On
+        a scene of several objects or instances every object is refit, then the
+        top level (Scene::refit, fcpw.inl:1146-1158)."""
+        if getattr(self, "_instances", None) is not None:
+            for k, bvh in enumerate(scene.instances.objects):
+                if not update_geometry:
+                    check(lib().fcpwgb_gpu_scene_refit_object(self._h, k, None, None))
+                    continue
+                bvh.update_positions(scene.positions(k))
+                _, prims, sils = bvh.export()
+                check(lib().fcpwgb_gpu_scene_refit_object(self._h, k, ptr(prims),
+                                                          ptr(sils) if sils is not None and len(sils) else None))
+            return
         if not update_geometry:
             check(lib().fcpwgb_gpu_scene_refit(self._h, None, None))
             return
@@ -455,6 +467,66 @@ class _GPUScene:
         check(lib().fcpwgb_intersect_rays_instanced(self._h, ptr(rays), ptr(out), ptr(inst), len(rays),
                                                     int(bool(check_for_occlusion))))
         return inst
+
+    def intersect_spheres_instanced(self, sphere_centers, sphere_squared_radii, rand_nums,
+                                    interactions) -> np.ndarray:
+        """Sphere sampling on a scene of several objects or instances, returning
+        the instance of every sample (UINT_MAX where none)."""
+        spheres = R.make_spheres(sphere_centers, sphere_squared_radii)
+        rn = np.zeros((len(spheres), 3), np.float32)
+        r = np.asarray(rand_nums, np.float32)
+        rn[:, : r.shape[1]] = r
+        out = self._out(interactions, len(spheres))
+        inst = np.zeros(len(spheres), np.uint32)
+        check(lib().fcpwgb_intersect_spheres_instanced(self._h, ptr(spheres), ptr(rn), ptr(out), ptr(inst),
+                                                       len(spheres)))
+        return inst
+
+    def find_closest_silhouette_points_instanced(self, query_points, squared_max_radii, flip_normal_orientation,
+                                                 interactions, squared_min_radius: float = 0.0,
+                                                 precision: float = 1e-3) -> np.ndarray:
+        """Closest silhouette points on a scene of several objects or instances
+        (every object built with silhouettes), returning the instance of every
+        answer (UINT_MAX where none)."""
+        spheres = R.make_spheres(query_points, squared_max_radii)
+        flip = np.ascontiguousarray(np.asarray(flip_normal_orientation).astype(np.uint32))
+        if len(flip) != len(spheres):
+            raise ValueError("flip_normal_orientation must have one entry per query")
+        out = self._out(interactions, len(spheres))
+        inst = np.zeros(len(spheres), np.uint32)
+        check(lib().fcpwgb_find_closest_silhouette_points_instanced(self._h, ptr(spheres), ptr(flip), ptr(out),
+                                                                    ptr(inst), len(spheres), float(squared_min_radius),
+                                                                    float(precision)))
+        return inst
+
+    def refit_object(self, object_index: int, primitives=None, silhouettes=None) -> None:
+        """Refits one object of a scene of several objects or instances from its
+        records (interop layouts, its leaf order; None: its device geometry as
+        it is), then the top-level tree (fcpwgb_gpu_scene_refit_object)."""
+        p = np.ascontiguousarray(primitives) if primitives is not None else None
+        s = np.ascontiguousarray(silhouettes) if silhouettes is not None and len(silhouettes) else None
+        check(lib().fcpwgb_gpu_scene_refit_object(self._h, int(object_index), ptr(p), ptr(s)))
+
+    def update_object_vertices_tensor(self, object_index: int, positions) -> None:
+        """Moves one object's vertices to ``positions`` (a CUDA float32 tensor (V, DIM)
+        in the object's vertex order) and refits it and the top level on the
+        device, on the current torch stream."""
+        import torch
+        if positions.dtype != torch.float32 or not positions.is_cuda or not positions.is_contiguous():
+            raise ValueError("positions must be a contiguous float32 CUDA tensor")
+        stream = torch.cuda.current_stream(positions.device).cuda_stream
+        check(lib().fcpwgb_gpu_scene_update_object_vertices_device(self._h, int(object_index), positions.data_ptr(),
+                                                                   positions.shape[0], C.c_void_p(stream)))
+
+    def export_top_nodes(self) -> np.ndarray:
+        """The device's top-level tree of a scene of several objects or instances
+        (32 B interop nodes; empty for a single instance)."""
+        n = C.c_uint32(0)
+        check(lib().fcpwgb_gpu_scene_export_top_nodes(self._h, None, C.byref(n)))
+        nodes = np.zeros(n.value, R.BVH_NODE)
+        if n.value:
+            check(lib().fcpwgb_gpu_scene_export_top_nodes(self._h, ptr(nodes), C.byref(n)))
+        return nodes
 
     def instance_objects(self) -> np.ndarray:
         """Object of every instance of the transferred scene."""

@@ -240,9 +240,8 @@ class _Scene:
             self._bvh = CpuBvh(self.DIM, self._positions[0], self._indices[0], int(aggregate_type),
                                self._silhouettes)
         else:
-            if self._silhouettes:
-                raise NotImplementedError("silhouettes are not supported on scenes of several objects or instances")
-            objs = [CpuBvh(self.DIM, p, f, int(aggregate_type), False) for p, f in zip(self._positions, self._indices)]
+            objs = [CpuBvh(self.DIM, p, f, int(aggregate_type), self._silhouettes)
+                    for p, f in zip(self._positions, self._indices)]
             inst_obj, mats = [], []
             for k, ts in enumerate(self._transforms):
                 if not ts:

@@ -243,6 +243,50 @@ int fcpwgb_intersect_rays_instanced(fcpwgb_gpu_scene *scene, const fcpwgb_ray *r
 int fcpwgb_intersect_rays_instanced_device(fcpwgb_gpu_scene *scene, const fcpwgb_ray *rays,
                                            fcpwgb_interaction *interactions, uint32_t *instance_out, uint32_t n,
                                            int check_for_occlusion, void *stream);
+/* Sphere sampling and closest silhouette points on a scene of several objects
+ * or instances: the reference CPU's stochastic top-level descent with
+ * aggregate leaves (include/fcpw/aggregates/bvh.inl:1140-1288; every instance
+ * in the chosen leaf sampled with the current random number, one of those
+ * that hit chosen uniformly) and its silhouette walk (bvh.inl:1435-1596), each
+ * instance through TransformedAggregate (include/fcpw/core/primitive.h:392-466:
+ * query and minimum radius to object space, the object's own tree, the answer
+ * back to world space; a sample keeps its object-space pdf). Silhouette
+ * queries need every object built with silhouettes, else every result keeps
+ * its default record. instance_out (may be NULL) receives each answer's
+ * instance (UINT_MAX when none). The regular fcpwgb_intersect_spheres* and
+ * fcpwgb_find_closest_silhouette_points* entry points route here too. */
+int fcpwgb_intersect_spheres_instanced(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                       const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out,
+                                       uint32_t *instance_out, uint32_t n);
+int fcpwgb_intersect_spheres_instanced_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                              const fcpwgb_float3 *rand_nums, fcpwgb_interaction *out,
+                                              uint32_t *instance_out, uint32_t n, void *stream);
+int fcpwgb_find_closest_silhouette_points_instanced(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                                    const uint32_t *flip, fcpwgb_interaction *out,
+                                                    uint32_t *instance_out, uint32_t n, float squared_min_radius,
+                                                    float precision);
+int fcpwgb_find_closest_silhouette_points_instanced_device(fcpwgb_gpu_scene *scene,
+                                                           const fcpwgb_bounding_sphere *spheres,
+                                                           const uint32_t *flip, fcpwgb_interaction *out,
+                                                           uint32_t *instance_out, uint32_t n,
+                                                           float squared_min_radius, float precision, void *stream);
+/* Refit of one object of an instanced scene without a new transfer
+ * (Scene::updateObjectVertices + Scene::refit, include/fcpw/fcpw.inl:1146-1158,
+ * bvh.inl:548-599): the object's tree is refit from the given records
+ * (primitives / silhouettes in its leaf order, NULL = its device geometry as
+ * it is; as fcpwgb_gpu_scene_refit), or from device vertex positions in the
+ * object's own vertex order (as fcpwgb_gpu_scene_update_vertices_device, on
+ * stream), then the top level: every instance's box is its object's new root
+ * box mapped by its transform, and the top-level nodes are their unions. The
+ * object is shared by all its instances. */
+int fcpwgb_gpu_scene_refit_object(fcpwgb_gpu_scene *scene, uint32_t object, const void *primitives,
+                                  const void *silhouettes);
+int fcpwgb_gpu_scene_update_object_vertices_device(fcpwgb_gpu_scene *scene, uint32_t object, const float *positions,
+                                                   uint32_t n_vertices, void *stream);
+/* The device's top-level tree of an instanced scene (32 B interop nodes, leaf
+ * references are instance indices): n_nodes receives the count, nodes (may be
+ * NULL) the records; synchronous. No counterpart in the reference's GPU path. */
+int fcpwgb_gpu_scene_export_top_nodes(fcpwgb_gpu_scene *scene, void *nodes, uint32_t *n_nodes);
 
 /* Scene::build(AggregateType::Bvh, ...) + transferToGPU (fcpw.h:95,
  * fcpw_gpu.h:21) with the tree built on the device: a linear BVH over the

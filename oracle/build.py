@@ -34,6 +34,7 @@ REF_OUT = HERE / "_ref"
 ORACLE_LIB = BUILD / "liboracle.so"
 REF_LIB = REF_OUT / "libfcpw_ref.so"
 REF_SIMD_LIB = REF_OUT / "libfcpw_ref_simd.so"
+REF_SIMD_ERROR = REF_OUT / "libfcpw_ref_simd.error.txt"  # why the vectorised build failed on this host
 STAGED = REPO / "baseline" / "_ref"
 STAGED_INCLUDE = STAGED / "include"
 STAGED_ENOKI = STAGED / "deps" / "enoki" / "include"
@@ -111,6 +112,8 @@ def _build_ref(out: Path, extra: list[str], force: bool) -> Path | None:
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         errors = [ln for ln in r.stderr.splitlines() if "error" in ln]
+        if out == REF_SIMD_LIB:
+            REF_SIMD_ERROR.write_text("\n".join(errors[:4]) + "\n")
         raise RuntimeError(f"reference build failed ({out.name}):\n" + "\n".join(errors[:20]) + "\n" +
                            r.stderr[-3000:])
     os.replace(tmp, out)
@@ -128,6 +131,8 @@ def build_reference_simd(force: bool = False) -> Path | None:
     aarch64; elsewhere the build takes whatever vector ISA the compiler's default enables."""
     if reference_include() is None or not (STAGED_ENOKI / "enoki" / "array.h").exists():
         return None
+    if REF_SIMD_ERROR.exists():
+        REF_SIMD_ERROR.unlink()
     extra = ["-DFCPW_USE_ENOKI", "-DFCPW_SIMD_WIDTH=4", "-I", str(STAGED_ENOKI), "-O3"]
     if host_isa() in ("aarch64", "arm64"):
         # Enoki's NEON backend converts between vector register types implicitly, which GCC 13 rejects

@@ -106,15 +106,18 @@ def affine(dim, rng):
     return m.astype(np.float32)
 
 
-def make_instanced(name, dim, objects, n_transforms, aggregate, box, seed, n=2000):
+def make_instanced(name, dim, objects, n_transforms, aggregate, box, seed, n=2000, silhouettes=False):
     """A scene of several objects with instance transforms (Scene::setObjectCount,
     setObjectInstanceTransforms): the reference's top-level tree (leaf
     references as instance numbers: objects in turn, an object without
     transforms one instance, an object's transforms in turn) and its answers
-    with the object index of every result."""
+    with the object index of every result: closest points, rays, sphere
+    samples, closest silhouette points (scenes built with silhouettes), and,
+    after moving the first object's vertices (updateObjectVertices + refit),
+    the refit top-level tree and closest points."""
     rng = np.random.default_rng(seed)
     transforms = [[affine(dim, rng) for _ in range(k)] for k in n_transforms]
-    ref = RefMultiScene(dim, objects, transforms, aggregate)
+    ref = RefMultiScene(dim, objects, transforms, aggregate, silhouettes=silhouettes)
     top_nodes, agg_refs = ref.export_top()
     agg_to_inst, inst, nxt = {}, 0, len(objects)
     for k, ts in enumerate(transforms):
@@ -126,7 +129,7 @@ def make_instanced(name, dim, objects, n_transforms, aggregate, box, seed, n=200
             nxt += 1
             inst += 1
     top_refs = np.array([agg_to_inst[int(a)] for a in agg_refs] if len(top_nodes) else [], np.uint32)
-    out = {"dim": dim, "aggregate": aggregate, "n_objects": len(objects),
+    out = {"dim": dim, "aggregate": aggregate, "n_objects": len(objects), "silhouettes": bool(silhouettes),
            "n_transforms": np.array(n_transforms, np.int32),
            "transforms": np.array([m for ts in transforms for m in ts], np.float32).reshape(-1, dim + 1, dim + 1),
            "top_nodes": top_nodes, "top_refs": top_refs}
@@ -145,6 +148,24 @@ def make_instanced(name, dim, objects, n_transforms, aggregate, box, seed, n=200
     _, oh, _ = ref.intersect_rays_objects(rays, occlusion=True)
     out.update(cp_points=pts, cp_out=res, cp_object=obj, cpr_r2=r2, cpr_out=res2, cpr_object=obj2,
                ray_o=o, ray_d=d, ray_out=ro, ray_hit=rh, ray_object=robj, occ_hit=oh)
+    # sphere sampling (Scene::intersect(sphere, randNums)): radii that reach a few primitives
+    ss_c = _queries(dim, n, lo, hi, seed + 5)
+    ss_r2 = (W.rng(seed + 6).uniform(0.05, 1.5, n) ** 2).astype(np.float32)
+    ss_rand = W.rng(seed + 7).uniform(0, 1, (n, 3)).astype(np.float32)
+    ss_out, ss_hit, ss_obj = ref.sphere_sample_objects(R.make_spheres(ss_c, ss_r2), ss_rand)
+    out.update(ss_c=ss_c, ss_r2=ss_r2, ss_rand=ss_rand, ss_out=ss_out, ss_hit=ss_hit, ss_object=ss_obj)
+    if silhouettes:
+        sil_pts = _queries(dim, n, lo, hi, seed + 8)
+        sil_flip = (W.rng(seed + 9).uniform(0, 1, n) < 0.5).astype(np.uint32)
+        sil_out, sil_obj = ref.silhouettes_objects(R.make_spheres(sil_pts, R.FLT_MAX), sil_flip)
+        out.update(sil_points=sil_pts, sil_flip=sil_flip, sil_out=sil_out, sil_object=sil_obj)
+    # refit after moving the first object (shared by all its instances)
+    v0 = np.asarray(objects[0][0], np.float32)
+    moved = (v0 * np.float32(1.04) + W.rng(seed + 10).normal(0, 0.01, v0.shape)).astype(np.float32)
+    ref.update_object_and_refit(0, moved)
+    rt_nodes, _ = ref.export_top()
+    rres, robj2 = ref.closest_points_objects(R.make_spheres(pts, R.FLT_MAX), record_normals=False)
+    out.update(refit_positions=moved, refit_top_nodes=rt_nodes, refit_cp_out=rres, refit_cp_object=robj2)
     np.savez_compressed(HERE / f"{name}.npz", **out)
     print(f"{name}: {len(objects)} objects, {inst} instances, {len(top_nodes)} top-level nodes")
 
@@ -177,6 +198,11 @@ def main(names=()):
     s1, g1 = W.star_polylines(1, 40, SEED + 15)
     if want("instanced2d"):
         make_instanced("instanced2d", 2, [(s0, g0), (s1, g1)], [9, 6], 3, (-5.0, 5.0), SEED + 50)
+    if want("instanced3d_sil"):
+        make_instanced("instanced3d_sil", 3, [(vt, ft), (v, f)], [6, 0], 3, (-5.0, 5.0), SEED + 60, silhouettes=True)
+    if want("instanced2d_sil"):
+        make_instanced("instanced2d_sil", 2, [(s0, g0), (s1, g1)], [5, 3], 3, (-5.0, 5.0), SEED + 70,
+                       silhouettes=True)
 
 
 if __name__ == "__main__":

@@ -15,6 +15,7 @@ from oracle import oracle as O
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 NAMES = ["instanced3d", "instanced3d_single", "multi3d_plain", "instanced2d"]
+SIL_NAMES = ["instanced3d_sil", "instanced2d_sil"]
 
 
 def load(name):
@@ -38,6 +39,8 @@ def scene_of(g):
         if n:
             s.set_object_instance_transforms(list(g["transforms"][t:t + n]), i)
             t += n
+    if bool(g.get("silhouettes", False)):
+        s.compute_silhouettes()
     s.build(int(g["aggregate"]), False)
     return s
 
@@ -49,7 +52,7 @@ def oracle_inputs(s):
     return inst, top_nodes, top_refs, mats, objs
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", NAMES + SIL_NAMES)
 def test_top_level_tree_equals_reference(name):
     g = load(name)
     s = scene_of(g)

@@ -12,7 +12,7 @@ from fcpw_gb300 import records as R
 from fcpw_gb300 import workloads as W
 from helpers import compare_rays, distance_tolerance, ray_prim_f64, _prim_vertices
 from oracle import oracle as O
-from test_cpu_instanced import NAMES, load, oracle_inputs, scene_of
+from test_cpu_instanced import NAMES, SIL_NAMES, load, oracle_inputs, scene_of
 
 pytestmark = pytest.mark.gpu
 
@@ -251,9 +251,10 @@ def test_single_tree_operations_refuse_instanced_scene():
     pts = gd["cp_points"][:100]
     with pytest.raises(F.FcpwError):
         g.refit_arrays()
-    with pytest.raises(F.FcpwError):
-        g.find_closest_silhouette_points(pts, np.full(100, R.FLT_MAX, np.float32), np.zeros(100, np.uint32),
-                                         F.GPUInteractionList())
+    # objects built without silhouettes: every silhouette result keeps its default record
+    sil = F.GPUInteractionList()
+    g.find_closest_silhouette_points(pts, np.full(100, R.FLT_MAX, np.float32), np.zeros(100, np.uint32), sil)
+    assert (sil.array()["index"] == R.UINT_MAX).all()
     with pytest.raises(F.FcpwError):
         g.contains(pts)
     # a single-tree transfer replaces the instanced scene
@@ -266,3 +267,93 @@ def test_single_tree_operations_refuse_instanced_scene():
     out = F.GPUInteractionList()
     g.find_closest_points(pts, np.full(100, R.FLT_MAX, np.float32), out)
     assert (out.array()["index"] != R.UINT_MAX).all()
+
+
+def _objects_of(s, which):
+    inst = s.instances.instance_objects
+    return np.where(which != R.UINT_MAX, inst[np.minimum(which, len(inst) - 1)].astype(np.int64), -1)
+
+
+@pytest.mark.parametrize("name", NAMES + SIL_NAMES)
+def test_sphere_sampling_matches_reference(name):
+    """Scene::intersect(sphere, randNums) on several objects: the reference's
+    stochastic top-level descent, every instance of the chosen leaf sampled
+    with the current random number through its transform. The same object
+    and primitive are chosen (the selection rescales one random number through
+    every choice, so a last-bit difference in an area can flip a choice: at
+    most 1 in 1000), and the sample's point and pdf agree."""
+    gd = load(name)
+    s = scene_of(gd)
+    g = gpu_of(s, branching=4, bits=32)
+    out = F.GPUInteractionList()
+    which = g.intersect_spheres_instanced(gd["ss_c"], gd["ss_r2"], gd["ss_rand"], out)
+    got, ref, hit = out.array(), gd["ss_out"], gd["ss_hit"]
+    gh = which != R.UINT_MAX
+    assert (gh != hit).sum() <= 1
+    both = gh & hit
+    assert both.sum() >= 50
+    same = (got["index"][both] == ref["index"][both]) & (_objects_of(s, which)[both] == gd["ss_object"][both])
+    assert same.mean() > 0.999
+    assert np.allclose(got["d"][both][same], ref["d"][both][same], rtol=1e-4)
+    assert np.allclose(got["p"][both][same], ref["p"][both][same], atol=1e-4)
+    plain = F.GPUInteractionList()  # the regular entry point routes to the same kernel
+    g.intersect(gd["ss_c"], gd["ss_r2"], gd["ss_rand"], plain)
+    assert plain.array().tobytes() == got.tobytes()
+    assert g.check_errors() == 0
+
+
+@pytest.mark.parametrize("name", SIL_NAMES)
+def test_silhouettes_match_reference(name):
+    """Closest silhouette points on several objects with instance transforms:
+    found flags equal, distances within the reference's own classification
+    precision (1e-3, tests/aggregate_tests.cpp:610), and the object the same
+    unless the two silhouette points are at the same distance."""
+    gd = load(name)
+    s = scene_of(gd)
+    dim = s.DIM
+    g = gpu_of(s, branching=4, bits=32)
+    pts = gd["sil_points"]
+    out = F.GPUInteractionList()
+    which = g.find_closest_silhouette_points_instanced(pts, np.full(len(pts), R.FLT_MAX, np.float32),
+                                                       gd["sil_flip"], out)
+    got, ref = out.array(), gd["sil_out"]
+    fg, fr = which != R.UINT_MAX, gd["sil_object"] >= 0
+    assert (fg != fr).sum() <= 1
+    both = fg & fr
+    tol = distance_tolerance(pts[both], ref["p"][both][:, :dim], ref["d"][both])
+    dd = np.abs(got["d"][both].astype(np.float64) - ref["d"][both])
+    assert np.all(dd <= 1e-3 * ref["d"][both] + tol)
+    obj_diff = _objects_of(s, which)[both] != gd["sil_object"][both]
+    assert np.all(dd[obj_diff] <= 1e-3 * ref["d"][both][obj_diff] + tol[obj_diff])
+    plain = F.GPUInteractionList()
+    g.find_closest_silhouette_points(pts, np.full(len(pts), R.FLT_MAX, np.float32), gd["sil_flip"], plain)
+    assert plain.array().tobytes() == got.tobytes()
+    assert g.check_errors() == 0
+
+
+@pytest.mark.parametrize("name", NAMES + SIL_NAMES)
+@pytest.mark.parametrize("device_update", [False, True])
+def test_object_refit_matches_reference(name, device_update):
+    """After the first object's vertices move, refitting that object (from its
+    records, or from device vertex positions) and the top level gives the
+    reference's refit top-level boxes bit for bit and its closest points."""
+    import torch
+    gd = load(name)
+    s = scene_of(gd)
+    g = gpu_of(s, branching=4, bits=32)
+    moved = gd["refit_positions"]
+    if device_update:
+        g.update_object_vertices_tensor(0, torch.from_numpy(moved).cuda())
+        torch.cuda.synchronize()
+    else:
+        s.update_object_vertices(moved, 0)
+        g.refit(s)
+    top = g.export_top_nodes()
+    assert top.tobytes() == gd["refit_top_nodes"].tobytes()
+    pts = gd["cp_points"]
+    out = F.GPUInteractionList()
+    which = g.find_closest_points_instanced(pts, np.full(len(pts), R.FLT_MAX, np.float32), out)
+    moved_scene = scene_of(dict(gd, obj0_positions=moved))
+    compare_instanced(moved_scene, pts, out.array(), which, gd["refit_cp_out"], gd["refit_cp_object"],
+                      f"{name} after refit")
+    assert g.check_errors() == 0
