@@ -517,13 +517,15 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
         ray_ms = timed(ray_run)
         hits = float((out[:, 9].view(torch.int32) != -1).float().mean())
         table = []
-        for wb in [(2, 32, True, False), (4, 8, True, False), (4, 16, True, False), (4, 32, True, False),
-                   (4, 32, False, False), (8, 8, True, False), (8, 16, True, False), (8, 32, True, False),
-                   (2, 32, True, True), (4, 8, True, True), (4, 32, True, True), (8, 32, True, True)]:
-            g.set_traversal(*wb[:2], sort_queries=wb[2], packet=wb[3])
+        # (branching, bits, sort, schedule): 0 one thread per ray, 1 warp packets, 2 per-lane refill
+        for wb in [(2, 32, True, 0), (4, 8, True, 0), (4, 16, True, 0), (4, 32, True, 0), (4, 32, False, 0),
+                   (8, 8, True, 0), (8, 16, True, 0), (8, 32, True, 0), (4, 32, True, 1), (8, 32, True, 1),
+                   (2, 32, True, 2), (2, 32, False, 2), (4, 8, True, 2), (4, 16, True, 2), (4, 32, True, 2),
+                   (4, 32, False, 2), (8, 8, True, 2), (8, 16, True, 2), (8, 32, True, 2), (8, 32, False, 2)]:
+            g.set_traversal(*wb[:2], sort_queries=wb[2], packet=wb[3] == 1, persistent=wb[3] == 2)
             table.append((wb, timed(ray_run, reps=3)))
         (wb_best, _) = min(table, key=lambda t: t[1])
-        g.set_traversal(*wb_best[:2], sort_queries=wb_best[2], packet=wb_best[3])
+        g.set_traversal(*wb_best[:2], sort_queries=wb_best[2], packet=wb_best[3] == 1, persistent=wb_best[3] == 2)
         fast_ms = timed(ray_run)
         nodes, prims, _ = s.cpu_bvh.export()
         refs = reference_cpu(3, v, f)
@@ -551,9 +553,10 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
                       "plain": {"queries_per_s": n / (ray_ms / 1e3), "ms": ray_ms},
                       "fast": {"queries_per_s": n / (fast_ms / 1e3), "ms": fast_ms,
                                "variant": {"branching": wb_best[0], "bits": wb_best[1], "sort_queries": wb_best[2],
-                                           "packet": wb_best[3]}},
+                                           "schedule": ["thread", "packet", "refill"][wb_best[3]]}},
                       "speedup_vs_plain": ray_ms / fast_ms, "hit_fraction": hits,
-                      "autotune_ms": [[w, b, int(o), int(pk), round(t, 3)] for (w, b, o, pk), t in table],
+                      "autotune_ms": [[w, b, int(o), ["thread", "packet", "refill"][pk], round(t, 3)]
+                                      for (w, b, o, pk), t in table],
                       "cpu_baseline": cpu})
         del g, s
 

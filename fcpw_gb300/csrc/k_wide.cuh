@@ -1027,6 +1027,150 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
     }
 }
 
+// Rays with per-lane refill (persistent blocks, one resident wave): a lane
+// whose ray is finished takes the next one at once (one atomicAdd per warp for
+// all lanes that need a ray), and every iteration advances each active lane's
+// ray by one step -- one record (child slab tests, nearest entry next, the
+// others pushed farthest first) or one leaf (its primitives, then a pop) -- so
+// lanes stay busy however unequal the rays' traversals are (most random rays
+// leave the scene box after a few records, a few cross many). The semantics
+// are those of wideRay: children within the current tMax, stacked entries
+// skipped once beyond it, hits accepted when 0 <= t <= tMax (a later equal t
+// wins), an occlusion ray done at its first hit. Only the winner's leaf
+// position is kept during the walk; its record (point, normal, uv) is
+// recomputed from it at the end with the same arithmetic.
+template<int W, int BITS, class Prim>
+__global__ void __launch_bounds__(kWideBlock, 8) kWideRayRefill(const unsigned char *__restrict__ nodes,
+                                                             const unsigned char *__restrict__ prims,
+                                                             const DevRay *__restrict__ rays,
+                                                             const uint32_t *__restrict__ perm,
+                                                             DevInteraction *__restrict__ out, uint32_t n, int occl,
+                                                             const DevRay *__restrict__ callerRays,
+                                                             const int *sortInfo, uint32_t *counter,
+                                                             uint32_t *errorWord, unsigned long long *stats) {
+    constexpr uint32_t kSlotMask = W - 1;
+    if (sortInfo && keepOrder(sortInfo, n)) {  // rays left in the caller's order
+        rays = callerRays;
+        perm = nullptr;
+    }
+    __shared__ uint32_t sRef[kShortStack * kWideBlock];
+    __shared__ float sD[kShortStack * kWideBlock];
+    WideStack<kShortStack> st;
+    st.sRef = sRef + threadIdx.x;
+    st.sD = sD + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    bool active = false;
+    uint32_t id = 0, cur = 0, bestSel = kUintMax;
+    int sp = 0;
+    DevRay r;
+    unsigned long long tExp = 0, tTests = 0;
+    WideNodeRegs<W, BITS> node;
+    for (;;) {
+        const uint32_t need = __ballot_sync(0xffffffffu, !active);
+        if (need) {
+            const uint32_t leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active) {
+                id = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
+                if (id < n) {
+                    const unsigned char *rp = reinterpret_cast<const unsigned char *>(rays + id);
+                    const float2 a = ldg2(rp), b = ldg2(rp + 8), cc = ldg2(rp + 16), d = ldg2(rp + 24),
+                                 e = ldg2(rp + 32);
+                    r.o = make_float3(a.x, a.y, b.x);
+                    r.d = make_float3(b.y, cc.x, cc.y);
+                    r.dInv = make_float3(d.x, d.y, e.x);
+                    r.tMax = e.y;
+                    cur = 0;
+                    sp = 0;
+                    bestSel = kUintMax;
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (!active) continue;
+        bool popNext = true, finished = false;
+        if (!(cur & kLeafBit)) {
+            node.load(nodes, cur);
+            tExp++;
+            uint32_t key[W];
+            int nh = 0;
+#pragma unroll
+            for (int k = 0; k < W; k++) {
+                float t0, t1;
+                const bool hit = node.cnt(k) != kWideEmpty &&
+                                 boxRayIntersect(make_float3(node.bound(0, k), node.bound(1, k), node.bound(2, k)),
+                                                 make_float3(node.bound(3, k), node.bound(4, k), node.bound(5, k)), r,
+                                                 t0, t1);
+                key[k] = hit ? ((__float_as_uint(t0 + 0.0f) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
+                nh += hit ? 1 : 0;
+            }
+            sortNetwork<W>(key);
+            if (nh > 0) {
+                if (sp + nh - 1 > kWideStack) {
+                    atomicOr(errorWord, kErrStackOverflow);
+                    finished = true;
+                } else {
+                    uint32_t refs[W];
+                    childRefs<W, BITS>(node, refs);
+#pragma unroll
+                    for (int k = W - 1; k >= 1; k--) {
+                        if (k < nh) {
+                            st.push(sp, selectBySlot<W>(refs, key[k] & kSlotMask),
+                                    __uint_as_float(key[k] & ~kSlotMask));
+                            sp++;
+                        }
+                    }
+                    cur = selectBySlot<W>(refs, key[0] & kSlotMask);
+                    popNext = false;
+                }
+            }
+        } else {
+            const uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+            tTests += cnt;
+            for (uint32_t p = 0; p < cnt; p++) {
+                const Prim prim = Prim::load(prims, off + p);
+                DevInteraction c;
+                if (prim.intersect(r, occl != 0, c)) {
+                    bestSel = off + p;
+                    if (occl) {
+                        finished = true;
+                        break;
+                    }
+                    r.tMax = fminf(r.tMax, c.d);
+                }
+            }
+        }
+        if (popNext && !finished) {
+            finished = true;
+            while (sp > 0) {
+                sp--;
+                if (st.dist(sp) <= r.tMax) {
+                    cur = st.ref(sp);
+                    finished = false;
+                    break;
+                }
+            }
+        }
+        if (finished) {
+            DevInteraction best = defaultInteraction();
+            if (bestSel != kUintMax) {
+                const Prim prim = Prim::load(prims, bestSel);
+                if (!occl) prim.intersect(r, false, best);  // the winner again: r.tMax is its t
+                best.index = prim.index;
+            }
+            out[perm ? __ldg(perm + id) : id] = best;
+            active = false;
+        }
+    }
+    if (stats) {
+        atomicAdd(stats + 1, tExp);
+        atomicAdd(stats + 2, tTests);
+    }
+}
+
 // Ray packets: the 32 (sorted) rays of a warp walk the wide tree together,
 // as kWidePacketClosestPoint does for closest points. Each record is loaded
 // once for the warp; every lane slab-tests its own ray against every child
@@ -1298,7 +1442,21 @@ template<int W> cudaError_t launchRequantizeT(int bits, unsigned char *wideNodes
             kern<<<g, b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.callerRays, l.sortInfo,  \
                                  l.errorWord, l.stats);                                                            \
         };                                                                                                         \
-        if (dim == 3) {                                                                                            \
+        auto refill = [&](auto kern) {                                                                             \
+            kern<<<dim3(l.grid), b, 0, s>>>(l.nodes, l.prims, l.rays, l.perm, l.out, l.n, l.occl, l.callerRays,     \
+                                            l.sortInfo, l.counter, l.errorWord, l.stats);                          \
+        };                                                                                                         \
+        if (l.counter) {                                                                                           \
+            if (dim == 3) {                                                                                        \
+                if (bits == 8) refill(kWideRayRefill<W, 8, Tri48Prim>);                                            \
+                else if (bits == 16) refill(kWideRayRefill<W, 16, Tri48Prim>);                                    \
+                else refill(kWideRayRefill<W, 32, Tri48Prim>);                                                     \
+            } else {                                                                                               \
+                if (bits == 8) refill(kWideRayRefill<W, 8, Seg24Prim>);                                            \
+                else if (bits == 16) refill(kWideRayRefill<W, 16, Seg24Prim>);                                    \
+                else refill(kWideRayRefill<W, 32, Seg24Prim>);                                                     \
+            }                                                                                                      \
+        } else if (dim == 3) {                                                                                     \
             if (bits == 8) l.packet ? go(kWidePacketRay<W, 8, Tri48Prim>) : go(kWideRay<W, 8, Tri48Prim>);         \
             else if (bits == 16) l.packet ? go(kWidePacketRay<W, 16, Tri48Prim>) : go(kWideRay<W, 16, Tri48Prim>); \
             else l.packet ? go(kWidePacketRay<W, 32, Tri48Prim>) : go(kWideRay<W, 32, Tri48Prim>);                 \

@@ -92,6 +92,8 @@ struct WideRayLaunch {
     uint32_t n = 0;
     int occl = 0;
     int packet = 0;                         // 1: warp packets (kWidePacketRay)
+    uint32_t *counter = nullptr;            // zeroed ray counter: per-lane refill (kWideRayRefill), grid blocks
+    uint32_t grid = 0;
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;
 };

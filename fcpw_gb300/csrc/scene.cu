@@ -155,6 +155,12 @@ int GpuScene::wideRays(const DevRay *r, DevInteraction *out, uint32_t n, int occ
     l.packet = wideConfig.packet;
     l.errorWord = (uint32_t *)errorWord.ptr;
     cudaError_t e;
+    if (wideConfig.persistent && !wideConfig.packet) {  // per-lane refill from a counter, one resident wave
+        if ((rc = workCounter.ensure(16))) return rc;
+        if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
+        l.counter = (uint32_t *)workCounter.ptr;
+        l.grid = std::min<uint32_t>((n + 127) / 128, (uint32_t)smCount() * 8u);
+    }
     if (wideConfig.sortQueries && n >= 4096) {
         if ((rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;
         if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;

@@ -166,10 +166,12 @@ def test_wide_2d_segments():
 
 @pytest.mark.parametrize("branching", [2, 4, 8])
 @pytest.mark.parametrize("bits", [32, 16, 8])
-@pytest.mark.parametrize("packet", [False, True])
-def test_wide_rays_match_oracle(torus, branching, bits, packet):
+@pytest.mark.parametrize("schedule", ["thread", "refill", "packet"])
+def test_wide_rays_match_oracle(torus, branching, bits, schedule):
     """Rays on the wide trees (sorted by direction octant and origin), one
-    thread per ray or warp packets, against the reference CPU order."""
+    thread per ray, lanes refilled from a counter (persistent), or warp
+    packets, against the reference CPU order."""
+    packet = schedule == "packet"
     s, g, pts, ref, prims = torus
     n = 60000
     o = W.uniform_points(n, 3, -2, 2, 51)
@@ -178,7 +180,7 @@ def test_wide_rays_match_oracle(torus, branching, bits, packet):
     nodes, _, _ = s.cpu_bvh.export()
     rays = R.make_rays(o, d, tmax)
     ref_out, ref_hit = O.intersect_rays_bvh(3, nodes, prims, rays)
-    g.set_traversal(branching, bits, sort_queries=True, packet=packet)
+    g.set_traversal(branching, bits, sort_queries=True, packet=packet, persistent=schedule == "refill")
     out = F.GPUInteractionList()
     g.intersect(o, d, tmax, out)
     compare_rays(3, prims, rays, out.array(), ref_out, ref_hit)
@@ -191,8 +193,9 @@ def test_wide_rays_match_oracle(torus, branching, bits, packet):
 
 @pytest.mark.parametrize("cfg", [dict(branching=0), dict(branching=2, bits=32, sort_queries=True),
                                  dict(branching=4, bits=8, sort_queries=True, packet=True),
-                                 dict(branching=8, bits=16, sort_queries=False),
-                                 dict(branching=4, bits=32, sort_queries=True, packet=False)])
+                                 dict(branching=8, bits=16, sort_queries=False, persistent=False),
+                                 dict(branching=4, bits=32, sort_queries=True, persistent=False),
+                                 dict(branching=4, bits=32, sort_queries=False, persistent=True)])
 def test_rays_aimed_at_edges_and_vertices(torus, cfg):
     """Rays through edge midpoints and vertices (grazing hits, equidistant
     ties between the faces of an edge or a vertex): every kernel passes the
