@@ -4,8 +4,9 @@
 // tree together: every node record is loaded once for the warp, and each
 // lane applies the reference's tests to its own query -- a child is visited
 // when it has a normal cone (halfAngle >= 0), its box is within the query's
-// radius and the cone overlaps the view cone of its box (coneOverlap on the
-// same box and squared distance) -- and a lane takes part in a subtree only
+// radius and the cone overlaps the view cone of its box (coneOverlapFast,
+// which decides as coneOverlap, on the same box and squared distance) -- and
+// a lane takes part in a subtree only
 // while it passes them. The children go in the order of the first active
 // lane's distances, the farther one onto a warp stack (shared memory, one
 // distance column per lane) that is re-checked against each lane's radius
@@ -101,11 +102,11 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
                 bool hitL = act && lc.halfAngle >= 0.0f, hitR = act && rc.halfAngle >= 0.0f;
                 if (hitL) {
                     dl = boxSphereD2Min(lb.pMin, lb.pMax, c);
-                    hitL = dl <= rp2 && coneOverlap<DIM>(lc.axis, lc.halfAngle, lc.radius, c, lb.pMin, lb.pMax, dl);
+                    hitL = dl <= rp2 && coneOverlapFast<DIM>(lc.axis, lc.halfAngle, lc.radius, c, lb.pMin, lb.pMax, dl);
                 }
                 if (hitR) {
                     dr = boxSphereD2Min(rb.pMin, rb.pMax, c);
-                    hitR = dr <= rp2 && coneOverlap<DIM>(rc.axis, rc.halfAngle, rc.radius, c, rb.pMin, rb.pMax, dr);
+                    hitR = dr <= rp2 && coneOverlapFast<DIM>(rc.axis, rc.halfAngle, rc.radius, c, rb.pMin, rb.pMax, dr);
                 }
                 const bool anyL = __ballot_sync(0xffffffffu, hitL) != 0, anyR = __ballot_sync(0xffffffffu, hitR) != 0;
                 if (anyL || anyR) {

@@ -155,13 +155,16 @@ int GpuScene::wideRays(const DevRay *r, DevInteraction *out, uint32_t n, int occ
     l.packet = wideConfig.packet;
     l.errorWord = (uint32_t *)errorWord.ptr;
     cudaError_t e;
-    if (wideConfig.persistent && !wideConfig.packet) {  // per-lane refill from a counter, one resident wave
+    // per-lane refill reads the rays in the caller's order: on 4M random rays it took 0.76 ms unsorted
+    // against 1.25 ms with the octant-and-origin sort (0.45 ms of it the sort itself)
+    const bool refill = wideConfig.persistent && !wideConfig.packet;
+    if (refill) {  // per-lane refill from a counter, one resident wave
         if ((rc = workCounter.ensure(16))) return rc;
         if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)workCounter.ptr;
         l.grid = std::min<uint32_t>((n + 127) / 128, (uint32_t)smCount() * 8u);
     }
-    if (wideConfig.sortQueries && n >= 4096) {
+    if (wideConfig.sortQueries && !refill && n >= 4096) {
         if ((rc = sortCells.ensure(sizeof(uint32_t) * kSortScratchWords))) return rc;
         if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
         if ((rc = sortRays.ensure((size_t)n * sizeof(DevRay)))) return rc;

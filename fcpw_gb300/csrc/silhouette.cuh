@@ -58,6 +58,55 @@ FCPWGB_HD bool coneOverlap(float3 axis, float halfAngle, float radius, float3 o,
                                  : inRangeF(kPi2F, dAxisAngle - halfAngleSum, dAxisAngle + halfAngleSum);
 }
 
+// The same decision as coneOverlap without its inverse trigonometric functions
+// wherever a margin makes the answer certain. With x = |axis . v| (v the unit
+// view-cone axis), h the cone's half angle and phi the view cone's half angle,
+// coneOverlap's test |acos(x') - pi/2| <= h + phi (x' the signed dot product)
+// is |asin(x')| <= H, H = h + phi, i.e. x <= sin(H) while H < pi/2, and
+// H >= pi/2 means sin(phi) >= cos(h). In sine space: sin(phi) = radius / l
+// (l > radius) or d / sqrt(d^2 + s^2) (the box's projected half extent d at
+// distance s), sin(H) = sin h cos phi + cos h sin phi, and sin h, cos h by
+// the fast intrinsics (absolute error below 1e-6 on [0, pi/2)). Every
+// comparison is decided only when it clears kConeMargin = 1e-5, which exceeds
+// the rounding of both evaluations by more than ten times (the dot product,
+// the intrinsics, and coneOverlap's acos / asin / atan2 and angle sums, each
+// within a few 2^-24 in sine space); otherwise coneOverlap itself decides. So
+// the outcome is coneOverlap's, with the transcendental functions evaluated
+// only for boxes within 1e-5 of the cone's boundary.
+constexpr float kConeMargin = 1e-5f;
+template<int DIM>
+FCPWGB_D bool coneOverlapFast(float3 axis, float halfAngle, float radius, float3 o, float3 bMin, float3 bMax,
+                              float distToBox) {
+    if (halfAngle >= kPi2F || distToBox < kFltEps) return true;
+    const float3 c = (bMin + bMax) * 0.5f;
+    float3 v = c - o;
+    const float l = len3(v);
+    v = v / l;
+    const float x = fabsf(fmaxf(-1.0f, fminf(1.0f, dot3(axis, v))));
+    const float sh = __sinf(halfAngle), ch = __cosf(halfAngle);
+    if (x <= sh - kConeMargin) return true;  // the first test: |acos - pi/2| <= h
+    float sp, cp;
+    if (l > radius) {
+        sp = radius / l;
+        cp = sqrtf(fmaxf(0.0f, 1.0f - sp * sp));
+    } else {
+        const float3 e = bMax - c;
+        const float d = dot3(e, make_float3(fabsf(v.x), fabsf(v.y), fabsf(v.z)));
+        const float s = l - d;
+        if (s <= 0.0f) return true;
+        const float dp = DIM == 3 ? projectToPlane3(v, e) : projectToPlane2(v, e);
+        const float nrm = sqrtf(dp * dp + s * s);
+        sp = dp / nrm;
+        cp = s / nrm;
+    }
+    if (sp >= ch + kConeMargin) return true;  // h + phi >= pi/2
+    if (sp > ch - kConeMargin) return coneOverlap<DIM>(axis, halfAngle, radius, o, bMin, bMax, distToBox);
+    const float sH = sh * cp + ch * sp;
+    if (x <= sH - kConeMargin) return true;
+    if (x >= sH + kConeMargin) return false;
+    return coneOverlap<DIM>(axis, halfAngle, radius, o, bMin, bMax, distToBox);
+}
+
 // geometry.slang:490-522
 FCPWGB_HD bool isSilhouetteVertex(float3 n0, float3 n1, float3 viewDir, float d, bool flip, float precision) {
     float sign = flip ? 1.0f : -1.0f;

@@ -379,7 +379,9 @@ int fcpwgb_debug_fill_static_scratch(fcpwgb_gpu_scene *scene, uint32_t word, uin
  * removed). With branching > 0, closest silhouette points are answered by
  * warp packets on the binary SNCH tree (unless squared_min_radius > 0),
  * contains sorts its points spatially (sort_queries), and rays are sorted by
- * direction octant, then origin (sort_queries). */
+ * direction octant, then origin (sort_queries), except with persistent (and
+ * not packet): a persistent wave of lanes then takes the rays in the
+ * caller's order, each lane the next ray as soon as its own is done. */
 typedef struct {
     int branching;     /* 0, 2, 4 or 8 */
     int bits;          /* 32, 16 or 8 */
