@@ -763,8 +763,8 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
 
 def _schedule(c) -> str:
     lanes = c.get("threads_per_query", 1)
-    s = "packet" if c.get("packet") else (f"coop{lanes}" if lanes > 1 else
-                                          ("persistent" if c.get("persistent") else "thread"))
+    s = ("packetq" if c.get("persistent") else "packet") if c.get("packet") else \
+        (f"coop{lanes}" if lanes > 1 else ("persistent" if c.get("persistent") else "thread"))
     if c.get("leaf_size"):
         s += f"+leaf{c['leaf_size']}"
     if not c.get("packet") and lanes == 1 and c.get("short_stack", 16) != 16:

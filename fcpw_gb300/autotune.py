@@ -14,9 +14,10 @@ import itertools
 
 # schedule: "thread" = one thread per query, "persistent" = persistent blocks
 # with neighbour seeding, "packet" = the queries of a warp traverse together,
+# "packetq" = packets handed to the warps of persistent blocks from a counter,
 # "coopL" = L lanes (2, 4, 8) answer one query together
 DEFAULT_SPACE = {"branching": [2, 4, 8], "bits": [8, 16, 32],
-                 "schedule": ["thread", "persistent", "packet", "coop2", "coop4", "coop8"],
+                 "schedule": ["thread", "persistent", "packet", "packetq", "coop2", "coop4", "coop8"],
                  "leaf_size": [6, 8, 12], "short_stack": [0]}
 
 
@@ -28,7 +29,8 @@ def candidates(space=None, sort_queries=True, precise=True):
     """The stage-1 grid (leaf_size 0, short_stack 16)."""
     space = dict(DEFAULT_SPACE, **(space or {}))
     for b, q, sch in itertools.product(space["branching"], space["bits"], space["schedule"]):
-        yield {"branching": b, "bits": q, "persistent": sch == "persistent", "packet": sch == "packet",
+        yield {"branching": b, "bits": q, "persistent": sch in ("persistent", "packetq"),
+               "packet": sch in ("packet", "packetq"),
                "sort_queries": sort_queries, "precise": precise, "leaf_size": 0, "short_stack": 16,
                "threads_per_query": lanes_of(sch)}
 

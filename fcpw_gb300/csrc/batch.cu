@@ -256,7 +256,7 @@ int enqueue(fcpwgb_gpu_batch *b, const DevSphere *spheres, DevInteraction *out, 
     l.packet = b->cfg.packet;
     l.shortStack = b->cfg.shortStack;
     l.lanes = b->cfg.lanes;
-    if (b->cfg.persistent && !b->cfg.packet && b->cfg.lanes == 1) {
+    if (b->cfg.persistent && b->cfg.lanes == 1) {
         if ((e = cudaMemsetAsync(b->counter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)b->counter.ptr;
         blocks = std::min<uint32_t>(blocks, (uint32_t)b->numSMs * 8u);

@@ -723,6 +723,11 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
 // entry is popped. Queries of a warp that start at different roots (a forest
 // whose scene boundary falls inside the warp) are walked one root at a time.
 constexpr int kPacketShort = 32;  // warp-stack entries held in shared memory
+// With `counter` non-NULL the blocks are persistent (one resident wave) and
+// every warp takes its next packet -- 32 consecutive sorted queries -- from
+// the counter as soon as its previous one is done, so a block whose warps
+// finish unevenly keeps all of them busy instead of holding its slot until
+// the slowest warp ends.
 template<int W, int BITS, class Prim, bool PRECISE, bool STATS>
 __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const unsigned char *__restrict__ nodes,
                                                                       const unsigned char *__restrict__ prims,
@@ -731,7 +736,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                                                                       const uint32_t *__restrict__ roots,
                                                                       DevInteraction *__restrict__ out,
                                                                       uint2 *__restrict__ sel, uint32_t n,
-                                                                      int recordNormal, uint32_t *errorWord,
+                                                                      int recordNormal, uint32_t *counter,
+                                                                      uint32_t *errorWord,
                                                                       unsigned long long *stats) {
     constexpr uint32_t kSlotMask = W - 1;
     constexpr int kWarps = kWideBlock / 32;
@@ -740,154 +746,164 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
     uint32_t lRef[kWideStack - kPacketShort];  // deeper entries: every lane keeps the (uniform) refs
     float lDist[kWideStack - kPacketShort];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
-    const bool valid = i < n;
-    float3 c = make_float3(0.f, 0.f, 0.f);
-    float r2 = -1.0f;  // a lane without a query needs nothing
-    uint32_t root = 0;
-    if (valid) {
-        float4 s4 = ldg4(spheres + i);
-        c = make_float3(s4.x, s4.y, s4.z);
-        r2 = queryRadius2(c, s4.w);
-        root = roots ? __ldg(roots + i) : 0u;
-    }
-    DevInteraction best = defaultInteraction();
-    uint32_t selected = kUintMax;
-    bool found = false;
-    NearTie<PRECISE> tie;
-    const float r2User = r2;
-    float rp2 = tie.prune(r2, c);  // pruning radius^2 (NaN for a lane without a query)
     Count<STATS> tExp, tTests, tVisits, tPrimLoads;
     WideNodeRegs<W, BITS> node;
+    uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
+    for (;;) {
+        if (counter) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(counter, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n) break;
+            i = base + lane;
+        }
+        const bool valid = i < n;
+        float3 c = make_float3(0.f, 0.f, 0.f);
+        float r2 = -1.0f;  // a lane without a query needs nothing
+        uint32_t root = 0;
+        if (valid) {
+            float4 s4 = ldg4(spheres + i);
+            c = make_float3(s4.x, s4.y, s4.z);
+            r2 = queryRadius2(c, s4.w);
+            root = roots ? __ldg(roots + i) : 0u;
+        }
+        DevInteraction best = defaultInteraction();
+        uint32_t selected = kUintMax;
+        bool found = false;
+        NearTie<PRECISE> tie;
+        const float r2User = r2;
+        float rp2 = tie.prune(r2, c);  // pruning radius^2 (NaN for a lane without a query)
 
-    uint32_t pending = __ballot_sync(0xffffffffu, valid);
-    while (pending) {
-        const uint32_t rootNow = __shfl_sync(0xffffffffu, root, __ffs(pending) - 1);
-        const bool mine = valid && root == rootNow && ((pending >> lane) & 1u);
-        pending &= ~__ballot_sync(0xffffffffu, mine);
-        bool act = mine;  // this lane needs the current record
-        uint32_t cur = rootNow;
-        int sp = 0;       // warp-uniform
-        for (;;) {
-            bool descend = false;
-            if (!(cur & kLeafBit)) {
-                node.load(nodes, cur);
-                tVisits.add(1);
-                float d2Min[W];
-                childD2Min<W, BITS>(node, c, d2Min);
-                if (act) {
-                    tExp.add(1);
-                    if (!found) {
-#pragma unroll
-                        for (int k = 0; k < W; k++)
-                            if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
-                        rp2 = tie.prune(r2, c);
+        uint32_t pending = __ballot_sync(0xffffffffu, valid);
+        while (pending) {
+            const uint32_t rootNow = __shfl_sync(0xffffffffu, root, __ffs(pending) - 1);
+            const bool mine = valid && root == rootNow && ((pending >> lane) & 1u);
+            pending &= ~__ballot_sync(0xffffffffu, mine);
+            bool act = mine;  // this lane needs the current record
+            uint32_t cur = rootNow;
+            int sp = 0;       // warp-uniform
+            for (;;) {
+                bool descend = false;
+                if (!(cur & kLeafBit)) {
+                    node.load(nodes, cur);
+                    tVisits.add(1);
+                    float d2Min[W];
+                    childD2Min<W, BITS>(node, c, d2Min);
+                    if (act) {
+                        tExp.add(1);
+                        if (!found) {
+    #pragma unroll
+                            for (int k = 0; k < W; k++)
+                                if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
+                            rp2 = tie.prune(r2, c);
+                        }
                     }
-                }
-                // children needed by any lane (one OR over the warp of each lane's
-                // mask), ordered by the first active lane's distances
-                uint32_t needMask = 0;
-#pragma unroll
-                for (int k = 0; k < W; k++)
-                    needMask |= (act && node.cnt(k) != kWideEmpty && d2Min[k] <= rp2) ? (1u << k) : 0u;
-                const uint32_t anyMask = __reduce_or_sync(0xffffffffu, needMask);
-                const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
-                uint32_t key[W];
-#pragma unroll
-                for (int k = 0; k < W; k++) {
-                    const float lead = __shfl_sync(0xffffffffu, d2Min[k], leader);
-                    key[k] = ((anyMask >> k) & 1u) ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
-                }
-                const int nh = __popc(anyMask);
-                sortNetwork<W>(key);
-                if (nh > 0) {
-                    if (sp + nh - 1 > kWideStack) {
-                        if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
-                        break;
+                    // children needed by any lane (one OR over the warp of each lane's
+                    // mask), ordered by the first active lane's distances
+                    uint32_t needMask = 0;
+    #pragma unroll
+                    for (int k = 0; k < W; k++)
+                        needMask |= (act && node.cnt(k) != kWideEmpty && d2Min[k] <= rp2) ? (1u << k) : 0u;
+                    const uint32_t anyMask = __reduce_or_sync(0xffffffffu, needMask);
+                    const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
+                    uint32_t key[W];
+    #pragma unroll
+                    for (int k = 0; k < W; k++) {
+                        const float lead = __shfl_sync(0xffffffffu, d2Min[k], leader);
+                        key[k] = ((anyMask >> k) & 1u) ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
                     }
-                    uint32_t rawRefs[W];
-#pragma unroll
-                    for (int s = 0; s < W; s++) rawRefs[s] = node.ref(s);
-#pragma unroll
-                    for (int k = W - 1; k >= 0; k--) {
-                        if (k < nh) {
-                            const uint32_t slot = key[k] & kSlotMask;
-                            const uint32_t cnt = node.cntAt(slot);
-                            const uint32_t ref = selectBySlot<W>(rawRefs, slot);
-                            const uint32_t packed = cnt == 0 ? ref : packLeaf(ref, cnt);
-                            // a lane out of this record is out of its children too (NaN is never <= rp2)
-                            const float dl = act ? selectBySlot<W>(d2Min, slot) : __int_as_float(0x7fc00000);
-                            if (k == 0) {
-                                cur = packed;
-                                act = dl <= rp2;
-                            } else {
-                                if (sp < kPacketShort) {
-                                    if (lane == 0) sRef[warp][sp] = packed;
-                                    sDist[warp][sp][lane] = dl;
+                    const int nh = __popc(anyMask);
+                    sortNetwork<W>(key);
+                    if (nh > 0) {
+                        if (sp + nh - 1 > kWideStack) {
+                            if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
+                            break;
+                        }
+                        uint32_t rawRefs[W];
+    #pragma unroll
+                        for (int s = 0; s < W; s++) rawRefs[s] = node.ref(s);
+    #pragma unroll
+                        for (int k = W - 1; k >= 0; k--) {
+                            if (k < nh) {
+                                const uint32_t slot = key[k] & kSlotMask;
+                                const uint32_t cnt = node.cntAt(slot);
+                                const uint32_t ref = selectBySlot<W>(rawRefs, slot);
+                                const uint32_t packed = cnt == 0 ? ref : packLeaf(ref, cnt);
+                                // a lane out of this record is out of its children too (NaN is never <= rp2)
+                                const float dl = act ? selectBySlot<W>(d2Min, slot) : __int_as_float(0x7fc00000);
+                                if (k == 0) {
+                                    cur = packed;
+                                    act = dl <= rp2;
                                 } else {
-                                    lRef[sp - kPacketShort] = packed;
-                                    lDist[sp - kPacketShort] = dl;
+                                    if (sp < kPacketShort) {
+                                        if (lane == 0) sRef[warp][sp] = packed;
+                                        sDist[warp][sp][lane] = dl;
+                                    } else {
+                                        lRef[sp - kPacketShort] = packed;
+                                        lDist[sp - kPacketShort] = dl;
+                                    }
+                                    sp++;
                                 }
-                                sp++;
+                            }
+                        }
+                        __syncwarp();
+                        descend = true;
+                    }
+                } else {
+                    uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
+                    tPrimLoads.add(cnt);
+                    if (act) tTests.add(cnt);
+                    for (uint32_t p = 0; p < cnt; p++) {
+                        Prim prim = Prim::load(prims, off + p);
+                        if (act) {
+                            float3 pt;
+                            float2 uv;
+                            float d = prim.closestPoint(c, pt, uv);
+                            if (beatsWinner(found, d, r2, best.d, off + p, selected)) {
+                                if (found) tie.replaced(best.d, selected);
+                                r2 = fminf(r2, d * d);
+                                rp2 = tie.pruneHit(d, c);
+                                best.p = pt;
+                                best.n = make_float3(0.f, 0.f, 0.f);
+                                best.uv = uv;
+                                best.d = d;
+                                best.index = prim.index;
+                                selected = off + p;
+                                found = true;
+                            } else {
+                                tie.offer(d, off + p, selected);
                             }
                         }
                     }
-                    __syncwarp();
-                    descend = true;
                 }
-            } else {
-                uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
-                tPrimLoads.add(cnt);
-                if (act) tTests.add(cnt);
-                for (uint32_t p = 0; p < cnt; p++) {
-                    Prim prim = Prim::load(prims, off + p);
-                    if (act) {
-                        float3 pt;
-                        float2 uv;
-                        float d = prim.closestPoint(c, pt, uv);
-                        if (beatsWinner(found, d, r2, best.d, off + p, selected)) {
-                            if (found) tie.replaced(best.d, selected);
-                            r2 = fminf(r2, d * d);
-                            rp2 = tie.pruneHit(d, c);
-                            best.p = pt;
-                            best.n = make_float3(0.f, 0.f, 0.f);
-                            best.uv = uv;
-                            best.d = d;
-                            best.index = prim.index;
-                            selected = off + p;
-                            found = true;
-                        } else {
-                            tie.offer(d, off + p, selected);
-                        }
+                if (descend) continue;
+                // pop until some lane needs the entry
+                bool next = false;
+                while (sp > 0) {
+                    sp--;
+                    uint32_t ref;
+                    float dl;
+                    if (sp < kPacketShort) {
+                        ref = sRef[warp][sp];
+                        dl = sDist[warp][sp][lane];
+                    } else {
+                        ref = lRef[sp - kPacketShort];
+                        dl = lDist[sp - kPacketShort];
+                    }
+                    act = dl <= rp2;
+                    if (__ballot_sync(0xffffffffu, act)) {
+                        cur = ref;
+                        next = true;
+                        break;
                     }
                 }
+                __syncwarp();
+                if (!next) break;
             }
-            if (descend) continue;
-            // pop until some lane needs the entry
-            bool next = false;
-            while (sp > 0) {
-                sp--;
-                uint32_t ref;
-                float dl;
-                if (sp < kPacketShort) {
-                    ref = sRef[warp][sp];
-                    dl = sDist[warp][sp][lane];
-                } else {
-                    ref = lRef[sp - kPacketShort];
-                    dl = lDist[sp - kPacketShort];
-                }
-                act = dl <= rp2;
-                if (__ballot_sync(0xffffffffu, act)) {
-                    cur = ref;
-                    next = true;
-                    break;
-                }
-            }
-            __syncwarp();
-            if (!next) break;
         }
+        if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, r2User, found, selected, recordNormal, best, tie);
+        if (!counter) break;
     }
-    if (valid) finishQuery<Prim, PRECISE>(prims, perm, out, sel, i, c, r2User, found, selected, recordNormal, best, tie);
     if (STATS && stats) {
         if (lane == 0) {
             atomicAdd(stats + 3, tVisits.get());
@@ -1382,7 +1398,8 @@ cudaError_t launchWideClosestKernel(const WideLaunch &l, cudaStream_t s) {
         launchCoop<W, B, Prim, PRECISE, STATS, 8>(l, s);
     else if (l.packet)
         kWidePacketClosestPoint<W, B, Prim, PRECISE, STATS><<<g, b, 0, s>>>(
-            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.errorWord, l.stats);
+            l.nodes, l.prims, l.spheres, l.perm, l.roots, l.out, l.sel, l.n, l.recordNormal, l.counter, l.errorWord,
+            l.stats);
     else if (l.counter) {
         if (l.shortStack)
             kWideClosestPoint<W, B, Prim, PRECISE, true, STATS, kShortStack><<<g, b, 0, s>>>(

@@ -116,7 +116,7 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
     l.packet = c.packet;
     l.shortStack = c.shortStack;
     l.lanes = c.lanes;
-    if (c.persistent && !c.packet && c.lanes == 1) {
+    if (c.persistent && c.lanes == 1) {  // persistent threads, or packets fed to warps from a counter
         if ((rc = workCounter.ensure(16))) return rc;
         if ((e = cudaMemsetAsync(workCounter.ptr, 0, 4, st)) != cudaSuccess) return cudaFail(e, "memset");
         l.counter = (uint32_t *)workCounter.ptr;

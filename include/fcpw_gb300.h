@@ -365,8 +365,9 @@ int fcpwgb_debug_fill_static_scratch(fcpwgb_gpu_scene *scene, uint32_t word, uin
  * for triangles in a second kernel after the traversal, for segments at its
  * end;
  * packet traverses the 32 (sorted) queries of a warp together, one record
- * load per warp and step, each query pruning with its own radius (persistent
- * is then ignored); leaf_size > 0 collapses binary subtrees of at most that
+ * load per warp and step, each query pruning with its own radius (with
+ * persistent, one resident wave of blocks whose warps take the next 32
+ * queries from a counter as soon as their packet is done); leaf_size > 0 collapses binary subtrees of at most that
  * many primitives (up to 15) into one wide leaf; short_stack is the number of
  * traversal-stack entries per thread kept in shared memory by the
  * one-thread-per-query schedules (0 or 16; the others in local memory);

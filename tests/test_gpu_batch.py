@@ -68,12 +68,13 @@ def _tensor_run(b, pts, offsets, **kw):
 
 @pytest.mark.parametrize("branching", [2, 4, 8])
 @pytest.mark.parametrize("bits", [32, 16, 8])
-@pytest.mark.parametrize("schedule", ["thread", "persistent", "packet"])
+@pytest.mark.parametrize("schedule", ["thread", "persistent", "packet", "packetq", "coop4"])
 def test_batch_matches_per_scene_oracle(batch3, branching, bits, schedule):
     """Warps straddling scene boundaries (137 and 1 queries) exercise the
     per-root passes of the packet kernel and the root change of the seeds."""
     b, scenes, pts, refs, prims, offsets = batch3
-    b.set_traversal(branching, bits, persistent=schedule == "persistent", precise=True, packet=schedule == "packet")
+    b.set_traversal(branching, bits, persistent=schedule in ("persistent", "packetq"), precise=True,
+                    packet=schedule in ("packet", "packetq"), threads_per_query=4 if schedule == "coop4" else 1)
     got, _ = _tensor_run(b, pts, offsets)
     _check(b, pts, refs, prims, offsets, got, f"batch {branching}/{bits}/{schedule}")
     assert b.check_errors() == 0

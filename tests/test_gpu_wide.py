@@ -336,7 +336,9 @@ def test_every_wide_layout_and_schedule_agrees_exactly(torus, precise, scale):
                 dict(branching=8, bits=32, packet=True), dict(branching=4, bits=16, sort_queries=False),
                 dict(branching=4, bits=32, threads_per_query=4), dict(branching=8, bits=8, threads_per_query=8),
                 dict(branching=2, bits=32, threads_per_query=2), dict(branching=8, bits=16, threads_per_query=2),
-                dict(branching=4, bits=8, leaf_size=12, threads_per_query=8)]:
+                dict(branching=4, bits=8, leaf_size=12, threads_per_query=8),
+                dict(branching=4, bits=32, packet=True, persistent=False),
+                dict(branching=8, bits=16, packet=True, persistent=True)]:
         g.set_traversal(precise=precise, **cfg)
         outs[str(cfg)] = _run(g, sub).tobytes()
     g.set_traversal(0)
