@@ -807,8 +807,8 @@ def batched_scenes_bench(device_index: int, reps: int = 5):
     t0 = time.perf_counter()
     batch.set_scenes(scenes)
     set_s = time.perf_counter() - t0
-    space = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "packet"], "leaf_size": [8],
-             "short_stack": [0]}
+    space = {"branching": [2, 4, 8], "bits": [8, 16, 32], "schedule": ["thread", "packet", "packetq"],
+             "leaf_size": [8], "short_stack": [0]}
     best, table = autotune_batch(batch, spheres, offsets, space=space, reps=2)
 
     def timed(fn):
@@ -948,10 +948,10 @@ def run_ours(args):
     sample = spheres[: min(n, 1 << 20)]
     if args.variant == "auto":
         best, table = autotune_closest_points(gpu, sample)
-    else:  # fixed "branching,bits,schedule" (0 thread, 1 persistent, 2 packet, 3/4/5 groups of 2/4/8 lanes),
-        # e.g. for profiling one kernel
+    else:  # fixed "branching,bits,schedule" (0 thread, 1 persistent, 2 packet, 3/4/5 groups of 2/4/8 lanes,
+        # 6 packets from a counter), e.g. for profiling one kernel
         b, q, p = (int(x) for x in args.variant.split(","))
-        best = {"branching": b, "bits": q, "persistent": p == 1, "packet": p == 2, "sort_queries": True,
+        best = {"branching": b, "bits": q, "persistent": p in (1, 6), "packet": p in (2, 6), "sort_queries": True,
                 "precise": True, "threads_per_query": {3: 2, 4: 4, 5: 8}.get(p, 1)}
         gpu.set_traversal(**best)
         table = []
@@ -971,9 +971,9 @@ def run_ours(args):
         for bits in (8, 16):
             rows = []
             for br in (4, 8):
-                for sch in ("thread", "packet"):
-                    cfg = dict(best, branching=br, bits=bits, persistent=False, packet=sch == "packet", leaf_size=0,
-                               short_stack=16)
+                for sch in ("thread", "packet", "packetq"):
+                    cfg = dict(best, branching=br, bits=bits, persistent=sch == "packetq", packet=sch != "thread",
+                               leaf_size=0, short_stack=16, threads_per_query=1)
                     try:
                         gpu.set_traversal(**cfg)
                         rows.append((cfg, timed(3, 2)[0]))
