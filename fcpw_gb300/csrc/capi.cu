@@ -780,7 +780,15 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
         perm = (const uint32_t *)s->sortPerm.ptr;
     }
     if (s->usePacketSilhouettes(sq_min_r)) {
-        FCPWGB_CUDA(launchSilhouettePacket(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st));
+        uint32_t *counter = nullptr, grid = 0;
+        if (s->wideConfig.persistent) {  // packets handed to the warps of one resident wave from a counter
+            if ((rc = s->workCounter.ensure(16))) return rc;
+            FCPWGB_CUDA(cudaMemsetAsync(s->workCounter.ptr, 0, 4, st));
+            counter = (uint32_t *)s->workCounter.ptr;
+            grid = std::min<uint32_t>((n + 127) / 128, (uint32_t)s->smCount() * 8u);
+        }
+        FCPWGB_CUDA(launchSilhouettePacket(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision,
+                                           counter, grid, st));
         return FCPWGB_OK;
     }
     FCPWGB_CUDA(launchSilhouetteBinary(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st));

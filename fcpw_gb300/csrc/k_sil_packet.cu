@@ -33,6 +33,9 @@ namespace {
 
 constexpr int kSilShort = 32;  // warp-stack entries in shared memory; deeper ones in registers/local
 
+// With `counter` non-NULL the blocks are persistent (one resident wave) and
+// every warp takes its next packet of 32 sorted queries from the counter as
+// soon as its previous one is done.
 template<class Sil, int DIM>
 __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigned char *__restrict__ nodes,
                                                                 const unsigned char *__restrict__ sils,
@@ -40,7 +43,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
                                                                 const uint32_t *__restrict__ flip,
                                                                 const uint32_t *__restrict__ perm,
                                                                 DevInteraction *__restrict__ out, uint32_t n,
-                                                                float sqMinR, float precision,
+                                                                float sqMinR, float precision, uint32_t *counter,
                                                                 uint32_t *errorWord) {
     constexpr int kWarps = kWideBlock / 32;
     __shared__ uint32_t sRef[kWarps][kSilShort];
@@ -48,136 +51,146 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
     uint32_t lRef[kStackDepth - kSilShort];
     float lDist[kStackDepth - kSilShort];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
-    const bool valid = i < n;
-    const uint32_t slot = valid ? (perm ? __ldg(perm + i) : i) : 0u;  // the caller's slot
-    float3 c = make_float3(0.f, 0.f, 0.f);
-    float r2 = -1.0f;
-    bool flipNormal = false;
-    if (valid) {
-        const float4 s4 = ldg4(spheres + i);
-        c = make_float3(s4.x, s4.y, s4.z);
-        r2 = queryRadius2(c, s4.w);
-        flipNormal = __ldg(flip + slot) != 0;
-    }
-    DevInteraction best = defaultInteraction();
-    uint32_t bestPos = kUintMax;
-    // boxes are pruned against rp2: the radius widened by the rounding band
-    float rp2 = bandRadius2(sqrtf(r2), c);
-
-    const NodeBox root = loadNode<64>(nodes, 0);
-    bool act = valid && !(sqMinR >= r2) && boxSphereD2Min(root.pMin, root.pMax, c) <= rp2;
-    uint32_t cur = 0;
-    int sp = 0;  // warp-uniform
-    if (__ballot_sync(0xffffffffu, act)) {
-        for (;;) {
-            const NodeBox node = loadNode<64>(nodes, cur);
-            bool next = false;
-            if (node.nPrims > 0) {
-                const NodeCone cone = loadCone(nodes, cur);
-                for (uint32_t p = 0; p < cone.nSil; p++) {
-                    const Sil sil = Sil::load(sils, cone.silOffset + p);
-                    const uint32_t pos = cone.silOffset + p;
-                    if (act && sil.index == best.index) {
-                        // the winner again, listed in another leaf (an edge is listed for both of
-                        // its faces): not tested again, as in the reference, but its earliest
-                        // listing is what a tie compares against
-                        bestPos = min(bestPos, pos);
-                    } else if (act) {
-                        DevInteraction cI = defaultInteraction();
-                        if (sil.closestSilhouettePoint(c, r2, flipNormal, sqMinR, precision, cI) &&
-                            (bestPos == kUintMax || cI.d < best.d || (cI.d == best.d && pos < bestPos))) {
-                            r2 = fminf(r2, cI.d * cI.d);
-                            rp2 = bandRadius2(cI.d, c);
-                            best = cI;
-                            bestPos = pos;
-                        }
-                    }
-                }
-            } else {
-                const uint32_t li = cur + 1, ri = cur + node.offset;
-                const NodeCone lc = loadCone(nodes, li), rc = loadCone(nodes, ri);
-                const NodeBox lb = loadNode<64>(nodes, li), rb = loadNode<64>(nodes, ri);
-                float dl = 0.0f, dr = 0.0f;
-                bool hitL = act && lc.halfAngle >= 0.0f, hitR = act && rc.halfAngle >= 0.0f;
-                if (hitL) {
-                    dl = boxSphereD2Min(lb.pMin, lb.pMax, c);
-                    hitL = dl <= rp2 && coneOverlapFast<DIM>(lc.axis, lc.halfAngle, lc.radius, c, lb.pMin, lb.pMax, dl);
-                }
-                if (hitR) {
-                    dr = boxSphereD2Min(rb.pMin, rb.pMax, c);
-                    hitR = dr <= rp2 && coneOverlapFast<DIM>(rc.axis, rc.halfAngle, rc.radius, c, rb.pMin, rb.pMax, dr);
-                }
-                const bool anyL = __ballot_sync(0xffffffffu, hitL) != 0, anyR = __ballot_sync(0xffffffffu, hitR) != 0;
-                if (anyL || anyR) {
-                    bool takeR = !anyL;
-                    if (anyL && anyR) {
-                        // the first active lane's nearer child first (the reference's order for that lane)
-                        const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
-                        const float ldl = __shfl_sync(0xffffffffu, hitL ? dl : kFltMax, leader);
-                        const float ldr = __shfl_sync(0xffffffffu, hitR ? dr : kFltMax, leader);
-                        takeR = ldr < ldl;
-                        if (sp >= kStackDepth) {
-                            if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
-                            break;
-                        }
-                        const uint32_t other = takeR ? li : ri;
-                        const float dOther = (takeR ? hitL : hitR) ? (takeR ? dl : dr) : __int_as_float(0x7fc00000);
-                        if (sp < kSilShort) {
-                            if (lane == 0) sRef[warp][sp] = other;
-                            sDist[warp][sp][lane] = dOther;  // NaN: this lane does not need it
-                        } else {
-                            lRef[sp - kSilShort] = other;
-                            lDist[sp - kSilShort] = dOther;
-                        }
-                        sp++;
-                        __syncwarp();
-                    }
-                    cur = takeR ? ri : li;
-                    act = takeR ? hitR : hitL;
-                    next = true;
-                }
-            }
-            if (next) continue;
-            // pop until some lane needs the entry
-            while (sp > 0) {
-                sp--;
-                uint32_t ref;
-                float d;
-                if (sp < kSilShort) {
-                    ref = sRef[warp][sp];
-                    d = sDist[warp][sp][lane];
-                } else {
-                    ref = lRef[sp - kSilShort];
-                    d = lDist[sp - kSilShort];
-                }
-                act = d <= rp2 && !(sqMinR >= r2);
-                if (__ballot_sync(0xffffffffu, act)) {
-                    cur = ref;
-                    next = true;
-                    break;
-                }
-            }
-            __syncwarp();
-            if (!next) break;
+    uint32_t i = blockIdx.x * kWideBlock + threadIdx.x;
+    for (;;) {
+        if (counter) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(counter, 32u);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n) break;
+            i = base + lane;
         }
+        const bool valid = i < n;
+        const uint32_t slot = valid ? (perm ? __ldg(perm + i) : i) : 0u;  // the caller's slot
+        float3 c = make_float3(0.f, 0.f, 0.f);
+        float r2 = -1.0f;
+        bool flipNormal = false;
+        if (valid) {
+            const float4 s4 = ldg4(spheres + i);
+            c = make_float3(s4.x, s4.y, s4.z);
+            r2 = queryRadius2(c, s4.w);
+            flipNormal = __ldg(flip + slot) != 0;
+        }
+        DevInteraction best = defaultInteraction();
+        uint32_t bestPos = kUintMax;
+        // boxes are pruned against rp2: the radius widened by the rounding band
+        float rp2 = bandRadius2(sqrtf(r2), c);
+
+        const NodeBox root = loadNode<64>(nodes, 0);
+        bool act = valid && !(sqMinR >= r2) && boxSphereD2Min(root.pMin, root.pMax, c) <= rp2;
+        uint32_t cur = 0;
+        int sp = 0;  // warp-uniform
+        if (__ballot_sync(0xffffffffu, act)) {
+            for (;;) {
+                const NodeBox node = loadNode<64>(nodes, cur);
+                bool next = false;
+                if (node.nPrims > 0) {
+                    const NodeCone cone = loadCone(nodes, cur);
+                    for (uint32_t p = 0; p < cone.nSil; p++) {
+                        const Sil sil = Sil::load(sils, cone.silOffset + p);
+                        const uint32_t pos = cone.silOffset + p;
+                        if (act && sil.index == best.index) {
+                            // the winner again, listed in another leaf (an edge is listed for both of
+                            // its faces): not tested again, as in the reference, but its earliest
+                            // listing is what a tie compares against
+                            bestPos = min(bestPos, pos);
+                        } else if (act) {
+                            DevInteraction cI = defaultInteraction();
+                            if (sil.closestSilhouettePoint(c, r2, flipNormal, sqMinR, precision, cI) &&
+                                (bestPos == kUintMax || cI.d < best.d || (cI.d == best.d && pos < bestPos))) {
+                                r2 = fminf(r2, cI.d * cI.d);
+                                rp2 = bandRadius2(cI.d, c);
+                                best = cI;
+                                bestPos = pos;
+                            }
+                        }
+                    }
+                } else {
+                    const uint32_t li = cur + 1, ri = cur + node.offset;
+                    const NodeCone lc = loadCone(nodes, li), rc = loadCone(nodes, ri);
+                    const NodeBox lb = loadNode<64>(nodes, li), rb = loadNode<64>(nodes, ri);
+                    float dl = 0.0f, dr = 0.0f;
+                    bool hitL = act && lc.halfAngle >= 0.0f, hitR = act && rc.halfAngle >= 0.0f;
+                    if (hitL) {
+                        dl = boxSphereD2Min(lb.pMin, lb.pMax, c);
+                        hitL = dl <= rp2 && coneOverlapFast<DIM>(lc.axis, lc.halfAngle, lc.radius, c, lb.pMin, lb.pMax, dl);
+                    }
+                    if (hitR) {
+                        dr = boxSphereD2Min(rb.pMin, rb.pMax, c);
+                        hitR = dr <= rp2 && coneOverlapFast<DIM>(rc.axis, rc.halfAngle, rc.radius, c, rb.pMin, rb.pMax, dr);
+                    }
+                    const bool anyL = __ballot_sync(0xffffffffu, hitL) != 0, anyR = __ballot_sync(0xffffffffu, hitR) != 0;
+                    if (anyL || anyR) {
+                        bool takeR = !anyL;
+                        if (anyL && anyR) {
+                            // the first active lane's nearer child first (the reference's order for that lane)
+                            const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
+                            const float ldl = __shfl_sync(0xffffffffu, hitL ? dl : kFltMax, leader);
+                            const float ldr = __shfl_sync(0xffffffffu, hitR ? dr : kFltMax, leader);
+                            takeR = ldr < ldl;
+                            if (sp >= kStackDepth) {
+                                if (lane == 0) atomicOr(errorWord, kErrStackOverflow);
+                                break;
+                            }
+                            const uint32_t other = takeR ? li : ri;
+                            const float dOther = (takeR ? hitL : hitR) ? (takeR ? dl : dr) : __int_as_float(0x7fc00000);
+                            if (sp < kSilShort) {
+                                if (lane == 0) sRef[warp][sp] = other;
+                                sDist[warp][sp][lane] = dOther;  // NaN: this lane does not need it
+                            } else {
+                                lRef[sp - kSilShort] = other;
+                                lDist[sp - kSilShort] = dOther;
+                            }
+                            sp++;
+                            __syncwarp();
+                        }
+                        cur = takeR ? ri : li;
+                        act = takeR ? hitR : hitL;
+                        next = true;
+                    }
+                }
+                if (next) continue;
+                // pop until some lane needs the entry
+                while (sp > 0) {
+                    sp--;
+                    uint32_t ref;
+                    float d;
+                    if (sp < kSilShort) {
+                        ref = sRef[warp][sp];
+                        d = sDist[warp][sp][lane];
+                    } else {
+                        ref = lRef[sp - kSilShort];
+                        d = lDist[sp - kSilShort];
+                    }
+                    act = d <= rp2 && !(sqMinR >= r2);
+                    if (__ballot_sync(0xffffffffu, act)) {
+                        cur = ref;
+                        next = true;
+                        break;
+                    }
+                }
+                __syncwarp();
+                if (!next) break;
+            }
+        }
+        if (valid) out[slot] = best;
+        if (!counter) break;
     }
-    if (valid) out[slot] = best;
 }
 
 }  // namespace
 
 cudaError_t launchSilhouettePacket(const SceneView &v, const DevSphere *spheres, const uint32_t *flip,
                                    const uint32_t *perm, DevInteraction *out, uint32_t n, float sqMinR,
-                                   float precision, cudaStream_t s) {
+                                   float precision, uint32_t *counter, uint32_t grid, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    const dim3 g((n + kWideBlock - 1) / kWideBlock), b(kWideBlock);
+    const dim3 g(counter ? grid : (n + kWideBlock - 1) / kWideBlock), b(kWideBlock);
     if (v.dim == 3)
         kPacketSilhouette<EdgeSil, 3><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR, precision,
-                                                      v.errorWord);
+                                                      counter, v.errorWord);
     else
         kPacketSilhouette<VertexSil, 2><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR,
-                                                        precision, v.errorWord);
+                                                        precision, counter, v.errorWord);
     return cudaGetLastError();
 }
 
