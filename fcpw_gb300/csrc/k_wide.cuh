@@ -1045,12 +1045,11 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRay(const unsigned char *_
 
 // Rays with per-lane refill (persistent blocks, one resident wave): a lane
 // whose ray is finished takes the next one at once (one atomicAdd per warp for
-// all lanes that need a ray), so lanes stay busy however unequal the rays'
-// traversals are (most random rays leave the scene box after a few records, a
-// few cross many). Every iteration first steps the lanes at inner records
-// (child slab tests, nearest entry next, the others pushed farthest first)
-// until every active lane holds a leaf or is done, then tests the leaves and
-// pops, so each phase runs with its lanes converged. The semantics
+// all lanes that need a ray), and every iteration advances each active lane's
+// ray by one step -- one record (child slab tests, nearest entry next, the
+// others pushed farthest first) or one leaf (its primitives, then a pop) -- so
+// lanes stay busy however unequal the rays' traversals are (most random rays
+// leave the scene box after a few records, a few cross many). The semantics
 // are those of wideRay: children within the current tMax, stacked entries
 // skipped once beyond it, hits accepted when 0 <= t <= tMax (a later equal t
 // wins), an occlusion ray done at its first hit. Only the winner's leaf
@@ -1107,26 +1106,9 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRayRefill(const unsigned c
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        // the next stacked entry within tMax, or finished
-        bool finished = false;
-        auto pop = [&]() {
-            finished = true;
-            while (sp > 0) {
-                sp--;
-                if (st.dist(sp) <= r.tMax) {
-                    cur = st.ref(sp);
-                    finished = false;
-                    break;
-                }
-            }
-        };
-        // inner records first: the lanes at an inner record step until every active lane
-        // holds a leaf (or is done), then those lanes test their leaves -- each phase runs
-        // with its lanes converged (the while-while order of Aila and Laine, HPG 2009)
-        for (;;) {
-            const bool atNode = active && !finished && !(cur & kLeafBit);
-            if (!__any_sync(0xffffffffu, atNode)) break;
-            if (!atNode) continue;
+        if (!active) continue;
+        bool popNext = true, finished = false;
+        if (!(cur & kLeafBit)) {
             node.load(nodes, cur);
             tExp++;
             uint32_t key[W];
@@ -1142,25 +1124,26 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRayRefill(const unsigned c
                 nh += hit ? 1 : 0;
             }
             sortNetwork<W>(key);
-            if (nh == 0) {
-                pop();
-            } else if (sp + nh - 1 > kWideStack) {
-                atomicOr(errorWord, kErrStackOverflow);
-                finished = true;
-            } else {
-                uint32_t refs[W];
-                childRefs<W, BITS>(node, refs);
+            if (nh > 0) {
+                if (sp + nh - 1 > kWideStack) {
+                    atomicOr(errorWord, kErrStackOverflow);
+                    finished = true;
+                } else {
+                    uint32_t refs[W];
+                    childRefs<W, BITS>(node, refs);
 #pragma unroll
-                for (int k = W - 1; k >= 1; k--) {
-                    if (k < nh) {
-                        st.push(sp, selectBySlot<W>(refs, key[k] & kSlotMask), __uint_as_float(key[k] & ~kSlotMask));
-                        sp++;
+                    for (int k = W - 1; k >= 1; k--) {
+                        if (k < nh) {
+                            st.push(sp, selectBySlot<W>(refs, key[k] & kSlotMask),
+                                    __uint_as_float(key[k] & ~kSlotMask));
+                            sp++;
+                        }
                     }
+                    cur = selectBySlot<W>(refs, key[0] & kSlotMask);
+                    popNext = false;
                 }
-                cur = selectBySlot<W>(refs, key[0] & kSlotMask);
             }
-        }
-        if (active && !finished) {  // at a leaf
+        } else {
             const uint32_t off = cur & 0x07ffffffu, cnt = (cur >> 27) & 0xfu;
             tTests += cnt;
             for (uint32_t p = 0; p < cnt; p++) {
@@ -1175,9 +1158,19 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideRayRefill(const unsigned c
                     r.tMax = fminf(r.tMax, c.d);
                 }
             }
-            if (!finished) pop();
         }
-        if (active && finished) {
+        if (popNext && !finished) {
+            finished = true;
+            while (sp > 0) {
+                sp--;
+                if (st.dist(sp) <= r.tMax) {
+                    cur = st.ref(sp);
+                    finished = false;
+                    break;
+                }
+            }
+        }
+        if (finished) {
             DevInteraction best = defaultInteraction();
             if (bestSel != kUintMax) {
                 const Prim prim = Prim::load(prims, bestSel);
