@@ -792,7 +792,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                     if (act) {
                         tExp.add(1);
                         if (!found) {
-    #pragma unroll
+#pragma unroll
                             for (int k = 0; k < W; k++)
                                 if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
                             rp2 = tie.prune(r2, c);
@@ -801,13 +801,13 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                     // children needed by any lane (one OR over the warp of each lane's
                     // mask), ordered by the first active lane's distances
                     uint32_t needMask = 0;
-    #pragma unroll
+#pragma unroll
                     for (int k = 0; k < W; k++)
                         needMask |= (act && node.cnt(k) != kWideEmpty && d2Min[k] <= rp2) ? (1u << k) : 0u;
                     const uint32_t anyMask = __reduce_or_sync(0xffffffffu, needMask);
                     const uint32_t leader = __ffs(__ballot_sync(0xffffffffu, act)) - 1;
                     uint32_t key[W];
-    #pragma unroll
+#pragma unroll
                     for (int k = 0; k < W; k++) {
                         const float lead = __shfl_sync(0xffffffffu, d2Min[k], leader);
                         key[k] = ((anyMask >> k) & 1u) ? ((__float_as_uint(lead) & ~kSlotMask) | (uint32_t)k) : 0xffffffffu;
@@ -820,9 +820,9 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                             break;
                         }
                         uint32_t rawRefs[W];
-    #pragma unroll
+#pragma unroll
                         for (int s = 0; s < W; s++) rawRefs[s] = node.ref(s);
-    #pragma unroll
+#pragma unroll
                         for (int k = W - 1; k >= 0; k--) {
                             if (k < nh) {
                                 const uint32_t slot = key[k] & kSlotMask;
