@@ -594,10 +594,15 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
     out[perm ? __ldg(perm + i) : i] = best;
 }
 
-// The refinement pass's work for sorted query i: the FP32 record of the
-// winner recorded in sel[i] (closest point for uv, distance, index), the
-// runner-up's FP32 distance, then refineRecord; written to the caller's
-// slot. Without a winner, the default record.
+// The refinement pass's work for sorted query i: the winner recorded in
+// sel[i] and the runner-up, if any, each evaluated in FP32 (closest point for
+// uv, distance as the refinement's conditioning estimate) and refined
+// (Prim::refine); the runner-up's record replaces the winner's when its
+// refined distance is smaller by more than kRefineTie, the same decision as
+// refineRecord. One loop iteration per candidate keeps a single copy of the
+// FP32 and double-single code in the kernel, whose warps otherwise stalled
+// on instruction fetch. Written to the caller's slot; without a winner, the
+// default record.
 template<class Prim>
 FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphere *__restrict__ spheres,
                           const uint32_t *__restrict__ perm, const uint2 *__restrict__ sel,
@@ -607,16 +612,27 @@ FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphe
     if (s.x != kUintMax) {
         const float4 s4 = ldg4(spheres + i);
         const float3 c = make_float3(s4.x, s4.y, s4.z);
-        const Prim prim = Prim::load(prims, s.x);
-        float3 pt;
-        best.d = prim.closestPoint(c, pt, best.uv);
-        best.index = prim.index;
-        float dSecond = kFltMax;
-        if (s.y != kUintMax) {
-            float2 uv2;
-            dSecond = Prim::load(prims, s.y).closestPoint(c, pt, uv2);
+        DS dKeep = dsOf(kFltMax);
+        uint32_t kept = s.x;
+#pragma unroll 1
+        for (int k = 0; k < 2; k++) {
+            const uint32_t pos = k == 0 ? s.x : s.y;
+            if (pos == kUintMax) break;
+            const Prim prim = Prim::load(prims, pos);
+            float3 pt, p;
+            float2 uv;
+            const float d32 = prim.closestPoint(c, pt, uv);
+            const DS d = prim.refine(c, d32, p);
+            if (k == 0 || dsSub(dKeep, d).hi > kRefineTie * dKeep.hi) {
+                dKeep = d;
+                kept = pos;
+                best.p = p;
+                best.uv = uv;
+                best.index = prim.index;
+            }
         }
-        refineRecord<Prim>(prims, c, s.x, s.y, dSecond, recordNormal, best);
+        best.d = dKeep.hi;
+        if (recordNormal) best.n = Prim::load(prims, kept).normal();
     }
     out[perm ? __ldg(perm + i) : i] = best;
 }
