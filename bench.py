@@ -336,6 +336,10 @@ def algorithmic_bytes(L, g, spheres, out, n, node_bytes, prim_bytes, in_bytes, p
         nb, pb = node_bytes * n_inner, prim_bytes * n_prim
     per_query = {"nodes_popped": n_pop / n_q if node_bytes == 32 else n_inner / n_q,
                  "inner_expanded": n_inner / n_q, "prim_tests": n_prim / n_q}
+    # secondary check: about 12 FLOPs per child box test and 60 per primitive test,
+    # every expansion testing the record's W child boxes (W = 2 on the binary tree)
+    w = int(g.get_traversal()["branching"]) or 2
+    per_query["flops_per_query"] = (12 * w * n_inner + 60 * n_prim) / n_q
     if packet:
         per_query.update({"warp_record_loads": w_rec / n_q, "warp_prim_loads": w_prim / n_q})
     return {"bytes": n_q * (in_bytes + 40) + nb + pb, "per_query": per_query}
@@ -411,6 +415,15 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
             t[:, 2] = 0.0
         t[:, 3] = float(r2)
         return t
+
+    def interior_flips(g, pts):
+        """The flip flag of every query as the reference's own tests set it
+        (tests/fcpw_tests.py:588-589): 1 for points inside the boundary, from
+        the GPU contains batch (equal to Scene::contains bit for bit)."""
+        p3 = torch.zeros((len(pts), 3), dtype=torch.float32, device=dev)
+        p3[:, : pts.shape[1]] = torch.from_numpy(pts).to(dev)
+        flip = g.contains_tensor(p3).to(torch.int32)
+        return flip, flip.cpu().numpy().astype(np.uint32)
 
     def closest_point_config(name, dim, v, idx, pts, silhouettes=False):
         s = F.Scene3D() if dim == 3 else F.Scene2D()
@@ -570,60 +583,67 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
         lines.append(line)
         n = len(pts2)
         sph = sph_tensor(pts2)
-        flip = torch.zeros(n, dtype=torch.int32, device=dev)
+        g2.set_traversal(0)
+        flip, hflip = interior_flips(g2, pts2)
         out = torch.empty((n, 10), dtype=torch.float32, device=dev)
         times = sil_times(g2, sph, flip, out, n)
         nodes, _, sils = s2.cpu_bvh.export()
-        zf = np.zeros(n, np.uint32)
         refs = reference_cpu(2, v, sg, silhouettes=True)
         if refs is not None:
-            cpu = reference_rate(refs, "silhouettes", R.make_spheres(pts2, R.FLT_MAX), flip=zf,
+            cpu = reference_rate(refs, "silhouettes", R.make_spheres(pts2, R.FLT_MAX), flip=hflip,
                                  budget_s=cpu_budget / 2)
         else:
-            cpu = cpu_rate(lambda m: O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts2[:m], R.FLT_MAX), zf[:m],
-                                                       nthreads=threads), n)
+            cpu = cpu_rate(lambda m: O.silhouettes_bvh(2, nodes, sils, R.make_spheres(pts2[:m], R.FLT_MAX),
+                                                       hflip[:m], nthreads=threads), n)
         del refs
-        lines.append({"config": "2D stars 131,072 segments, 8,388,608 closest-silhouette queries (flip 0)",
+        lines.append({"config": "2D stars 131,072 segments, 8,388,608 closest-silhouette queries "
+                                f"(flip 1 inside the boundary: {int(hflip.sum()):,} queries)",
                       "queries": n, **times,
                       "roofline": _compulsory(n, 20, 40, nodes.nbytes + sils.nbytes, times["fast"]["ms"], peak),
                       "accuracy": "no FP64 silhouette oracle; parity with the reference's answers is tested",
                       "cpu_baseline": cpu})
         del g2, s2
 
-    # 3D silhouettes on the 1M-triangle torus (SNCH), 4,194,304 queries in [-2, 2]^3
+    # 3D silhouettes (SNCH) on the 1M-triangle torus, 4,194,304 queries in [-2, 2]^3, and on the
+    # 20,480-triangle icosphere with its 1,048,576 queries in [-1.5, 1.5]^3
     if want("sil3d"):
         v, f, pts = make_workload(0, args.queries)
-        s = F.Scene3D()
-        s.set_object_count(1)
-        s.set_object_vertices(v, 0)
-        s.set_object_triangles(f, 0)
-        s.compute_silhouettes()
-        s.build(F.AggregateType.Bvh_SurfaceArea, False)
-        g = F.GPUScene3D("", False, device=0)
-        g.transfer_to_gpu(s)
-        n = len(pts)
-        sph = sph_tensor(pts)
-        flip = torch.zeros(n, dtype=torch.int32, device=dev)
-        out = torch.empty((n, 10), dtype=torch.float32, device=dev)
-        times = sil_times(g, sph, flip, out, n)
-        nodes, _, sils = s.cpu_bvh.export()
-        zf = np.zeros(n, np.uint32)
-        cpu = None
-        if not args.no_cpu_baseline:
-            refs = reference_cpu(3, v, f, silhouettes=True)
-            if refs is not None:
-                cpu = reference_rate(refs, "silhouettes", R.make_spheres(pts, R.FLT_MAX), flip=zf,
-                                     budget_s=cpu_budget / 2)
-            else:
-                cpu = cpu_rate(lambda m: O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pts[:m], R.FLT_MAX), zf[:m],
-                                                           nthreads=threads), n)
-            del refs
-        lines.append({"config": f"3D silhouettes, torus 1,048,576 triangles (SNCH), {n:,} queries (flip 0)",
-                      "queries": n, **times,
-                      "roofline": _compulsory(n, 20, 40, nodes.nbytes + sils.nbytes, times["fast"]["ms"], peak),
-                      "accuracy": "no FP64 silhouette oracle; parity with the reference's answers is tested",
-                      "cpu_baseline": cpu})
-        del g, s
+        vi, fi = W.perturbed_sphere(32, W.SEED_BASE + 1)
+        pts_i = W.uniform_points(1 << 20, 3, -1.5, 1.5, W.SEED_BASE + 1001)
+        for mesh, (vv, ff, pp) in (("torus 1,048,576 triangles", (v, f, pts)),
+                                   ("icosphere 20,480 triangles", (vi, fi, pts_i))):
+            s = F.Scene3D()
+            s.set_object_count(1)
+            s.set_object_vertices(vv, 0)
+            s.set_object_triangles(ff, 0)
+            s.compute_silhouettes()
+            s.build(F.AggregateType.Bvh_SurfaceArea, False)
+            g = F.GPUScene3D("", False, device=0)
+            g.transfer_to_gpu(s)
+            n = len(pp)
+            sph = sph_tensor(pp)
+            g.set_traversal(0)
+            flip, hflip = interior_flips(g, pp)
+            out = torch.empty((n, 10), dtype=torch.float32, device=dev)
+            times = sil_times(g, sph, flip, out, n)
+            nodes, _, sils = s.cpu_bvh.export()
+            cpu = None
+            if not args.no_cpu_baseline:
+                refs = reference_cpu(3, vv, ff, silhouettes=True)
+                if refs is not None:
+                    cpu = reference_rate(refs, "silhouettes", R.make_spheres(pp, R.FLT_MAX), flip=hflip,
+                                         budget_s=cpu_budget / 2)
+                else:
+                    cpu = cpu_rate(lambda m: O.silhouettes_bvh(3, nodes, sils, R.make_spheres(pp[:m], R.FLT_MAX),
+                                                               hflip[:m], nthreads=threads), n)
+                del refs
+            lines.append({"config": f"3D silhouettes, {mesh} (SNCH), {n:,} queries "
+                                    f"(flip 1 inside the boundary: {int(hflip.sum()):,} queries)",
+                          "queries": n, **times,
+                          "roofline": _compulsory(n, 20, 40, nodes.nbytes + sils.nbytes, times["fast"]["ms"], peak),
+                          "accuracy": "no FP64 silhouette oracle; parity with the reference's answers is tested",
+                          "cpu_baseline": cpu})
+            del g, s
 
     # contains / line of sight (CPU-only in the reference) on the 1M-triangle torus
     if want("inside"):
