@@ -283,9 +283,13 @@ static obox load_node(int snch, const void *nodes, uint32_t i) {
 
 /* ------------------------------------------------------ closest point */
 /* bvh.inl:1291-1418; the sphere's r2 is shrunk in place (as the reference
-   does on its BoundingSphere&), *bestOut receives the winner; returns found */
+   does on its BoundingSphere&), *bestOut receives the winner; returns found.
+   gpuOrder: children ordered as the reference's GPU traversal orders them
+   (bvh.slang:458-470, by d2Min alone, the left child first on equal
+   distances) instead of the CPU's d2Max tie-break when both d2Min are 0; it
+   counts the visits of the GPU reference-order kernel (traversal statistics) */
 static int closest_point_bvh_core(int dim, int snch, const void *nodes, const void *prims, osphere *sp_,
-                                  int recordNormal, oint *bestOut, uint32_t *visited) {
+                                  int recordNormal, oint *bestOut, uint32_t *visited, int gpuOrder) {
     osphere s = *sp_;
     oint best = default_interaction();
     int found = 0;
@@ -333,7 +337,7 @@ static int closest_point_bvh_core(int dim, int snch, const void *nodes, const vo
                 s.r2 = minf_(s.r2, bh[3]);
                 if (hit0 && hit1) {
                     closer = li; other = ri;
-                    if (bh[0] == 0.0f && bh[2] == 0.0f) {
+                    if (!gpuOrder && bh[0] == 0.0f && bh[2] == 0.0f) {
                         if (bh[3] < bh[1]) { closer = ri; other = li; }
                     } else if (bh[2] < bh[0]) {
                         float t = bh[0]; bh[0] = bh[2]; bh[2] = t;
@@ -361,9 +365,9 @@ static int closest_point_bvh_core(int dim, int snch, const void *nodes, const vo
 }
 
 static oint closest_point_bvh_one(int dim, int snch, const void *nodes, const void *prims, osphere s,
-                                  int recordNormal, uint32_t *visited) {
+                                  int recordNormal, uint32_t *visited, int gpuOrder) {
     oint best;
-    closest_point_bvh_core(dim, snch, nodes, prims, &s, recordNormal, &best, visited);
+    closest_point_bvh_core(dim, snch, nodes, prims, &s, recordNormal, &best, visited, gpuOrder);
     return best;
 }
 
@@ -1032,7 +1036,7 @@ static void refit_rec(int dim, int snch, void *nodes, const void *prims, const v
 
 /* ------------------------------------------------------- threaded drivers */
 typedef struct {
-    int kind, dim, snch, flag;
+    int kind, dim, snch, flag, order;
     const void *nodes, *prims, *sils;
     uint32_t nPrims;
     const void *queries;
@@ -1051,7 +1055,7 @@ static void run_range(ojob *j) {
         switch (j->kind) {
             case 0: j->out[q] = closest_point_bvh_one(j->dim, j->snch, j->nodes, j->prims,
                                                      ((const osphere *)j->queries)[q], j->flag,
-                                                     j->u32out ? j->u32out + q : 0);
+                                                     j->u32out ? j->u32out + q : 0, j->order);
                 break;
             case 1: j->out[q] = closest_point_brute_one(j->dim, j->prims, j->nPrims, ((const osphere *)j->queries)[q]);
                 break;
@@ -1151,6 +1155,15 @@ int oracle_closest_points_bvh(int dim, int snch, const void *nodes, const void *
     ojob j;
     memset(&j, 0, sizeof(j));
     j.kind = 0; j.dim = dim; j.snch = snch; j.flag = recordNormal;
+    j.nodes = nodes; j.prims = prims; j.queries = spheres; j.out = (oint *)out; j.u32out = nodesVisited;
+    return run_threaded(j, n, nthreads);
+}
+/* the same with the GPU reference traversal's child order (closest_point_bvh_core) */
+int oracle_closest_points_bvh_gpu_order(int dim, int snch, const void *nodes, const void *prims, const void *spheres,
+                                        uint32_t n, void *out, uint32_t *nodesVisited, int nthreads) {
+    ojob j;
+    memset(&j, 0, sizeof(j));
+    j.kind = 0; j.dim = dim; j.snch = snch; j.order = 1;
     j.nodes = nodes; j.prims = prims; j.queries = spheres; j.out = (oint *)out; j.u32out = nodesVisited;
     return run_threaded(j, n, nthreads);
 }
@@ -1474,9 +1487,9 @@ static int inst_closest(int dim, const oinst *in, const void *const *objNodes, c
     const void *nodes = objNodes[in->object], *prims = objPrims[in->object];
     osphere sInv;
     int found;
-    if (!in->transformed) return closest_point_bvh_core(dim, 0, nodes, prims, s, recordNormal, c, NULL);
+    if (!in->transformed) return closest_point_bvh_core(dim, 0, nodes, prims, s, recordNormal, c, NULL, 0);
     sInv = xf_sphere(dim, in->ti, *s);
-    found = closest_point_bvh_core(dim, 0, nodes, prims, &sInv, recordNormal, c, NULL);
+    found = closest_point_bvh_core(dim, 0, nodes, prims, &sInv, recordNormal, c, NULL, 0);
     s->r2 = xf_sphere(dim, in->t, sInv).r2;
     if (found) xf_interaction(dim, in, s->c, c);
     return found;

@@ -25,6 +25,7 @@ def _load():
         i, u, f = C.c_int, C.c_uint32, C.c_float
         sig = {
             "oracle_closest_points_bvh": [i, i, P, P, P, u, i, P, P, i],
+            "oracle_closest_points_bvh_gpu_order": [i, i, P, P, P, u, P, P, i],
             "oracle_closest_points_brute": [i, P, u, P, u, P, i],
             "oracle_closest_points_brute_f64": [i, P, u, P, u, P, P, i],
             "oracle_intersect_rays_bvh": [i, i, P, P, P, u, i, P, P, i],
@@ -61,13 +62,24 @@ def _records():
     return R
 
 
-def closest_points_bvh(dim, nodes, prims, spheres, record_normals=False, nthreads=None, visited=False):
+def closest_points_bvh(dim, nodes, prims, spheres, record_normals=False, nthreads=None, visited=False,
+                       gpu_order=False):
+    """bvh.inl:1291-1418. With gpu_order the children are ordered as the
+    reference's GPU traversal orders them (bvh.slang:458-470, by the smaller
+    d2Min, the left child on ties), whose visit counts the GPU reference-order
+    kernel's traversal statistics must match; the answers are the same."""
     R = _records()
     snch = nodes.dtype == R.SNCH_NODE
     out = R.default_interactions(len(spheres))
     nv = np.zeros(len(spheres), np.uint32) if visited else None
-    _load().oracle_closest_points_bvh(dim, int(snch), _p(nodes), _p(prims), _p(spheres), len(spheres),
-                                      int(record_normals), _p(out), _p(nv), threads(nthreads))
+    if gpu_order:
+        if record_normals:
+            raise ValueError("gpu_order counts visits only; record_normals is not supported with it")
+        _load().oracle_closest_points_bvh_gpu_order(dim, int(snch), _p(nodes), _p(prims), _p(spheres), len(spheres),
+                                                    _p(out), _p(nv), threads(nthreads))
+    else:
+        _load().oracle_closest_points_bvh(dim, int(snch), _p(nodes), _p(prims), _p(spheres), len(spheres),
+                                          int(record_normals), _p(out), _p(nv), threads(nthreads))
     return (out, nv) if visited else out
 
 
