@@ -197,8 +197,10 @@ def reference_rate(refs, kind, queries, flip=None, budget_s: float = 6.0):
     v, n, sec = rates[best]
     from oracle import reference as REF
     width = REF.simd_width() if rates.get("vectorized") else 0
+    dim = refs[best].dim
     return {"value": v, "unit": UNIT, "cores": threads, "kind": "reference",
-            "sample": f"first {n} of {n_all} queries through the reference's Scene<{3}>::"
+            "host": {"cpu": _cpu_model(), "isa": platform.machine()},
+            "sample": f"first {n} of {n_all} queries through the reference's Scene<{dim}>::"
                       f"{'findClosestPoints' if kind == 'closest' else ('intersect' if kind == 'rays' else 'findClosestSilhouettePoints')}"
                       f" ({best}{f', FCPW_SIMD_WIDTH={width}' if best == 'vectorized' else ''}), "
                       f"its own std::thread split over {threads} hardware threads, {sec:.2f} s",
