@@ -429,6 +429,23 @@ FCPWGB_D bool beatsWinner(bool found, float d, float r2, float bestD, uint32_t s
     return found ? (d < bestD || (d == bestD && sel < selected)) : d * d <= r2;
 }
 
+// A tested primitive becomes the winner: its distance always; its point, uv
+// and index only where the traversal writes the record itself. In precise
+// mode on triangles the refinement pass recomputes the whole record from the
+// winner's leaf position, so the traversal keeps no point, uv or index (five
+// registers fewer around the traversal loop, and the FP32 uv is never formed).
+template<class Prim, bool PRECISE> constexpr bool kKeepsRecord = !(PRECISE && Prim::kRefinePass);
+template<class Prim, bool PRECISE>
+FCPWGB_D void takeWinner(DevInteraction &best, float d, float3 pt, float2 uv, uint32_t index) {
+    if constexpr (kKeepsRecord<Prim, PRECISE>) {
+        best.p = pt;
+        best.n = make_float3(0.f, 0.f, 0.f);
+        best.uv = uv;
+        best.index = index;
+    }
+    best.d = d;
+}
+
 // Closest point of one query on a wide tree (bvh.slang:395-502 semantics:
 // inclusive d2Min <= r2 pruning, r2 shrunk by child d2Max, primitives accepted
 // when d*d <= r2; exact distance ties go to the earlier leaf position, see
@@ -507,11 +524,7 @@ FCPWGB_D bool wideClosest(const unsigned char *__restrict__ nodes, const unsigne
                     if (found) tie.replaced(best.d, selected);
                     r2 = fminf(r2, d * d);
                     rp2 = tie.pruneHit(d, c);
-                    best.p = pt;
-                    best.n = make_float3(0.f, 0.f, 0.f);
-                    best.uv = uv;
-                    best.d = d;
-                    best.index = prim.index;
+                    takeWinner<Prim, TRACK>(best, d, pt, uv, prim.index);
                     selected = off + p;
                     found = true;
                 } else {
@@ -706,10 +719,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWideClosestPoint(const unsigne
                     tTests.add(1);
                     if (d * d <= r2) {
                         r2 = d * d;
-                        best.p = pt;
-                        best.uv = uv;
-                        best.d = d;
-                        best.index = prim.index;
+                        takeWinner<Prim, PRECISE>(best, d, pt, uv, prim.index);
                         selected = seed;
                         found = true;
                     }
@@ -879,11 +889,7 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                                 if (found) tie.replaced(best.d, selected);
                                 r2 = fminf(r2, d * d);
                                 rp2 = tie.pruneHit(d, c);
-                                best.p = pt;
-                                best.n = make_float3(0.f, 0.f, 0.f);
-                                best.uv = uv;
-                                best.d = d;
-                                best.index = prim.index;
+                                takeWinner<Prim, PRECISE>(best, d, pt, uv, prim.index);
                                 selected = off + p;
                                 found = true;
                             } else {
