@@ -815,15 +815,13 @@ __global__ void __launch_bounds__(kWideBlock, 8) kWidePacketClosestPoint(const u
                     tVisits.add(1);
                     float d2Min[W];
                     childD2Min<W, BITS>(node, c, d2Min);
-                    if (act) {
-                        tExp.add(1);
-                        if (!found) {
-#pragma unroll
-                            for (int k = 0; k < W; k++)
-                                if (node.cnt(k) != kWideEmpty) r2 = fminf(r2, childD2Max<W, BITS>(node, c, k));
-                            rp2 = tie.prune(r2, c);
-                        }
-                    }
+                    if (act) tExp.add(1);
+                    // no far-distance shrink of r2 before the first hit (the reference's
+                    // d2Max, which one thread per query keeps): the packet descends in its
+                    // first lane's nearest-first order anyway, lanes meet primitives within a
+                    // few records, and the W far distances per record cost more issue slots
+                    // than the pruning saved (6.69 to 6.36 ms on 4M queries, same records:
+                    // the winner does not depend on the radius a query starts from)
                     // children needed by any lane (one OR over the warp of each lane's
                     // mask), ordered by the first active lane's distances
                     uint32_t needMask = 0;
