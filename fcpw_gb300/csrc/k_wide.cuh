@@ -430,11 +430,12 @@ FCPWGB_D bool beatsWinner(bool found, float d, float r2, float bestD, uint32_t s
 }
 
 // A tested primitive becomes the winner: its distance always; its point, uv
-// and index only where the traversal writes the record itself. In precise
-// mode on triangles the refinement pass recomputes the whole record from the
-// winner's leaf position, so the traversal keeps no point, uv or index (five
-// registers fewer around the traversal loop, and the FP32 uv is never formed).
-template<class Prim, bool PRECISE> constexpr bool kKeepsRecord = !(PRECISE && Prim::kRefinePass);
+// and index only where the traversal writes the record from them. In precise
+// mode the record is formed from the winner's leaf position at the end (by
+// the refinement pass on triangles, by finishQuery on segments), so the
+// traversal keeps no point, uv or index (five registers fewer around the
+// traversal loop, and the FP32 uv is never formed inside it).
+template<class Prim, bool PRECISE> constexpr bool kKeepsRecord = !PRECISE;
 template<class Prim, bool PRECISE>
 FCPWGB_D void takeWinner(DevInteraction &best, float d, float3 pt, float2 uv, uint32_t index) {
     if constexpr (kKeepsRecord<Prim, PRECISE>) {
@@ -597,9 +598,13 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
         if constexpr (Prim::kRefinePass) {
             sel[i] = make_uint2(found ? selected : kUintMax, second ? tie.sel2nd : kUintMax);
             return;
-        } else {
-            if (found) refineRecord<Prim>(prims, c, selected, second ? tie.sel2nd : kUintMax, tie.d2nd, recordNormal,
-                                          best);
+        } else if (found) {
+            // the winner's uv and index, not kept by the traversal (takeWinner)
+            const Prim w = Prim::load(prims, selected);
+            float3 pt;
+            w.closestPoint(c, pt, best.uv);
+            best.index = w.index;
+            refineRecord<Prim>(prims, c, selected, second ? tie.sel2nd : kUintMax, tie.d2nd, recordNormal, best);
         }
     } else {
         if (found && recordNormal) best.n = Prim::load(prims, selected).normal();
