@@ -1166,11 +1166,20 @@ def run_reference(args):
     }), flush=True)
 
 
+# Arm CPU part numbers (the MIDR part field /proc/cpuinfo reports as "CPU part")
+_ARM_PARTS = {"0xd40": "Neoverse-V1", "0xd49": "Neoverse-N2", "0xd4f": "Neoverse-V2 (Grace)", "0xd0c": "Neoverse-N1",
+              "0xd8e": "Neoverse-N3", "0xd84": "Neoverse-V3"}
+
+
 def _cpu_model() -> str:
     try:
         for line in open("/proc/cpuinfo"):
-            if line.lower().startswith(("model name", "cpu part", "hardware")):
+            key = line.lower()
+            if key.startswith(("model name", "hardware")):
                 return line.split(":", 1)[1].strip()
+            if key.startswith("cpu part"):
+                part = line.split(":", 1)[1].strip().lower()
+                return _ARM_PARTS.get(part, f"Arm CPU part {part}")
     except OSError:
         pass
     return platform.processor() or "unknown"
