@@ -489,6 +489,22 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
         return lambda: check(L.fcpwgb_find_closest_silhouette_points_device(
             gs.handle, sph.data_ptr(), flip.data_ptr(), out.data_ptr(), n, 0.0, 1e-3, sp))
 
+    def sil_algorithmic(gs, sph, flip, out, n, sil_bytes):
+        """Algorithmic bytes of the sorted silhouette packets, counted by their
+        statistics mode (fcpwgb_silhouette_traversal_stats) on the same queries:
+        per query 16 B sphere, 4 B flag and 4 B sort index read, 40 B record written;
+        per warp step the current node's 32 B box part, plus two 64 B child records at
+        an inner node or the node's 32 B cone part and its silhouette records at a leaf."""
+        gs.set_traversal(4, 32, sort_queries=True)
+        st = (C.c_uint64 * 8)()
+        check(L.fcpwgb_silhouette_traversal_stats(gs.handle, sph.data_ptr(), flip.data_ptr(), out.data_ptr(), n,
+                                                  C.c_float(0.0), C.c_float(1e-3), st))
+        gs.set_traversal(0)
+        n_q, w_in, w_leaf, w_sil, t_child, t_sil = [int(x) for x in st[:6]]
+        b = n_q * (24 + 40) + w_in * (32 + 128) + w_leaf * (32 + 32) + w_sil * sil_bytes
+        return b, {"warp_inner_steps": w_in / n_q, "warp_leaf_steps": w_leaf / n_q, "warp_sil_loads": w_sil / n_q,
+                   "child_tests": t_child / n_q, "sil_tests": t_sil / n_q}
+
     def sil_times(gs, sph, flip, out, n):
         gs.set_traversal(0)
         plain = timed(sil_run(gs, sph, flip, out, n))
@@ -505,6 +521,14 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
                 "fast": {"queries_per_s": n / (fast / 1e3), "ms": fast, "variant": best},
                 "variants_ms": {k: round(v, 3) for k, v in variants.items()},
                 "speedup_vs_plain": plain / fast}
+
+    def sil_roofline(gs, sph, flip, out, n, times, scene_bytes, sil_bytes):
+        roof = _compulsory(n, 20, 40, scene_bytes, times["fast"]["ms"], peak)
+        ab, per_q = sil_algorithmic(gs, sph, flip, out, n, sil_bytes)
+        a = ab / (times["variants_ms"]["warp packets, queries sorted"] / 1e3) / 1e9
+        roof.update({"algorithmic_bytes": ab, "algorithmic_gbs": a, "algorithmic_frac": a / peak, "per_query": per_q,
+                     "time": "CUDA events around the whole call (sort, packets)"})
+        return roof
 
     # C1: 20,480-triangle perturbed icosphere, 1,048,576 queries in [-1.5, 1.5]^3
     if want("c1"):
@@ -601,7 +625,7 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
         lines.append({"config": "2D stars 131,072 segments, 8,388,608 closest-silhouette queries "
                                 f"(flip 1 inside the boundary: {int(hflip.sum()):,} queries)",
                       "queries": n, **times,
-                      "roofline": _compulsory(n, 20, 40, nodes.nbytes + sils.nbytes, times["fast"]["ms"], peak),
+                      "roofline": sil_roofline(g2, sph, flip, out, n, times, nodes.nbytes + sils.nbytes, 32),
                       "accuracy": "no FP64 silhouette oracle; parity with the reference's answers is tested",
                       "cpu_baseline": cpu})
         del g2, s2
@@ -642,7 +666,7 @@ def suite_records(args, only_arg="", cpu_budget=6.0):
             lines.append({"config": f"3D silhouettes, {mesh} (SNCH), {n:,} queries "
                                     f"(flip 1 inside the boundary: {int(hflip.sum()):,} queries)",
                           "queries": n, **times,
-                          "roofline": _compulsory(n, 20, 40, nodes.nbytes + sils.nbytes, times["fast"]["ms"], peak),
+                          "roofline": sil_roofline(g, sph, flip, out, n, times, nodes.nbytes + sils.nbytes, 56),
                           "accuracy": "no FP64 silhouette oracle; parity with the reference's answers is tested",
                           "cpu_baseline": cpu})
             del g, s

@@ -67,6 +67,7 @@ SIGNATURES = {
     "fcpwgb_intersect_spheres_device": (c_int, [P, P, P, P, c_uint32, P]),
     "fcpwgb_find_closest_silhouette_points_device": (c_int, [P, P, P, P, c_uint32, c_float, c_float, P]),
     "fcpwgb_closest_points_traversal_stats": (c_int, [P, P, P, c_uint32, P]),
+    "fcpwgb_silhouette_traversal_stats": (c_int, [P, P, P, P, c_uint32, c_float, c_float, P]),
     "fcpwgb_gpu_scene_export_nodes": (c_int, [P, P]),
     "fcpwgb_closest_point_backward_device": (c_int, [P, P, P, P, c_uint32, P, P, P]),
     "fcpwgb_ray_backward_device": (c_int, [P, P, P, P, c_uint32, P, P, P, P]),

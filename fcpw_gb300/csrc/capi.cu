@@ -742,30 +742,18 @@ extern "C" int fcpwgb_intersect_spheres_device(fcpwgb_gpu_scene *s, const fcpwgb
     return FCPWGB_OK;
 }
 
-extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
-                                                            const fcpwgb_bounding_sphere *spheres,
-                                                            const uint32_t *flip, fcpwgb_interaction *out,
-                                                            uint32_t n, float sq_min_r, float precision,
-                                                            void *stream) {
-    if (s && s->inst) {
-        int rc = s->activate();
-        if (rc) return rc;
-        if (n > 0 && (!spheres || !flip || !out))
-            return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
-        return instancedSilhouettes(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, nullptr, n, sq_min_r,
-                                    precision, s->pick(stream));
-    }
-    int rc = requireTree(s);
-    if (rc) return rc;
-    if (n > 0 && (!spheres || !flip || !out))
-        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
-    cudaStream_t st = s->pick(stream);
+namespace {
+// closest silhouette points of a transferred single tree on device arrays:
+// queries sorted spatially with a fast-path configuration, warp packets or the
+// binary kernel; with stats (zeroed, 5 words) the packets' counting variant
+int silhouettesDevice(fcpwgb_gpu_scene *s, const DevSphere *q, const uint32_t *flip, DevInteraction *out, uint32_t n,
+                      float sq_min_r, float precision, cudaStream_t st, unsigned long long *stats) {
+    int rc;
     if (!s->snch || s->nSils == 0) {
         // no silhouette data: the reference kernel leaves every result at its default
-        FCPWGB_CUDA(launchFillDefault((DevInteraction *)out, n, st));
+        FCPWGB_CUDA(launchFillDefault(out, n, st));
         return FCPWGB_OK;
     }
-    const DevSphere *q = (const DevSphere *)spheres;
     const uint32_t *perm = nullptr;
     if (s->useWide() && s->wideConfig.sortQueries && n >= 4096) {
         // with a fast-path configuration the queries are sorted spatially first, so
@@ -787,11 +775,58 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
             counter = (uint32_t *)s->workCounter.ptr;
             grid = std::min<uint32_t>((n + 127) / 128, (uint32_t)s->smCount() * 8u);
         }
-        FCPWGB_CUDA(launchSilhouettePacket(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision,
-                                           counter, grid, st));
+        FCPWGB_CUDA(launchSilhouettePacket(s->view(), q, flip, perm, out, n, sq_min_r, precision, counter, grid, st,
+                                           stats));
         return FCPWGB_OK;
     }
-    FCPWGB_CUDA(launchSilhouetteBinary(s->view(), q, flip, perm, (DevInteraction *)out, n, sq_min_r, precision, st));
+    if (stats) return setError(FCPWGB_ERR_UNSUPPORTED, "silhouette statistics count the warp packets: set a fast-path "
+                                                       "configuration and a squared minimum radius <= 0");
+    FCPWGB_CUDA(launchSilhouetteBinary(s->view(), q, flip, perm, out, n, sq_min_r, precision, st));
+    return FCPWGB_OK;
+}
+}  // namespace
+
+extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
+                                                            const fcpwgb_bounding_sphere *spheres,
+                                                            const uint32_t *flip, fcpwgb_interaction *out,
+                                                            uint32_t n, float sq_min_r, float precision,
+                                                            void *stream) {
+    if (s && s->inst) {
+        int rc = s->activate();
+        if (rc) return rc;
+        if (n > 0 && (!spheres || !flip || !out))
+            return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        return instancedSilhouettes(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, nullptr, n, sq_min_r,
+                                    precision, s->pick(stream));
+    }
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (n > 0 && (!spheres || !flip || !out))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    return silhouettesDevice(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, n, sq_min_r, precision,
+                             s->pick(stream), nullptr);
+}
+
+extern "C" int fcpwgb_silhouette_traversal_stats(fcpwgb_gpu_scene *s, const fcpwgb_bounding_sphere *spheres,
+                                                 const uint32_t *flip, fcpwgb_interaction *out, uint32_t n,
+                                                 float sq_min_r, float precision, uint64_t *stats) {
+    int rc = requireTree(s);
+    if (rc) return rc;
+    if (!stats) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL stats");
+    if (n > 0 && (!spheres || !flip || !out))
+        return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    DeviceBuffer counters;
+    if ((rc = counters.ensure(8 * sizeof(unsigned long long)))) return rc;
+    FCPWGB_CUDA(cudaMemsetAsync(counters.ptr, 0, 8 * sizeof(unsigned long long), s->stream));
+    if ((rc = silhouettesDevice(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, n, sq_min_r, precision,
+                                s->stream, (unsigned long long *)counters.ptr)))
+        return rc;
+    unsigned long long h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    FCPWGB_CUDA(cudaMemcpyAsync(h, counters.ptr, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    FCPWGB_CUDA(cudaStreamSynchronize(s->stream));
+    stats[0] = n;
+    for (int k = 0; k < 5; k++) stats[k + 1] = h[k];
+    stats[6] = stats[7] = 0;
     return FCPWGB_OK;
 }
 

@@ -35,8 +35,11 @@ constexpr int kSilShort = 32;  // warp-stack entries in shared memory; deeper on
 
 // With `counter` non-NULL the blocks are persistent (one resident wave) and
 // every warp takes its next packet of 32 sorted queries from the counter as
-// soon as its previous one is done.
-template<class Sil, int DIM>
+// soon as its previous one is done. With STATS, per-launch totals go to
+// stats[0..4]: warp steps at an inner node (two 64 B child records loaded),
+// warp steps at a leaf, silhouette records loaded by warps, and the lanes'
+// child tests and silhouette tests.
+template<class Sil, int DIM, bool STATS>
 __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigned char *__restrict__ nodes,
                                                                 const unsigned char *__restrict__ sils,
                                                                 const DevSphere *__restrict__ spheres,
@@ -44,7 +47,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
                                                                 const uint32_t *__restrict__ perm,
                                                                 DevInteraction *__restrict__ out, uint32_t n,
                                                                 float sqMinR, float precision, uint32_t *counter,
-                                                                uint32_t *errorWord) {
+                                                                uint32_t *errorWord, unsigned long long *stats) {
+    Count<STATS> wInner, wLeaf, wSil, tChild, tSil;
     constexpr int kWarps = kWideBlock / 32;
     __shared__ uint32_t sRef[kWarps][kSilShort];
     __shared__ float sDist[kWarps][kSilShort][32];
@@ -86,6 +90,9 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
                 bool next = false;
                 if (node.nPrims > 0) {
                     const NodeCone cone = loadCone(nodes, cur);
+                    wLeaf.add(1);
+                    wSil.add(cone.nSil);
+                    if (act) tSil.add(cone.nSil);
                     for (uint32_t p = 0; p < cone.nSil; p++) {
                         const Sil sil = Sil::load(sils, cone.silOffset + p);
                         const uint32_t pos = cone.silOffset + p;
@@ -107,6 +114,8 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
                     }
                 } else {
                     const uint32_t li = cur + 1, ri = cur + node.offset;
+                    wInner.add(1);
+                    if (act) tChild.add(2);
                     const NodeCone lc = loadCone(nodes, li), rc = loadCone(nodes, ri);
                     const NodeBox lb = loadNode<64>(nodes, li), rb = loadNode<64>(nodes, ri);
                     float dl = 0.0f, dr = 0.0f;
@@ -176,21 +185,41 @@ __global__ void __launch_bounds__(kWideBlock, 8) kPacketSilhouette(const unsigne
         if (valid) out[slot] = best;
         if (!counter) break;
     }
+    if (STATS && stats) {
+        const uint32_t lane = threadIdx.x & 31u;
+        if (lane == 0) {
+            atomicAdd(stats + 0, wInner.get());
+            atomicAdd(stats + 1, wLeaf.get());
+            atomicAdd(stats + 2, wSil.get());
+        }
+        atomicAdd(stats + 3, tChild.get());
+        atomicAdd(stats + 4, tSil.get());
+    }
 }
 
 }  // namespace
 
 cudaError_t launchSilhouettePacket(const SceneView &v, const DevSphere *spheres, const uint32_t *flip,
                                    const uint32_t *perm, DevInteraction *out, uint32_t n, float sqMinR,
-                                   float precision, uint32_t *counter, uint32_t grid, cudaStream_t s) {
+                                   float precision, uint32_t *counter, uint32_t grid, cudaStream_t s,
+                                   unsigned long long *stats) {
     if (n == 0) return cudaSuccess;
     const dim3 g(counter ? grid : (n + kWideBlock - 1) / kWideBlock), b(kWideBlock);
-    if (v.dim == 3)
-        kPacketSilhouette<EdgeSil, 3><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR, precision,
-                                                      counter, v.errorWord);
-    else
-        kPacketSilhouette<VertexSil, 2><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR,
-                                                        precision, counter, v.errorWord);
+    if (v.dim == 3) {
+        if (stats)
+            kPacketSilhouette<EdgeSil, 3, true><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR,
+                                                                precision, counter, v.errorWord, stats);
+        else
+            kPacketSilhouette<EdgeSil, 3, false><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR,
+                                                                 precision, counter, v.errorWord, nullptr);
+    } else {
+        if (stats)
+            kPacketSilhouette<VertexSil, 2, true><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n, sqMinR,
+                                                                  precision, counter, v.errorWord, stats);
+        else
+            kPacketSilhouette<VertexSil, 2, false><<<g, b, 0, s>>>(v.nodes, v.sils, spheres, flip, perm, out, n,
+                                                                   sqMinR, precision, counter, v.errorWord, nullptr);
+    }
     return cudaGetLastError();
 }
 

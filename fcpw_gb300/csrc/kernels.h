@@ -77,10 +77,12 @@ cudaError_t launchRefineTriangles(const unsigned char *prims, const DevSphere *s
 cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
 // closest silhouette points with warp packets on the binary SNCH tree
 // (k_sil_packet.cu): queries sorted when perm is set, flip in caller order;
-// counter non-NULL (zeroed): grid persistent blocks whose warps take packets from it
+// counter non-NULL (zeroed): grid persistent blocks whose warps take packets from it;
+// stats non-NULL (zeroed, 5 words): the counting variant (traversal statistics)
 cudaError_t launchSilhouettePacket(const SceneView &v, const DevSphere *spheres, const uint32_t *flip,
                                    const uint32_t *perm, DevInteraction *out, uint32_t n, float sqMinR,
-                                   float precision, uint32_t *counter, uint32_t grid, cudaStream_t s);
+                                   float precision, uint32_t *counter, uint32_t grid, cudaStream_t s,
+                                   unsigned long long *stats = nullptr);
 // rays on the wide trees (one thread per ray)
 struct WideRayLaunch {
     const unsigned char *nodes = nullptr;

@@ -445,6 +445,22 @@ int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *scene,
 int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                           fcpwgb_interaction *interactions, uint32_t n, uint64_t stats[8]);
 
+/* Like fcpwgb_closest_points_traversal_stats, it runs on the scene's own
+ * stream and uses the scene's scratch arrays: the caller's earlier work on the
+ * scene must have completed.
+ * Runs fcpwgb_find_closest_silhouette_points_device's warp-packet path (a
+ * fast-path configuration and squared_min_radius <= 0, else
+ * FCPWGB_ERR_UNSUPPORTED) over device arrays in counting mode and returns,
+ * synchronously: stats[0] = queries, stats[1] = warp steps at an inner node
+ * (two 64 B child records loaded), stats[2] = warp steps at a leaf,
+ * stats[3] = silhouette records loaded by warps, stats[4] = child tests and
+ * stats[5] = silhouette tests of the queries (lanes), stats[6..7] = 0. Used
+ * to compute the algorithmic bytes of a launch; results are written to
+ * interactions. */
+int fcpwgb_silhouette_traversal_stats(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
+                                      const uint32_t *flip_normal_orientation, fcpwgb_interaction *interactions,
+                                      uint32_t n, float squared_min_radius, float precision, uint64_t stats[8]);
+
 /* ----- differentiation (no counterpart in the reference; needs a tree
  * transferred with prim_vertices). Device arrays, asynchronous on stream. ----- */
 /* Backward of the unsigned closest point distance d(x) = |x - p(x, V)| from

@@ -57,3 +57,46 @@ def test_binary_kernel_counts_equal_reference_visits(name):
     d = out[:, 8].cpu().numpy()
     assert np.allclose(d, ref["d"], rtol=1e-5, atol=1e-6)
     assert g.check_errors() == 0
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_silhouette_packet_counts(dim):
+    """The silhouette packets' counting launch (fcpwgb_silhouette_traversal_stats)
+    returns the same records as the timed launch, and its counts are those of
+    warps of 32 lanes: every lane test belongs to a warp step that loaded the
+    record; it refuses a configuration that does not run the packets."""
+    import torch
+    from fcpw_gb300._lib import FcpwError
+    if dim == 2:
+        v, idx = W.star_polylines(64, 128, W.SEED_BASE + 3)
+        pts = W.uniform_points(60_000, 2, -3, 3, 84)
+    else:
+        v, idx = W.torus(64, 32, W.SEED_BASE + 2)
+        pts = W.uniform_points(40_000, 3, -2, 2, 85)
+    s = build_scene(dim, v, idx, silhouettes=True)
+    g = F.GPUScene3D() if dim == 3 else F.GPUScene2D()
+    g.transfer_to_gpu(s)
+    n = len(pts)
+    sph = torch.from_numpy(R.make_spheres(pts, R.FLT_MAX).view(np.float32).reshape(n, 4).copy()).cuda()
+    flip = torch.from_numpy((W.rng(86).uniform(0, 1, n) < 0.5).astype(np.uint32)).cuda()
+    a = torch.empty((n, 10), dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    g.set_traversal(4, 32)
+    check(lib().fcpwgb_find_closest_silhouette_points_device(g.handle, sph.data_ptr(), flip.data_ptr(), a.data_ptr(), n,
+                                                             C.c_float(0.0), C.c_float(1e-3), None))
+    # the counting call runs on the scene's own stream and shares its scratch arrays
+    # with the call above: that one must have finished (one stream per scene at a time)
+    torch.cuda.synchronize()
+    stats = (C.c_uint64 * 8)()
+    check(lib().fcpwgb_silhouette_traversal_stats(g.handle, sph.data_ptr(), flip.data_ptr(), b.data_ptr(), n,
+                                                  C.c_float(0.0), C.c_float(1e-3), stats))
+    torch.cuda.synchronize()
+    assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    n_q, w_in, w_leaf, w_sil, t_child, t_sil = [int(x) for x in stats[:6]]
+    assert n_q == n and w_in > 0 and w_leaf > 0 and w_sil > 0
+    assert 0 < t_child <= 2 * 32 * w_in and 0 < t_sil <= 32 * w_sil
+    g.set_traversal(0)
+    with pytest.raises(FcpwError):
+        check(lib().fcpwgb_silhouette_traversal_stats(g.handle, sph.data_ptr(), flip.data_ptr(), b.data_ptr(), n,
+                                                      C.c_float(0.0), C.c_float(1e-3), stats))
+    assert g.check_errors() == 0
