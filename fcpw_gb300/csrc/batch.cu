@@ -5,7 +5,7 @@
 // references and leaf offsets rebased, so every record addresses the forest
 // directly) and the primitives into one array. The queries arrive grouped by
 // scene (offsets[s] .. offsets[s+1]); one counting sort orders them by
-// (scene, Morton cell of that scene's own grid) and records each query's
+// (scene, Hilbert index of the cell in that scene's own grid) and records each query's
 // root, and the wide kernel -- persistent blocks taking neighbouring queries
 // from a work counter -- starts every query at its scene's root. The
 // sequence (clears, sort, traversal) is captured once in a CUDA graph and

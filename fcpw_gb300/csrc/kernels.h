@@ -136,7 +136,7 @@ cudaError_t launchPackTri48(const DevTriangle *tris, uint32_t n, float4 *out, cu
 struct BatchSceneGrid {
     float3 lo, inv;     // grid origin and cells per unit length (2^bits / extent)
     uint32_t cellBase;  // first cell of the scene in the concatenated cell array
-    uint32_t bits;      // cells per axis = 2^bits (<= 6 in 3D, <= 9 in 2D)
+    uint32_t bits;      // cells per axis = 2^bits (<= 8 in 3D, <= 12 in 2D)
     uint32_t root;      // wide record of the scene's root in the forest
     uint32_t pad;
 };
