@@ -4,9 +4,9 @@
 // (512^2 in 2D) and counting-sorted (histogram, exclusive scan, scatter). On 4M queries the 3D grid at 128^3
 // made the closest-point packets 1.3 % faster than at 64^3; in 2D 1024^2 was 4 % slower than 512^2 on 8M
 // queries. Hilbert order keeps every run of consecutive cells face-connected, where Morton (Z) order jumps
-// between blocks: a packet of 32 sorted queries then spans a more compact region wherever the queries are
-// sparse (1M queries on the icosphere, half a query per cell: 0.785 against 0.930 ms, 10 % fewer triangle
-// loads per packet), and the same at 2 queries per cell (4M queries on the torus).
+// between blocks: a packet of 32 sorted queries then spans a more compact region (4M queries on the torus,
+// 2 queries per cell: 6.01 against 6.39 ms per call; 1M queries on the icosphere, half a query per cell:
+// 0.785 against 0.930 ms, 10 % fewer triangle loads per packet).
 // The grid spans the bounding box of the batch's own query centres, clipped
 // to limits around the scene, so that cells are neither empty nor crowded
 // whatever the query distribution. Threads of a warp then traverse
