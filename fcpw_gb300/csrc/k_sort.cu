@@ -233,7 +233,8 @@ __global__ void kCellHistogram(SortLimits lim, const int *qb, const Rec *__restr
 
 template<class Rec>
 __global__ void kScatterQueries(SortLimits lim, const int *qb, const Rec *__restrict__ q, uint32_t n,
-                                uint32_t *cells, uint32_t nCells, Rec *sorted, uint32_t *perm, bool skipInOrder) {
+                                uint32_t *cells, uint32_t nCells, Rec *sorted, uint32_t *perm, uint32_t *inv,
+                                bool skipInOrder) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const bool inOrder = keepOrder(qb, n);
@@ -242,6 +243,7 @@ __global__ void kScatterQueries(SortLimits lim, const int *qb, const Rec *__rest
     uint32_t pos = atomicAdd(cells + recordCell(lim.dim, g, q, i, inOrder, nCells), 1u);
     copyRecord(q, i, sorted, pos);
     perm[pos] = i;
+    if (inv) inv[i] = pos;
 }
 
 cudaError_t scanCounts(uint32_t *cells, uint32_t nCells, uint32_t *tileSums, cudaStream_t s);
@@ -265,7 +267,7 @@ __global__ void kRayCoherence(const DevRay *__restrict__ q, uint32_t n, int *qb)
 
 template<class Rec>
 cudaError_t sortRecords(const SortLimits &lim, const Rec *recs, uint32_t n, uint32_t *cells, Rec *sorted,
-                        uint32_t *perm, int numSMs, cudaStream_t s, bool skipInOrder = false) {
+                        uint32_t *perm, int numSMs, cudaStream_t s, bool skipInOrder = false, uint32_t *inv = nullptr) {
     if (n == 0) return cudaSuccess;
     int *qb = reinterpret_cast<int *>(cells + kSortCells);
     const uint32_t nCells = lim.dim == 3 ? 1u << 21 : 1u << 18;  // the cells cellOf can return
@@ -282,13 +284,13 @@ cudaError_t sortRecords(const SortLimits &lim, const Rec *recs, uint32_t n, uint
                                                                                                      qb);
     kCellHistogram<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, nCells, skipInOrder);
     if ((e = scanCounts(cells, nCells, cells + kSortCells + 8, s)) != cudaSuccess) return e;
-    kScatterQueries<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, nCells, sorted, perm, skipInOrder);
+    kScatterQueries<Rec><<<blocks, 256, 0, s>>>(lim, qb, recs, n, cells, nCells, sorted, perm, inv, skipInOrder);
     return cudaGetLastError();
 }
 
 cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, uint32_t n, uint32_t *cells,
-                              DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s) {
-    return sortRecords(lim, spheres, n, cells, sorted, perm, numSMs, s);
+                              DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s, uint32_t *inv) {
+    return sortRecords(lim, spheres, n, cells, sorted, perm, numSMs, s, false, inv);
 }
 
 cudaError_t launchSortRays(const SortLimits &lim, const DevRay *rays, uint32_t n, uint32_t *cells, DevRay *sorted,

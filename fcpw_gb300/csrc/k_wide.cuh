@@ -612,15 +612,45 @@ FCPWGB_D void finishQuery(const unsigned char *__restrict__ prims, const uint32_
     out[perm ? __ldg(perm + i) : i] = best;
 }
 
-// The refinement pass's work for sorted query i: the winner recorded in
-// sel[i] and the runner-up, if any, each evaluated in FP32 (closest point for
-// uv, distance as the refinement's conditioning estimate) and refined
-// (Prim::refine); the runner-up's record replaces the winner's when its
-// refined distance is smaller by more than kRefineTie, the same decision as
-// refineRecord. One loop iteration per candidate keeps a single copy of the
-// FP32 and double-single code in the kernel, whose warps otherwise stalled
-// on instruction fetch. Written to the caller's slot; without a winner, the
-// default record.
+// The precise record of a query at c from its winner (leaf position
+// `first`) and runner-up within the band (`second`, kUintMax: none), each
+// evaluated in FP32 (closest point for uv, distance as the refinement's
+// conditioning estimate) and refined (Prim::refine); the runner-up's record
+// replaces the winner's when its refined distance is smaller by more than
+// kRefineTie, the same decision as refineRecord. One loop iteration per
+// candidate keeps a single copy of the FP32 and double-single code in the
+// kernel, whose warps otherwise stalled on instruction fetch.
+template<class Prim>
+FCPWGB_D DevInteraction refineCandidates(const unsigned char *__restrict__ prims, float3 c, uint32_t first,
+                                         uint32_t second, int recordNormal) {
+    DevInteraction best = defaultInteraction();
+    DS dKeep = dsOf(kFltMax);
+    uint32_t kept = first;
+#pragma unroll 1
+    for (int k = 0; k < 2; k++) {
+        const uint32_t pos = k == 0 ? first : second;
+        if (pos == kUintMax) break;
+        const Prim prim = Prim::load(prims, pos);
+        float3 pt, p;
+        float2 uv;
+        const float d32 = prim.closestPoint(c, pt, uv);
+        const DS d = prim.refine(c, d32, p);
+        if (k == 0 || dsSub(dKeep, d).hi > kRefineTie * dKeep.hi) {
+            dKeep = d;
+            kept = pos;
+            best.p = p;
+            best.uv = uv;
+            best.index = prim.index;
+        }
+    }
+    best.d = dKeep.hi;
+    if (recordNormal) best.n = Prim::load(prims, kept).normal();
+    return best;
+}
+
+// The refinement pass's work for sorted query i: refineCandidates on the
+// leaf positions in sel[i], written to the caller's slot; without a winner,
+// the default record.
 template<class Prim>
 FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphere *__restrict__ spheres,
                           const uint32_t *__restrict__ perm, const uint2 *__restrict__ sel,
@@ -629,28 +659,7 @@ FCPWGB_D void refineQuery(const unsigned char *__restrict__ prims, const DevSphe
     DevInteraction best = defaultInteraction();
     if (s.x != kUintMax) {
         const float4 s4 = ldg4(spheres + i);
-        const float3 c = make_float3(s4.x, s4.y, s4.z);
-        DS dKeep = dsOf(kFltMax);
-        uint32_t kept = s.x;
-#pragma unroll 1
-        for (int k = 0; k < 2; k++) {
-            const uint32_t pos = k == 0 ? s.x : s.y;
-            if (pos == kUintMax) break;
-            const Prim prim = Prim::load(prims, pos);
-            float3 pt, p;
-            float2 uv;
-            const float d32 = prim.closestPoint(c, pt, uv);
-            const DS d = prim.refine(c, d32, p);
-            if (k == 0 || dsSub(dKeep, d).hi > kRefineTie * dKeep.hi) {
-                dKeep = d;
-                kept = pos;
-                best.p = p;
-                best.uv = uv;
-                best.index = prim.index;
-            }
-        }
-        best.d = dKeep.hi;
-        if (recordNormal) best.n = Prim::load(prims, kept).normal();
+        best = refineCandidates<Prim>(prims, make_float3(s4.x, s4.y, s4.z), s.x, s.y, recordNormal);
     }
     out[perm ? __ldg(perm + i) : i] = best;
 }
@@ -1454,7 +1463,7 @@ cudaError_t launchWideClosestPrim(bool precise, const WideLaunch &l, cudaStream_
         if (Prim::kRefinePass && !l.sel) return cudaErrorInvalidValue;
         cudaError_t e = l.stats ? launchWideClosestKernel<W, B, Prim, true, true>(l, s)
                                 : launchWideClosestKernel<W, B, Prim, true, false>(l, s);
-        if (e != cudaSuccess || !Prim::kRefinePass) return e;
+        if (e != cudaSuccess || !Prim::kRefinePass || l.deferRefine) return e;
         return launchRefineTriangles(l.prims, l.spheres, l.perm, l.sel, l.out, l.n, l.recordNormal, s);
     }
     return l.stats ? launchWideClosestKernel<W, B, Prim, false, true>(l, s)

@@ -66,6 +66,7 @@ struct WideLaunch {
     uint32_t *errorWord = nullptr;
     unsigned long long *stats = nullptr;   // traversal statistics, or NULL
     uint32_t grid = 0;
+    bool deferRefine = false;              // precise mode on triangles: leave the refinement pass to the caller
 };
 template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
 // precise mode's second pass on triangles (48 B records): one thread per
@@ -73,6 +74,12 @@ template<int W> cudaError_t launchWideClosestT(int bits, int dim, bool precise, 
 // record to out[perm[i]] (out[i])
 cudaError_t launchRefineTriangles(const unsigned char *prims, const DevSphere *spheres, const uint32_t *perm,
                                   const uint2 *sel, DevInteraction *out, uint32_t n, int recordNormal, cudaStream_t s);
+// the same pass in the caller's order: thread i refines caller query i
+// (spheres in the caller's order) from sel[inv[i]] and writes out[i], so that
+// consecutive threads write consecutive records (out may be mapped host memory)
+cudaError_t launchRefineTrianglesInOrder(const unsigned char *prims, const DevSphere *spheres, const uint32_t *inv,
+                                         const uint2 *sel, DevInteraction *out, uint32_t n, int recordNormal,
+                                         cudaStream_t s);
 // dispatch over W = 2, 4, 8
 cudaError_t launchWide(int W, int bits, int dim, bool precise, const WideLaunch &l, cudaStream_t s);
 // closest silhouette points with warp packets on the binary SNCH tree
@@ -113,8 +120,9 @@ constexpr uint32_t kSortCells = 1u << kSortCellBits;
 struct SortLimits { float3 lo; float3 hi; int dim; };
 // cells: scratch of kSortScratchWords words (counters, query bounds, scan tile sums)
 constexpr uint32_t kSortScratchWords = kSortCells + 8 + kSortCells / 4096;
+// inv non-NULL: also the inverse permutation, inv[caller index] = sorted position
 cudaError_t launchSortQueries(const SortLimits &lim, const DevSphere *spheres, uint32_t n, uint32_t *cells,
-                              DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s);
+                              DevSphere *sorted, uint32_t *perm, int numSMs, cudaStream_t s, uint32_t *inv = nullptr);
 // the same for rays: by direction octant, then origin; rays that are already
 // coherent keep the caller's order (keepOrder on cells + kSortCells), and with
 // skipInOrder then nothing is written to sorted / perm (the caller reads its

@@ -83,7 +83,7 @@ int GpuScene::smCount() {
 }
 
 int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal,
-                          unsigned long long *stats, cudaStream_t st) {
+                          unsigned long long *stats, cudaStream_t st, uint32_t *inv) {
     int rc = ensureWide(st);
     if (rc) return rc;
     if (n == 0) return 0;
@@ -103,10 +103,11 @@ int GpuScene::wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_
         if ((rc = sortPerm.ensure((size_t)n * sizeof(uint32_t)))) return rc;
         if ((rc = sortSpheres.ensure((size_t)n * sizeof(DevSphere)))) return rc;
         if ((e = launchSortQueries(sortLimits(), spheres, n, (uint32_t *)sortCells.ptr, (DevSphere *)sortSpheres.ptr,
-                                   (uint32_t *)sortPerm.ptr, numSMs, st)) != cudaSuccess)
+                                   (uint32_t *)sortPerm.ptr, numSMs, st, inv)) != cudaSuccess)
             return cudaFail(e, "sort queries");
         l.spheres = (const DevSphere *)sortSpheres.ptr;
         l.perm = (const uint32_t *)sortPerm.ptr;
+        l.deferRefine = inv != nullptr;
     }
     if (c.precise && dim == 3) {
         if ((rc = refineSel.ensure((size_t)n * sizeof(uint2)))) return rc;
@@ -227,6 +228,17 @@ int GpuScene::rays(const DevRay *r, DevInteraction *out, uint32_t n, int occl, c
     return e == cudaSuccess ? 0 : cudaFail(e, "ray launch");
 }
 
+// The device address of a caller's page-locked host array (cudaHostAlloc, or
+// registered mapped), NULL for pageable memory.
+static void *mappedHostPointer(void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // pageable memory on older runtimes: not an error of ours
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int GpuScene::closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_interaction *out, uint32_t n,
                                 int recordNormal) {
     size_t ib = (size_t)n * sizeof(DevSphere), ob = (size_t)n * sizeof(DevInteraction);
@@ -235,11 +247,30 @@ int GpuScene::closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_in
     if ((rc = qOut.ensure(ob))) return rc;
     cudaError_t e = cudaMemcpyAsync(qIn0.ptr, spheres, ib, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return cudaFail(e, "cudaMemcpyAsync");
-    if ((rc = closestPoints((const DevSphere *)qIn0.ptr, (DevInteraction *)qOut.ptr, n, recordNormal, stream)))
-        return rc;
+    // Precise mode on triangles with sorted queries, into a page-locked array:
+    // the refinement pass runs in the caller's order and writes each record
+    // straight into the caller's array over the host link, coalesced, instead
+    // of a device buffer copied back afterwards (the copy would follow the pass;
+    // this way the pass's work hides under the transfer). The same records.
+    DevInteraction *direct = nullptr;
+    if (useWide() && wideConfig.precise && dim == 3 && wideConfig.sortQueries && n >= 4096 && !inst)
+        direct = (DevInteraction *)mappedHostPointer(out);
+    if (direct) {
+        if ((rc = sortInv.ensure((size_t)n * sizeof(uint32_t)))) return rc;
+        if ((rc = wideClosest((const DevSphere *)qIn0.ptr, (DevInteraction *)qOut.ptr, n, recordNormal, nullptr, stream,
+                              (uint32_t *)sortInv.ptr)))
+            return rc;
+        if ((e = launchRefineTrianglesInOrder((const unsigned char *)widePrims.ptr, (const DevSphere *)qIn0.ptr,
+                                              (const uint32_t *)sortInv.ptr, (const uint2 *)refineSel.ptr, direct, n,
+                                              recordNormal, stream)) != cudaSuccess)
+            return cudaFail(e, "refinement in the caller's order");
+    } else {
+        if ((rc = closestPoints((const DevSphere *)qIn0.ptr, (DevInteraction *)qOut.ptr, n, recordNormal, stream)))
+            return rc;
+        e = cudaMemcpyAsync(out, qOut.ptr, ob, cudaMemcpyDeviceToHost, stream);
+        if (e != cudaSuccess) return cudaFail(e, "cudaMemcpyAsync");
+    }
     uint32_t err[4] = {0, 0, 0, 0};
-    e = cudaMemcpyAsync(out, qOut.ptr, ob, cudaMemcpyDeviceToHost, stream);
-    if (e != cudaSuccess) return cudaFail(e, "cudaMemcpyAsync");
     e = cudaMemcpyAsync(err, errorWord.ptr, sizeof(err), cudaMemcpyDeviceToHost, stream);
     if (e != cudaSuccess) return cudaFail(e, "cudaMemcpyAsync");
     e = cudaStreamSynchronize(stream);

@@ -82,7 +82,7 @@ struct GpuScene {
     DeviceBuffer wideNodes, wideChildBinary, widePrims;
     // scratch of the fast path: query sort cells / permutation / sorted copy, work counter,
     // precise mode's winner and runner-up leaf positions
-    DeviceBuffer sortCells, sortPerm, sortSpheres, sortRays, workCounter, refineSel, packedPoints;
+    DeviceBuffer sortCells, sortPerm, sortInv, sortSpheres, sortRays, workCounter, refineSel, packedPoints;
     int numSMs = 0;
 
     // optional event timing of traversal launches
@@ -141,8 +141,11 @@ struct GpuScene {
     int wideRays(const DevRay *rays, DevInteraction *out, uint32_t n, int occl, cudaStream_t st);
     SortLimits sortLimits() const;
     int smCount();  // multiprocessors of the scene's device (queried once)
+    // inv non-NULL (n words), with the queries sorted: the sort also writes the
+    // inverse permutation there and precise mode on triangles stops after the
+    // traversal, leaving sel for the caller's refinement pass
     int wideClosest(const DevSphere *spheres, DevInteraction *out, uint32_t n, int recordNormal,
-                    unsigned long long *stats, cudaStream_t st);
+                    unsigned long long *stats, cudaStream_t st, uint32_t *inv = nullptr);
 };
 
 }  // namespace fcpwgb
