@@ -463,6 +463,8 @@ extern "C" int fcpwgb_gpu_batch_find_closest_points_device(fcpwgb_gpu_batch *b, 
                                                            fcpwgb_interaction *interactions, int record_normals,
                                                            void *stream) {
     if (!b) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL batch");
+    int rc;
+    if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(interactions, 8, "interaction"))) return rc;
     return runDevice(b, (const DevSphere *)spheres, query_offsets, n_offsets, (DevInteraction *)interactions,
                      record_normals, (cudaStream_t)stream);
 }

@@ -25,6 +25,12 @@ using namespace fcpwgb;
 static thread_local std::string g_lastError;
 
 namespace fcpwgb {
+int checkAligned(const void *p, size_t bytes, const char *what) {
+    if (((uintptr_t)p & (uintptr_t)(bytes - 1)) == 0) return FCPWGB_OK;
+    return setError(FCPWGB_ERR_INVALID_ARGUMENT,
+                    std::string(what) + " array must start on a " + std::to_string(bytes) + " B boundary");
+}
+
 int setError(int code, const std::string &msg) {
     g_lastError = msg;
     return code;
@@ -699,12 +705,14 @@ extern "C" int fcpwgb_find_closest_points_device(fcpwgb_gpu_scene *s, const fcpw
         int rc = s->activate();
         if (rc) return rc;
         if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction"))) return rc;
         return instancedClosest(s, (const DevSphere *)spheres, (DevInteraction *)out, nullptr, n, record_normals,
                                 s->pick(stream));
     }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction"))) return rc;
     return s->closestPoints((const DevSphere *)spheres, (DevInteraction *)out, n, record_normals, s->pick(stream));
 }
 
@@ -714,11 +722,13 @@ extern "C" int fcpwgb_intersect_rays_device(fcpwgb_gpu_scene *s, const fcpwgb_ra
         int rc = s->activate();
         if (rc) return rc;
         if (n > 0 && (!rays || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        if ((rc = checkAligned(rays, 8, "ray")) || (rc = checkAligned(out, 8, "interaction"))) return rc;
         return instancedRays(s, (const DevRay *)rays, (DevInteraction *)out, nullptr, n, occl, s->pick(stream));
     }
     int rc = requireTree(s);
     if (rc) return rc;
     if (n > 0 && (!rays || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    if ((rc = checkAligned(rays, 8, "ray")) || (rc = checkAligned(out, 8, "interaction"))) return rc;
     return s->rays((const DevRay *)rays, (DevInteraction *)out, n, occl, s->pick(stream));
 }
 
@@ -730,6 +740,9 @@ extern "C" int fcpwgb_intersect_spheres_device(fcpwgb_gpu_scene *s, const fcpwgb
         if (rc) return rc;
         if (n > 0 && (!spheres || !rand_nums || !out))
             return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction")) ||
+            (rc = checkAligned(rand_nums, 4, "random number")))
+            return rc;
         return instancedSample(s, (const DevSphere *)spheres, (const float3 *)rand_nums, (DevInteraction *)out,
                                nullptr, n, s->pick(stream));
     }
@@ -737,6 +750,9 @@ extern "C" int fcpwgb_intersect_spheres_device(fcpwgb_gpu_scene *s, const fcpwgb
     if (rc) return rc;
     if (n > 0 && (!spheres || !rand_nums || !out))
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction")) ||
+        (rc = checkAligned(rand_nums, 4, "random number")))
+        return rc;
     FCPWGB_CUDA(launchSphereSampleBinary(s->view(), (const DevSphere *)spheres, (const float3 *)rand_nums,
                                          (DevInteraction *)out, n, s->pick(stream)));
     return FCPWGB_OK;
@@ -796,6 +812,9 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
         if (rc) return rc;
         if (n > 0 && (!spheres || !flip || !out))
             return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+        if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction")) ||
+            (rc = checkAligned(flip, 4, "flip")))
+            return rc;
         return instancedSilhouettes(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, nullptr, n, sq_min_r,
                                     precision, s->pick(stream));
     }
@@ -803,6 +822,9 @@ extern "C" int fcpwgb_find_closest_silhouette_points_device(fcpwgb_gpu_scene *s,
     if (rc) return rc;
     if (n > 0 && (!spheres || !flip || !out))
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction")) ||
+        (rc = checkAligned(flip, 4, "flip")))
+        return rc;
     return silhouettesDevice(s, (const DevSphere *)spheres, flip, (DevInteraction *)out, n, sq_min_r, precision,
                              s->pick(stream), nullptr);
 }
@@ -815,6 +837,9 @@ extern "C" int fcpwgb_silhouette_traversal_stats(fcpwgb_gpu_scene *s, const fcpw
     if (!stats) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL stats");
     if (n > 0 && (!spheres || !flip || !out))
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction")) ||
+        (rc = checkAligned(flip, 4, "flip")))
+        return rc;
     DeviceBuffer counters;
     if ((rc = counters.ensure(8 * sizeof(unsigned long long)))) return rc;
     FCPWGB_CUDA(cudaMemsetAsync(counters.ptr, 0, 8 * sizeof(unsigned long long), s->stream));
@@ -944,6 +969,7 @@ extern "C" int fcpwgb_closest_points_traversal_stats(fcpwgb_gpu_scene *s, const 
     if (rc) return rc;
     if (!stats) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL stats");
     if (n > 0 && (!spheres || !out)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL query or output array");
+    if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(out, 8, "interaction"))) return rc;
     DeviceBuffer counters;
     if ((rc = counters.ensure(8 * sizeof(unsigned long long)))) return rc;
     FCPWGB_CUDA(cudaMemsetAsync(counters.ptr, 0, 8 * sizeof(unsigned long long), s->stream));
@@ -1029,6 +1055,7 @@ extern "C" int fcpwgb_closest_point_backward_device(fcpwgb_gpu_scene *s, const f
     if (rc) return rc;
     if ((n > 0 && (!spheres || !forward || !grad_d || !grad_x)) || !grad_vertices)
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL array");
+    if ((rc = checkAligned(spheres, 16, "sphere")) || (rc = checkAligned(forward, 8, "interaction"))) return rc;
     GradView gv;
     if ((rc = gradView(s, gv))) return rc;
     FCPWGB_CUDA(launchDistanceBackward(gv, (const DevSphere *)spheres, (const DevInteraction *)forward, grad_d, n,
@@ -1043,6 +1070,7 @@ extern "C" int fcpwgb_ray_backward_device(fcpwgb_gpu_scene *s, const fcpwgb_ray 
     if (rc) return rc;
     if ((n > 0 && (!rays || !forward || !grad_t || !grad_o || !grad_dir)) || !grad_vertices)
         return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL array");
+    if ((rc = checkAligned(rays, 8, "ray")) || (rc = checkAligned(forward, 8, "interaction"))) return rc;
     GradView gv;
     if ((rc = gradView(s, gv))) return rc;
     FCPWGB_CUDA(launchRayBackward(gv, (const DevRay *)rays, (const DevInteraction *)forward, grad_t, n, grad_o,
@@ -1133,6 +1161,7 @@ extern "C" int fcpwgb_closest_distances_f64_device(fcpwgb_gpu_scene *s, const fc
     if (rc) return rc;
     if (n > (1u << 24)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "at most 2^24 queries per brute-force call");
     if (n && (!spheres || !distances)) return setError(FCPWGB_ERR_INVALID_ARGUMENT, "NULL array");
+    if ((rc = checkAligned(spheres, 16, "sphere"))) return rc;
     FCPWGB_CUDA(launchBruteF64(s->dim, (const unsigned char *)s->prims.ptr, s->nPrims, (const DevSphere *)spheres, n,
                                distances, s->pick(stream)));
     return FCPWGB_OK;

@@ -255,6 +255,7 @@ int GpuScene::closestPointsHost(const fcpwgb_bounding_sphere *spheres, fcpwgb_in
     DevInteraction *direct = nullptr;
     if (useWide() && wideConfig.precise && dim == 3 && wideConfig.sortQueries && n >= 4096 && !inst)
         direct = (DevInteraction *)mappedHostPointer(out);
+    if (((uintptr_t)direct & 15u) != 0) direct = nullptr;  // the pass stores 16 B vectors from the array's start
     if (direct) {
         if ((rc = sortInv.ensure((size_t)n * sizeof(uint32_t)))) return rc;
         if ((rc = wideClosest((const DevSphere *)qIn0.ptr, (DevInteraction *)qOut.ptr, n, recordNormal, nullptr, stream,

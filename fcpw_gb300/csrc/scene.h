@@ -17,6 +17,12 @@ namespace fcpwgb {
 
 int setError(int code, const std::string &msg);
 int cudaFail(cudaError_t e, const char *where);
+// Device arrays of queries and records must start on the boundaries the
+// kernels read them on: a sphere is one 16 B vector, rays and interaction
+// records are read and written in 8 B parts (cudaMalloc and torch
+// allocations, and every element of them, satisfy this). Returns
+// FCPWGB_ERR_INVALID_ARGUMENT otherwise, before anything is launched.
+int checkAligned(const void *p, size_t bytes, const char *what);
 // consumes one injected allocation failure (fcpwgb_debug_fail_allocations)
 bool injectedAllocFailure();
 

@@ -399,7 +399,10 @@ int fcpwgb_gpu_scene_set_traversal(fcpwgb_gpu_scene *scene, const fcpwgb_travers
 int fcpwgb_gpu_scene_get_traversal(const fcpwgb_gpu_scene *scene, fcpwgb_traversal_config *config);
 
 /* ----- queries with HOST arrays (synchronous, as the reference) ----- */
-/* findClosestPoints, fcpw_gpu.h:60-62 */
+/* findClosestPoints, fcpw_gpu.h:60-62. In precise mode on triangles with a
+ * fast-path configuration (sorted queries, n >= 4096) and a page-locked
+ * interactions array starting on a 16 B boundary, the records are written
+ * into that array by the device directly; otherwise they are copied back. */
 int fcpwgb_find_closest_points(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                fcpwgb_interaction *interactions, uint32_t n, int record_normals);
 /* intersect(rays), fcpw_gpu.h:38-40 */
@@ -417,7 +420,10 @@ int fcpwgb_find_closest_silhouette_points(fcpwgb_gpu_scene *scene,
                                           float squared_min_radius, float precision);
 
 /* ----- queries with DEVICE arrays: asynchronous on stream (a cudaStream_t, used as
- * given; NULL is the CUDA default stream, as for any CUDA runtime call) ----- */
+ * given; NULL is the CUDA default stream, as for any CUDA runtime call).
+ * Sphere arrays must start on a 16 B boundary, ray and interaction arrays on
+ * an 8 B boundary, flag arrays on 4 B (cudaMalloc'd arrays and every element
+ * of them do); otherwise FCPWGB_ERR_INVALID_ARGUMENT, before any launch. ----- */
 int fcpwgb_find_closest_points_device(fcpwgb_gpu_scene *scene, const fcpwgb_bounding_sphere *spheres,
                                       fcpwgb_interaction *interactions, uint32_t n,
                                       int record_normals, void *stream);

@@ -50,3 +50,39 @@ def test_host_array_records_equal_device_records(cfg, record_normals):
     assert np.array_equal(pinned.numpy().view(np.uint32), want.view(np.uint32))
     assert np.array_equal(pageable.view(np.uint32), want.view(np.uint32))
     assert g.check_errors() == 0
+
+
+def test_misaligned_arrays():
+    """Device arrays off the boundary the kernels read them on are refused
+    before anything is launched (the scene stays usable); a page-locked
+    output array off a 16 B boundary takes the copy path and gets the same
+    records."""
+    import torch
+    from fcpw_gb300._lib import FcpwError
+    v, f = W.torus(64, 32, W.SEED_BASE + 2)
+    s = build_scene(3, v, f)
+    g = F.GPUScene3D()
+    g.transfer_to_gpu(s)
+    g.set_traversal(4, 32, packet=True, persistent=True)
+    n = 20_000
+    sph = R.make_spheres(W.uniform_points(n, 3, -2.0, 2.0, 90), R.FLT_MAX)
+    flat = sph.view(np.float32).reshape(n, 4)
+    d_out = torch.empty((n, 10), dtype=torch.float32, device="cuda")
+    shifted = torch.empty(4 * n + 2, dtype=torch.float32, device="cuda")  # spheres 8 B off their 16 B boundary
+    shifted[2:] = torch.from_numpy(flat.reshape(-1).copy()).cuda()
+    with pytest.raises(FcpwError):
+        check(lib().fcpwgb_find_closest_points_device(g.handle, shifted.data_ptr() + 8, d_out.data_ptr(), n, 0, None))
+    odd_out = torch.empty(10 * n + 1, dtype=torch.float32, device="cuda")  # records 4 B off their 8 B boundary
+    d_sph = torch.from_numpy(flat.copy()).cuda()
+    with pytest.raises(FcpwError):
+        check(lib().fcpwgb_find_closest_points_device(g.handle, d_sph.data_ptr(), odd_out.data_ptr() + 4, n, 0, None))
+    check(lib().fcpwgb_find_closest_points_device(g.handle, d_sph.data_ptr(), d_out.data_ptr(), n, 0, None))
+    torch.cuda.synchronize()
+    want = d_out.cpu().numpy()
+    h_sph = torch.from_numpy(flat.copy()).pin_memory()
+    pinned = torch.full((n + 1, 10), -7.0, dtype=torch.float32).pin_memory()  # record 1 starts 40 B in: 8 B off 16
+    check(lib().fcpwgb_find_closest_points(g.handle, h_sph.data_ptr(), pinned.data_ptr() + 40, n, 0))
+    got = pinned.numpy()[1:]
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert np.all(pinned.numpy()[0] == -7.0)
+    assert g.check_errors() == 0
